@@ -1,0 +1,117 @@
+"""Seeded synthetic initial states for the fluid step (host-side workload setup).
+
+The reference ships no datasets; its examples build a dam break with a
+``FluidSource`` (examples/simple.cpp:36) or mouse-driven sources
+(examples/opengl_example/FluidInteractionHandler.cpp).  The workloads here are
+dam breaks whose particles are jittered inside their cells by a SplitMix64
+stream, so that every implementation (GPU, oracle, reference) starts from the
+same bytes.  SplitMix64 is used instead of ``std::uniform_real_distribution``
+because the latter is implementation-defined.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+
+import numpy as np
+
+_M64 = (1 << 64) - 1
+
+
+def splitmix64(seed: int, n: int) -> np.ndarray:
+    """n successive SplitMix64 outputs (Steele, Lea & Flood 2014) as uint64."""
+    with np.errstate(over="ignore"):
+        idx = np.arange(1, n + 1, dtype=np.uint64)
+        z = (np.uint64(seed & _M64) + idx * np.uint64(0x9E3779B97F4A7C15))
+        z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+        z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+        z = z ^ (z >> np.uint64(31))
+    return z
+
+
+def uniform01(seed: int, n: int) -> np.ndarray:
+    """n float32 values in [0, 1): the top 24 bits of each SplitMix64 output."""
+    return ((splitmix64(seed, n) >> np.uint64(40)).astype(np.float64) * (2.0 ** -24)).astype(np.float32)
+
+
+@dataclass
+class Scene:
+    """Everything needed to construct and fill one simulation."""
+
+    size_x: int
+    size_y: int
+    length_x: float
+    length_y: float
+    density: float
+    pic_ratio: float
+    dt: float
+    particles: np.ndarray                     # (n, 4) float32 {x, y, vx, vy}
+    solid: np.ndarray | None = None           # (size_y, size_x) uint8 or None
+    gravity: tuple[float, float] = (0.0, -9.82)
+    cg_tolerance: float = 1.1920928955078125e-07
+    cg_max_iterations: int = 100
+    description: str = ""
+    meta: dict = field(default_factory=dict)
+
+    @property
+    def cells(self) -> int:
+        return self.size_x * self.size_y
+
+
+def block_particles(size_x: int, size_y: int, length_x: float, length_y: float, i0: int, i1: int,
+                    j0: int, j1: int, per_cell: int, seed: int,
+                    solid: np.ndarray | None = None) -> np.ndarray:
+    """per_cell jittered particles in each cell of [i0, i1) x [j0, j1), j-major
+    cell order, skipping cells that are solid; positions (i + U, j + U) * delta."""
+    dx = np.float32(np.float32(length_x) / np.float32(size_x))
+    dy = np.float32(np.float32(length_y) / np.float32(size_y))
+    jj, ii = np.meshgrid(np.arange(j0, j1), np.arange(i0, i1), indexing="ij")
+    ii = ii.reshape(-1)
+    jj = jj.reshape(-1)
+    if solid is not None:
+        keep = solid[jj, ii] == 0
+        ii, jj = ii[keep], jj[keep]
+    ncell = ii.size
+    u = uniform01(seed, 2 * per_cell * ncell).reshape(ncell, per_cell, 2)
+    x = (ii[:, None].astype(np.float32) + u[:, :, 0]) * dx
+    y = (jj[:, None].astype(np.float32) + u[:, :, 1]) * dy
+    out = np.zeros((ncell * per_cell, 4), np.float32)
+    out[:, 0] = x.reshape(-1).astype(np.float32)
+    out[:, 1] = y.reshape(-1).astype(np.float32)
+    return out
+
+
+def disc_mask(size_x: int, size_y: int, cx: float, cy: float, radius: float) -> np.ndarray:
+    """uint8 mask of cells whose centre lies within radius (in cells) of (cx, cy)."""
+    jj, ii = np.meshgrid(np.arange(size_y), np.arange(size_x), indexing="ij")
+    d2 = (ii + 0.5 - cx) ** 2 + (jj + 0.5 - cy) ** 2
+    return (d2 <= radius * radius).astype(np.uint8)
+
+
+def dam_break_small(seed: int = 0xC1) -> Scene:
+    """64x64 unit cells, solid border, fluid block over the left 40% x 60%,
+    4 jittered particles per cell, rho = dt = 0.005, FLIP ratio 0.98
+    (pic_ratio 0.02), CG to relative residual 1e-6."""
+    n = 64
+    i1 = int(np.ceil(0.4 * n))
+    j1 = int(np.ceil(0.6 * n))
+    parts = block_particles(n, n, float(n), float(n), 1, i1, 1, j1, 4, seed)
+    return Scene(n, n, float(n), float(n), 0.005, 0.02, 0.005, parts,
+                 cg_tolerance=1e-6, cg_max_iterations=2000,
+                 description="dam break 64x64, 4 particles/cell, CG 1e-6",
+                 meta={"block": [1, i1, 1, j1], "seed": seed})
+
+
+def dam_break_large(n: int = 1024, seed: int = 0xC2) -> Scene:
+    """n x n unit cells with a circular solid obstacle of radius 100 cells
+    (n/1024 scaled) right of a dam-break block sized to ~1.7M particles at
+    n = 1024 (655 x 655 cells x 4), rho = dt = 0.005, FLIP ratio 0.95
+    (pic_ratio 0.05), CG to relative residual 1e-5."""
+    scale = n / 1024.0
+    w = max(2, int(round(655 * scale)))
+    cx, cy, r = 840.0 * scale, 200.0 * scale, 100.0 * scale
+    solid = disc_mask(n, n, cx, cy, r)
+    parts = block_particles(n, n, float(n), float(n), 1, 1 + w, 1, 1 + w, 4, seed, solid)
+    return Scene(n, n, float(n), float(n), 0.005, 0.05, 0.005, parts, solid=solid,
+                 cg_tolerance=1e-5, cg_max_iterations=100000,
+                 description="dam break %dx%d + disc r=%g, 4 particles/cell, CG 1e-5" % (n, n, r),
+                 meta={"block": [1, 1 + w, 1, 1 + w], "disc": [cx, cy, r], "seed": seed})

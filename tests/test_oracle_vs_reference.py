@@ -1,0 +1,103 @@
+"""The C restatement against the reference's own code, run side by side
+(only where the reference checkout exists, i.e. where oracle/_ref builds)."""
+import numpy as np
+import pytest
+
+from fluid_simulation_gb300 import scenes
+from oracle import pyoracle as po
+
+pytestmark = pytest.mark.skipif(not po.reference_available(), reason="reference build unavailable")
+
+
+def _pair(sc, cg_maxit=400):
+    sims = []
+    for kind in ("restatement", "reference"):
+        s = po.OracleSim(kind, sc.size_x, sc.size_y, sc.length_x, sc.length_y, sc.density, sc.pic_ratio)
+        s.set_cg(sc.cg_tolerance, cg_maxit)
+        s.set_particles(sc.particles)
+        sims.append(s)
+    return sims
+
+
+def _same(a, b):
+    sa, sb = a.state(), b.state()
+    for k in sa:
+        assert np.array_equal(sa[k].view(np.uint8), sb[k].view(np.uint8)), k
+
+
+@pytest.mark.parametrize("method", [po.STEP_PICFLIP, po.STEP_PIC, po.STEP_FLIP, po.STEP_SEMI_LAGRANGIAN])
+def test_step_methods(method):
+    sc = scenes.dam_break_small()
+    a, b = _pair(sc)
+    for _ in range(15):
+        assert a.step(method, sc.dt) == 0 and b.step(method, sc.dt) == 0
+    _same(a, b)
+
+
+def test_phase_sequence_equals_stock_step():
+    """The harness's explicit phase sequence equals FluidSolver::stepPICFLIP."""
+    sc = scenes.dam_break_small()
+    a, b = _pair(sc)
+    _, c = _pair(sc)
+    c.set_use_stock(False)
+    for _ in range(10):
+        b.step(po.STEP_PICFLIP, sc.dt)
+        c.step(po.STEP_PICFLIP, sc.dt)
+    _same(b, c)
+
+
+@pytest.mark.parametrize("ph", [po.PH_CLASSIFY, po.PH_P2G, po.PH_SAVE_PREV, po.PH_GRAVITY, po.PH_DIRICHLET,
+                                po.PH_EXTEND, po.PH_PRESSURE, po.PH_SAVE_DIFF, po.PH_G2P_PICFLIP,
+                                po.PH_G2P_PIC, po.PH_G2P_FLIP, po.PH_ADVECT_SAFE, po.PH_ADVECT,
+                                po.PH_SL_VELOCITY, po.PH_SL_PARTICLES])
+def test_single_phase_on_random_state(ph):
+    """Each phase on a randomised mid-simulation state (random velocities,
+    jittered particles incl. negative and out-of-cell positions)."""
+    sc = scenes.dam_break_small()
+    a, b = _pair(sc)
+    for s in (a, b):
+        for _ in range(3):
+            s.step(po.STEP_PICFLIP, sc.dt)
+    rng = np.random.default_rng(ph)
+    grids = {w: rng.standard_normal((sc.size_y, sc.size_x)).astype(np.float32) for w in range(8)}
+    parts = a.particles()
+    parts[:, 2:] = rng.standard_normal((parts.shape[0], 2)).astype(np.float32)
+    if ph == po.PH_PRESSURE:
+        # pressureSolve counts particles without clamping (FluidSolver.cpp:353-360):
+        # a particle outside the grid is undefined behaviour there.
+        parts[:3, 0] = np.array([-0.3, 0.0, 63.99], np.float32)
+    else:
+        parts[:5, 0] = np.array([-0.3, -2.5, 0.0, 63.99, 70.0], np.float32)
+    for s in (a, b):
+        for w, g in grids.items():
+            s.set_grid(w, g)
+        s.set_particles(parts)
+        s.set_pic_ratio(0.3)
+        assert s.phase(ph, sc.dt) == 0
+    _same(a, b)
+
+
+def test_fluid_source_and_obstacle():
+    sc = scenes.dam_break_small()
+    disc = scenes.disc_mask(64, 64, 45.0, 20.0, 8.0)
+    sims = []
+    for kind in ("restatement", "reference"):
+        s = po.OracleSim(kind, 64, 64, 64.0, 64.0, sc.density, sc.pic_ratio)
+        s.set_cg(1e-6, 500)
+        s.set_solid_mask(disc)
+        s.set_gravity(0.0, -9.81)
+        s.add_source(2.0, 10.0, 40.0, 50.0, 1.0, 1.0, 3.0, 0.0, 0.05, 3)
+        sims.append(s)
+    for _ in range(40):
+        for s in sims:
+            s.update(sc.dt)
+            assert s.step(po.STEP_PICFLIP, sc.dt) == 0
+    _same(*sims)
+
+
+def test_non_square_cells_rejected_like_reference():
+    """dx != dy: the solver's pool copy keeps dx for dy, so validate() fails
+    and every step throws in the reference (FluidSolver.cpp:56-62, 215-221)."""
+    for kind in ("restatement", "reference"):
+        s = po.OracleSim(kind, 32, 16, 32.0, 32.0, 0.005, 0.05)
+        assert s.step(po.STEP_PICFLIP, 0.005) == -1
