@@ -1,0 +1,386 @@
+"""Benchmark of the per-step PIC/FLIP + MAC-grid + pressure-projection path.
+
+Workload: the 1024x1024 dam break with a circular solid obstacle (radius 100
+cells), ~1.7M marker particles (4 per fluid cell), FLIP ratio 0.95, rho = dt =
+0.005, Jacobi-PCG to relative residual 1e-5 -- FluidSolver::stepPICFLIP
+(src/FluidSolver.cpp:211-251) per step.  Metric: cell-steps/s (cells x steps /
+device time).  A "step" is one stepPICFLIP of the evolving simulation.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gpu|reference]
+
+--impl gpu (default) prints one JSON line with the device-time throughput
+(`value`), the end-to-end throughput through the C ABI with host particle
+buffers (`e2e`), the CG kernel's roofline, the CPU baseline of the same
+workload and the SM clocks seen during the timed region.  --impl reference
+times the reference's CPU implementation of the path (the reference's own
+sources when built here, else the C restatement of them) on the same
+workload.  Under torchrun (N > 1) every rank runs an independent replica
+(nothing on the data path is exchanged); rank 0 prints.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "cell-steps/s at 1024^2 (CG tol 1e-5)"
+UNIT = "cell-steps/s"
+CG_BYTES_PER_CELL_ITER = 42  # fused Jacobi-PCG: 17 B (SpMV pass) + 25 B (update pass) per fluid cell
+L2_FLUSH_BYTES = 256 << 20
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["gpu", "reference"], default="gpu")
+    ap.add_argument("--size", type=int, default=1024)
+    ap.add_argument("--cpu-budget", type=float, default=150.0, help="seconds of CPU work for CPU timings")
+    return ap.parse_args()
+
+
+def workload(size):
+    from fluid_simulation_gb300 import scenes
+
+    return scenes.dam_break_large(size)
+
+
+def config_of(sc, extra=None):
+    c = {"workload": "dam break %dx%d, solid disc r=%g cells, %d particles (4/fluid cell), FLIP 0.95, "
+                     "rho=dt=0.005, Jacobi-PCG rel. residual 1e-5, stepPICFLIP"
+                     % (sc.size_x, sc.size_y, sc.meta["disc"][2], sc.particles.shape[0]),
+         "cells": sc.cells, "particles": int(sc.particles.shape[0]), "dt": sc.dt,
+         "cg_tolerance": sc.cg_tolerance, "method": "stepPICFLIP"}
+    if extra:
+        c.update(extra)
+    return c
+
+
+# ---------------------------------------------------------------- clocks
+class ClockSampler:
+    """nvidia-smi clock / throttle-reason samples every 200 ms while running."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "--query-gpu=" + self.Q, "--format=csv,noheader,nounits",
+                                          "-lms", "200", "-i", str(self.gpu)], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.t.join(timeout=2)
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------------- CPU timings
+def cpu_oracle_kind():
+    from oracle import pyoracle as po
+
+    return "reference" if po.reference_available() else "restatement"
+
+
+def cpu_sim_from_state(sc, kind, grids, particles):
+    from oracle import pyoracle as po
+
+    o = po.OracleSim(kind, sc.size_x, sc.size_y, sc.length_x, sc.length_y, sc.density, sc.pic_ratio)
+    o.set_cg(sc.cg_tolerance, sc.cg_max_iterations)
+    o.set_use_stock(False)
+    if sc.solid is not None:
+        o.set_solid_mask(sc.solid)
+    for w, g in enumerate(grids):
+        o.set_grid(w, g)
+    o.set_particles(particles)
+    return o
+
+
+def time_cpu_steps(o, sc, max_steps, budget_s):
+    from oracle import pyoracle as po
+
+    times = []
+    t_all = time.perf_counter()
+    while len(times) < max_steps:
+        t0 = time.perf_counter()
+        rc = o.step(po.STEP_PICFLIP, sc.dt)
+        times.append(time.perf_counter() - t0)
+        assert rc == 0
+        if time.perf_counter() - t_all > budget_s:
+            break
+    return times
+
+
+def run_reference(args, rank):
+    """--impl reference: the reference's CPU implementation on the same workload."""
+    if rank != 0:
+        return
+    from oracle import build_oracle
+
+    build_oracle.build_restatement()
+    build_oracle.build_reference()
+    kind = cpu_oracle_kind()
+    sc = workload(args.size)
+    from oracle import pyoracle as po
+
+    o = po.OracleSim(kind, sc.size_x, sc.size_y, sc.length_x, sc.length_y, sc.density, sc.pic_ratio)
+    o.set_cg(sc.cg_tolerance, sc.cg_max_iterations)
+    if sc.solid is not None:
+        o.set_solid_mask(sc.solid)
+    o.set_particles(sc.particles)
+    budget = args.cpu_budget
+    t0 = time.perf_counter()
+    warm = 0
+    for _ in range(args.warmup):
+        if time.perf_counter() - t0 > budget / 3:
+            break
+        o.step(po.STEP_PICFLIP, sc.dt)
+        warm += 1
+    times = time_cpu_steps(o, sc, args.steps, budget - (time.perf_counter() - t0))
+    total = sum(times)
+    value = sc.cells * len(times) / total
+    sample = ("steps %d..%d of the workload from its initial state (%d warm-up steps run), single thread"
+              % (warm + 1, warm + len(times), warm))
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": len(times), "warmup": warm, "ms_per_step": 1000 * total / len(times),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded SplitMix64 dam break)",
+            "config": config_of(sc, {"implementation": "reference C++ sources + Eigen-subset stand-in"
+                                     if kind == "reference" else "C restatement of the reference (port)"}),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1,
+                             "kind": "reference" if kind == "reference" else "port", "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------- GPU arm
+def read_traffic():
+    """DRAM bytes per CG launch from the committed ncu summary, if any."""
+    p = os.path.join(ROOT, "profiles", "k_cg_dam_break_1024.md")
+    if not os.path.exists(p):
+        return None
+    for ln in open(p):
+        if ln.startswith("traffic_bytes_per_launch:"):
+            try:
+                return float(ln.split(":", 1)[1].strip())
+            except ValueError:
+                return None
+    return None
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        try:
+            d = json.load(open(p))
+            return float(d["hbm_gbs"]), "measured"
+        except Exception:
+            pass
+    return 6800.0, "fallback"
+
+
+def run_gpu(args, rank, world, local_rank):
+    import torch
+
+    import fluid_simulation_gb300 as fsg
+    from fluid_simulation_gb300 import build as fsbuild
+
+    if rank == 0 or not os.path.exists(fsg.library_path()):
+        fsbuild.build()
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+    torch.cuda.set_device(local_rank)
+    sc = workload(args.size)
+    sim = fsg.FluidSim.from_scene(sc, device=local_rank)
+    stream = torch.cuda.ExternalStream(sim.stream(), device=local_rank)
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda:%d" % local_rank)
+
+    for _ in range(args.warmup):
+        sim.step(fsg.STEP_PICFLIP, sc.dt)
+    sim.synchronize()
+    # state at the start of the timed region, for the CPU baseline sample
+    grids0 = [sim.grid(w) for w in range(8)] if rank == 0 else None
+    parts0 = sim.particles() if rank == 0 else None
+
+    sim.set_timing(True)
+    sim.step(fsg.STEP_PICFLIP, sc.dt)  # records the timed graph variant; not counted
+    sim.synchronize()
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+    torch.cuda.synchronize()
+    step_ms, cg_ms, fi, iters, phases = [], [], 0, [], {k: 0.0 for k in fsg.TIMED_PHASES}
+    launches0 = sim.kernel_launches()
+    with ClockSampler(local_rank) as clk:
+        for _ in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.zero_()
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+            sim.step(fsg.STEP_PICFLIP, sc.dt)
+            e1.record(stream)
+            st = sim.stats()  # synchronises; outside the events
+            step_ms.append(e0.elapsed_time(e1))
+            cg_ms.append(st["ms_phase"]["cg"])
+            for k, v in st["ms_phase"].items():
+                phases[k] += v
+            fi += st["n_fluid"] * st["cg_iterations"]
+            iters.append(st["cg_iterations"])
+    launches = sim.kernel_launches() - launches0
+    torch.cuda.synchronize()
+    t_dev = sum(step_ms) / 1000.0
+    if world > 1:
+        import torch.distributed as dist
+
+        t = torch.tensor([t_dev], dtype=torch.float64, device="cuda:%d" % local_rank)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_dev = float(t.item())
+    value = sc.cells * args.steps * world / t_dev
+
+    # end to end through the C ABI with host (pinned) particle buffers
+    sim.set_timing(False)
+    n = sim.num_particles()
+    host_in = torch.empty((n, 4), dtype=torch.float32, pin_memory=True).numpy()
+    host_out = torch.empty((n, 4), dtype=torch.float32, pin_memory=True).numpy()
+    host_in[:] = sim.particles()
+    e2e_steps = max(3, args.steps // 2)
+    sim.set_particles(host_in)
+    sim.step(fsg.STEP_PICFLIP, sc.dt)  # graph for this configuration
+    sim.synchronize()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        sim.set_particles(host_in)
+        sim.step(fsg.STEP_PICFLIP, sc.dt)
+        sim.lib.fs_get_particles(sim.h, host_out.ctypes.data, n)
+        host_in, host_out = host_out, host_in
+    sim.synchronize()
+    t_e2e = time.perf_counter() - t0
+    if world > 1:
+        import torch.distributed as dist
+
+        t = torch.tensor([t_e2e], dtype=torch.float64, device="cuda:%d" % local_rank)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_e2e = float(t.item())
+    e2e_value = sc.cells * e2e_steps * world / t_e2e
+
+    if rank != 0:
+        return
+    # roofline of the dominant kernel (the CG)
+    peak, peak_kind = peaks()
+    cg_s = sum(cg_ms) / 1000.0
+    achieved = CG_BYTES_PER_CELL_ITER * fi / cg_s / 1e9 if cg_s > 0 else None
+    traffic = read_traffic()
+    # CPU baseline: the oracle on the state at the start of the timed region
+    kind = cpu_oracle_kind()
+    o = cpu_sim_from_state(sc, kind, grids0, parts0)
+    ctimes = time_cpu_steps(o, sc, 1, args.cpu_budget)
+    cpu_value = sc.cells * len(ctimes) / sum(ctimes)
+    clocks = clk.summary()
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1000.0 * t_dev / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 (CG dot products f64)",
+        "data": "synthetic (seeded SplitMix64 dam break)",
+        "config": config_of(sc, {"parallelism": "replicas" if world > 1 else "single GPU",
+                                 "l2": "256 MiB written before every timed step; the step's CUDA events exclude it",
+                                 "cg_iterations_mean": float(np.mean(iters)), "cg_iterations": iters}),
+        "phases_ms_per_step": {k: v / args.steps for k, v in phases.items()},
+        "gpu_launches": int(launches),
+        "e2e": {"value": e2e_value, "unit": UNIT, "steps": e2e_steps,
+                "h2d_bytes_per_step": int(n * 16), "d2h_bytes_per_step": int(n * 16),
+                "path": "fs_set_particles (pinned host) + fs_step + fs_get_particles (pinned host)"},
+        "roofline": {"kernel": "k_cg (persistent Jacobi-PCG)", "bound": "hbm", "achieved": achieved,
+                     "peak": peak, "peak_source": peak_kind, "unit": "GB/s",
+                     "frac": (achieved / peak) if achieved else None, "traffic": traffic,
+                     "algorithmic_bytes": "%d B per fluid cell per CG iteration x sum(F x I) = %d B"
+                                          % (CG_BYTES_PER_CELL_ITER, CG_BYTES_PER_CELL_ITER * fi),
+                     "cg_ms_per_step": 1000.0 * cg_s / args.steps},
+        "cpu_baseline": {"value": cpu_value, "unit": UNIT, "cores": 1,
+                         "kind": "reference" if kind == "reference" else "port",
+                         "sample": "1 stepPICFLIP of the same workload from the GPU state at the start of "
+                                   "the timed region (%.1f s), single thread" % sum(ctimes)},
+        "clocks": clocks,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        dist.init_process_group(backend=backend)
+    try:
+        if args.impl == "reference":
+            run_reference(args, rank)
+        else:
+            run_gpu(args, rank, world, local_rank)
+    finally:
+        if world > 1:
+            import torch.distributed as dist
+
+            dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

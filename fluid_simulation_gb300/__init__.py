@@ -1,0 +1,281 @@
+"""fluid_simulation_gb300: GB300 (sm_103a) implementation of Fluid_Simulation's
+per-step PIC/FLIP + MAC-grid + pressure-projection path.
+
+The product is the CUDA library ``_build/libfsgpu.so`` behind the C ABI of
+``include/fsgpu.h`` and the C++ drop-in classes in ``dropin/``.  This module is
+the Python front end of that C ABI (ctypes), used by the tests and bench.py.
+There is no CPU fallback: without the built library every call raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "_build", "libfsgpu.so")
+
+# Constants of include/fsgpu.h
+FS_OK = 0
+STATUS_NAMES = {0: "FS_OK", 1: "FS_ERR_INVALID_ARGUMENT", 2: "FS_ERR_VALIDATE", 3: "FS_ERR_CUDA",
+                4: "FS_ERR_TIMEOUT", 5: "FS_ERR_TOO_LARGE", 6: "FS_ERR_INTERNAL", 7: "FS_ERR_OUT_OF_MEMORY"}
+FS_WARN_PARTICLE_OUTSIDE = 1
+FS_WARN_CG_NOT_CONVERGED = 2
+U_FRONT, V_FRONT, U_BACK, V_BACK, U_PREV, V_PREV, U_DIFF, V_DIFF = range(8)
+STEP_SEMI_LAGRANGIAN, STEP_PIC, STEP_FLIP, STEP_PICFLIP = range(4)
+(PH_CLASSIFY, PH_P2G, PH_SAVE_PREV, PH_GRAVITY, PH_DIRICHLET, PH_EXTEND, PH_PRESSURE, PH_SAVE_DIFF,
+ PH_G2P_PICFLIP, PH_G2P_PIC, PH_G2P_FLIP, PH_ADVECT_SAFE, PH_ADVECT, PH_SL_VELOCITY, PH_SL_PARTICLES,
+ PH_SWAP) = range(16)
+TIMED_PHASES = ("classify", "p2g", "forces", "assembly", "cg", "project", "g2p")
+
+
+class FsError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__("%s: %s" % (STATUS_NAMES.get(code, code), msg))
+        self.code = code
+
+
+class fs_config(C.Structure):
+    _fields_ = [("size_x", C.c_int), ("size_y", C.c_int), ("length_x", C.c_float), ("length_y", C.c_float),
+                ("density", C.c_float), ("pic_ratio", C.c_float), ("gravity_x", C.c_float),
+                ("gravity_y", C.c_float), ("cg_max_iterations", C.c_int), ("cg_tolerance", C.c_double),
+                ("extension_iterations", C.c_int), ("device", C.c_int), ("reserved", C.c_int * 8)]
+
+
+class fs_step_stats(C.Structure):
+    _fields_ = [("cg_iterations", C.c_int), ("n_fluid", C.c_int), ("cg_residual", C.c_double),
+                ("warnings", C.c_uint), ("ms_total", C.c_float), ("ms_phase", C.c_float * 7)]
+
+
+# Every function include/fsgpu.h declares, with its ctypes signature.
+_vp, _i, _f, _d, _i64 = C.c_void_p, C.c_int, C.c_float, C.c_double, C.c_int64
+SIGNATURES = {
+    "fs_config_init": (None, [C.POINTER(fs_config), _i, _i]),
+    "fs_create": (_i, [C.POINTER(fs_config), C.POINTER(_vp)]),
+    "fs_destroy": (_i, [_vp]),
+    "fs_last_error": (C.c_char_p, [_vp]),
+    "fs_set_pic_ratio": (_i, [_vp, _f]),
+    "fs_set_gravity": (_i, [_vp, _f, _f]),
+    "fs_set_cg": (_i, [_vp, _d, _i]),
+    "fs_set_extension_iterations": (_i, [_vp, _i]),
+    "fs_set_solid_mask": (_i, [_vp, _vp]),
+    "fs_set_particles": (_i, [_vp, _vp, _i64]),
+    "fs_set_particles_device": (_i, [_vp, _vp, _i64]),
+    "fs_add_particles": (_i, [_vp, _vp, _i64]),
+    "fs_num_particles": (_i, [_vp, C.POINTER(_i64)]),
+    "fs_get_particles": (_i, [_vp, _vp, _i64]),
+    "fs_get_particles_device": (_i, [_vp, _vp, _i64]),
+    "fs_get_grid": (_i, [_vp, _i, _vp]),
+    "fs_set_grid": (_i, [_vp, _i, _vp]),
+    "fs_get_labels": (_i, [_vp, _vp]),
+    "fs_set_labels": (_i, [_vp, _vp]),
+    "fs_get_fluid_indices": (_i, [_vp, _vp]),
+    "fs_get_particle_counts": (_i, [_vp, _vp]),
+    "fs_get_pressure": (_i, [_vp, _vp]),
+    "fs_step": (_i, [_vp, _i, _f]),
+    "fs_phase": (_i, [_vp, _i, _f]),
+    "fs_synchronize": (_i, [_vp]),
+    "fs_get_stats": (_i, [_vp, C.POINTER(fs_step_stats)]),
+    "fs_set_timing": (_i, [_vp, _i]),
+    "fs_set_graphs": (_i, [_vp, _i]),
+    "fs_get_stream": (_vp, [_vp]),
+    "fs_set_stream": (_i, [_vp, _vp]),
+    "fs_kernel_launches": (_i64, [_vp]),
+}
+
+_LIB: C.CDLL | None = None
+
+
+def library_path() -> str:
+    return LIB_PATH
+
+
+def load_library(path: str | None = None) -> C.CDLL:
+    """Loads libfsgpu.so (built by fluid_simulation_gb300/build.py); raises if absent."""
+    global _LIB
+    if _LIB is not None and path is None:
+        return _LIB
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise RuntimeError("libfsgpu.so is not built (%s); run fluid_simulation_gb300/build.py" % p)
+    lib = C.CDLL(p)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    if path is None:
+        _LIB = lib
+    return lib
+
+
+def _ptr(a: np.ndarray) -> int:
+    return a.ctypes.data
+
+
+class FluidSim:
+    """One FluidDomain + FluidSolver pair on the GPU (a C-ABI handle)."""
+
+    def __init__(self, size_x: int, size_y: int, length_x: float, length_y: float, density: float,
+                 pic_ratio: float, device: int = 0, cg_tolerance: float | None = None,
+                 cg_max_iterations: int | None = None, gravity: tuple[float, float] | None = None,
+                 extension_iterations: int | None = None):
+        self.lib = load_library()
+        cfg = fs_config()
+        self.lib.fs_config_init(C.byref(cfg), size_x, size_y)
+        cfg.length_x, cfg.length_y = length_x, length_y
+        cfg.density, cfg.pic_ratio, cfg.device = density, pic_ratio, device
+        if cg_tolerance is not None:
+            cfg.cg_tolerance = cg_tolerance
+        if cg_max_iterations is not None:
+            cfg.cg_max_iterations = cg_max_iterations
+        if gravity is not None:
+            cfg.gravity_x, cfg.gravity_y = gravity
+        if extension_iterations is not None:
+            cfg.extension_iterations = extension_iterations
+        h = C.c_void_p()
+        rc = self.lib.fs_create(C.byref(cfg), C.byref(h))
+        if rc != FS_OK:
+            raise FsError(rc, self.lib.fs_last_error(None).decode())
+        self.h = h
+        self.nx, self.ny = size_x, size_y
+
+    @classmethod
+    def from_scene(cls, sc, device: int = 0) -> "FluidSim":
+        sim = cls(sc.size_x, sc.size_y, sc.length_x, sc.length_y, sc.density, sc.pic_ratio, device,
+                  cg_tolerance=sc.cg_tolerance, cg_max_iterations=sc.cg_max_iterations, gravity=sc.gravity)
+        if sc.solid is not None:
+            sim.set_solid_mask(sc.solid)
+        sim.set_particles(sc.particles)
+        return sim
+
+    def _check(self, rc: int) -> None:
+        if rc != FS_OK:
+            raise FsError(rc, self.lib.fs_last_error(self.h).decode())
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            self.lib.fs_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # settings
+    def set_cg(self, tol: float, maxit: int) -> None:
+        self._check(self.lib.fs_set_cg(self.h, float(tol), int(maxit)))
+
+    def set_gravity(self, gx: float, gy: float) -> None:
+        self._check(self.lib.fs_set_gravity(self.h, gx, gy))
+
+    def set_extension_iterations(self, n: int) -> None:
+        self._check(self.lib.fs_set_extension_iterations(self.h, n))
+
+    def set_pic_ratio(self, r: float) -> None:
+        self._check(self.lib.fs_set_pic_ratio(self.h, r))
+
+    def set_solid_mask(self, mask: np.ndarray | None) -> None:
+        if mask is None:
+            self._check(self.lib.fs_set_solid_mask(self.h, None))
+        else:
+            m = np.ascontiguousarray(mask, dtype=np.uint8).reshape(-1)
+            assert m.size == self.nx * self.ny
+            self._check(self.lib.fs_set_solid_mask(self.h, _ptr(m)))
+
+    def set_timing(self, on: bool) -> None:
+        self._check(self.lib.fs_set_timing(self.h, int(on)))
+
+    def set_graphs(self, on: bool) -> None:
+        self._check(self.lib.fs_set_graphs(self.h, int(on)))
+
+    # particles
+    def set_particles(self, xyuv: np.ndarray) -> None:
+        a = np.ascontiguousarray(xyuv, dtype=np.float32).reshape(-1, 4)
+        self._check(self.lib.fs_set_particles(self.h, _ptr(a), a.shape[0]))
+
+    def add_particles(self, xyuv: np.ndarray) -> None:
+        a = np.ascontiguousarray(xyuv, dtype=np.float32).reshape(-1, 4)
+        self._check(self.lib.fs_add_particles(self.h, _ptr(a), a.shape[0]))
+
+    def num_particles(self) -> int:
+        n = C.c_int64()
+        self._check(self.lib.fs_num_particles(self.h, C.byref(n)))
+        return n.value
+
+    def particles(self) -> np.ndarray:
+        n = self.num_particles()
+        out = np.empty((n, 4), np.float32)
+        self._check(self.lib.fs_get_particles(self.h, _ptr(out), n))
+        return out
+
+    # grids
+    def grid(self, which: int) -> np.ndarray:
+        out = np.empty((self.ny, self.nx), np.float32)
+        self._check(self.lib.fs_get_grid(self.h, which, _ptr(out)))
+        return out
+
+    def set_grid(self, which: int, g: np.ndarray) -> None:
+        a = np.ascontiguousarray(g, dtype=np.float32).reshape(self.ny, self.nx)
+        self._check(self.lib.fs_set_grid(self.h, which, _ptr(a)))
+
+    def labels(self) -> np.ndarray:
+        out = np.empty((self.ny, self.nx), np.uint8)
+        self._check(self.lib.fs_get_labels(self.h, _ptr(out)))
+        return out
+
+    def set_labels(self, lab: np.ndarray) -> None:
+        a = np.ascontiguousarray(lab, dtype=np.uint8).reshape(self.ny, self.nx)
+        self._check(self.lib.fs_set_labels(self.h, _ptr(a)))
+
+    def fluid_indices(self) -> np.ndarray:
+        out = np.empty((self.ny, self.nx), np.int32)
+        self._check(self.lib.fs_get_fluid_indices(self.h, _ptr(out)))
+        return out
+
+    def particle_counts(self) -> np.ndarray:
+        out = np.empty((self.ny, self.nx), np.uint8)
+        self._check(self.lib.fs_get_particle_counts(self.h, _ptr(out)))
+        return out
+
+    def pressure(self) -> np.ndarray:
+        out = np.empty((self.ny, self.nx), np.float32)
+        self._check(self.lib.fs_get_pressure(self.h, _ptr(out)))
+        return out
+
+    # stepping
+    def step(self, method: int, dt: float) -> None:
+        self._check(self.lib.fs_step(self.h, method, dt))
+
+    def phase(self, ph: int, dt: float = 0.0) -> None:
+        self._check(self.lib.fs_phase(self.h, ph, dt))
+
+    def synchronize(self) -> None:
+        self._check(self.lib.fs_synchronize(self.h))
+
+    def stats(self) -> dict:
+        s = fs_step_stats()
+        self._check(self.lib.fs_get_stats(self.h, C.byref(s)))
+        return {"cg_iterations": s.cg_iterations, "n_fluid": s.n_fluid, "cg_residual": s.cg_residual,
+                "warnings": s.warnings, "ms_total": s.ms_total,
+                "ms_phase": dict(zip(TIMED_PHASES, list(s.ms_phase)))}
+
+    def stream(self) -> int:
+        return self.lib.fs_get_stream(self.h) or 0
+
+    def kernel_launches(self) -> int:
+        return self.lib.fs_kernel_launches(self.h)
+
+    def state(self) -> dict[str, np.ndarray]:
+        s = {name: self.grid(w) for name, w in (("u_front", U_FRONT), ("v_front", V_FRONT),
+                                                 ("u_back", U_BACK), ("v_back", V_BACK),
+                                                 ("u_prev", U_PREV), ("v_prev", V_PREV),
+                                                 ("u_diff", U_DIFF), ("v_diff", V_DIFF))}
+        s["labels"] = self.labels()
+        s["fluid_indices"] = self.fluid_indices()
+        s["particle_counts"] = self.particle_counts()
+        s["pressure"] = self.pressure()
+        s["particles"] = self.particles()
+        return s

@@ -1,0 +1,957 @@
+// C ABI (include/fsgpu.h): one handle = one FluidDomain + FluidSolver pair
+// resident in device memory, stepped by the kernels of this library on the
+// handle's CUDA stream.  A whole step is recorded once into a CUDA graph (per
+// method, dt, buffer parity and particle count) and replayed afterwards.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "fs_internal.h"
+
+using namespace fs;
+
+namespace {
+
+thread_local std::string g_create_error;
+
+struct GraphEntry
+{
+    int method;
+    uint32_t dt_bits;
+    int front_in, vfront_in;
+    int front_out, vfront_out;
+    int64_t n_part;
+    bool timing;
+    int64_t kernels;
+    cudaGraphExec_t exec;
+};
+
+uint32_t float_bits(float f)
+{
+    uint32_t b;
+    std::memcpy(&b, &f, 4);
+    return b;
+}
+
+}  // namespace
+
+struct fs_handle
+{
+    fs_config cfg{};
+    Geom g{};
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    int64_t ncell = 0;
+
+    int front = 0, vfront = 0;
+    float* u[2] = {nullptr, nullptr};
+    float* v[2] = {nullptr, nullptr};
+    float *u_prev = nullptr, *v_prev = nullptr, *u_diff = nullptr, *v_diff = nullptr;
+    uint8_t* labels = nullptr;
+    uint8_t* solid = nullptr;
+    uint8_t* vmx[2] = {nullptr, nullptr};
+    uint8_t* vmy[2] = {nullptr, nullptr};
+    int32_t *fidx = nullptr, *cell_of = nullptr, *counts32 = nullptr;
+    uint8_t* counts8 = nullptr;
+    float* acc[4] = {nullptr, nullptr, nullptr, nullptr};
+    float* grid_tmp = nullptr;
+
+    // semi-Lagrangian face scratch (allocated on first use)
+    float* sl[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    uint8_t* sl_ok[2] = {nullptr, nullptr};
+
+    // particles (SoA)
+    float *px = nullptr, *py = nullptr, *pvx = nullptr, *pvy = nullptr;
+    float *yu = nullptr, *xv = nullptr;
+    float* staging = nullptr;  // AoS staging, 4 * cap floats
+    int64_t n_part = 0, cap_part = 0;
+
+    SplatWork sw{};
+    int64_t sw_items = 0;
+
+    // pressure solve
+    CgWork cg{};
+    float* cg_b = nullptr;
+    int32_t *cg_down = nullptr, *cg_up = nullptr;
+    uint8_t* cg_flags = nullptr;
+    int32_t* d_nfluid = nullptr;
+    unsigned* d_status = nullptr;
+    unsigned* d_warn = nullptr;
+    int32_t* scan_tmp = nullptr;
+    float diag_tab[5]{};
+    float off = 0.0f;
+
+    float pic = 0.0f;
+    float gx = 0.0f, gy = -9.82f;
+    double cg_tol = 0.0;
+    int cg_maxit = 100;
+    int n_ext = 2;
+
+    bool timing = false;
+    bool graphs = true;
+    bool timed_valid = false;
+    cudaEvent_t ev[FS_NUM_TIMED + 1] = {};
+    int64_t launches = 0;
+    std::vector<GraphEntry> graph_cache;
+    std::string err;
+
+    Launch L() { return Launch{stream, &launches, 0}; }
+};
+
+namespace {
+
+int fail(fs_handle* h, int code, const std::string& msg)
+{
+    if (h) h->err = msg;
+    return code;
+}
+
+int cuda_fail(fs_handle* h, cudaError_t e, const char* what)
+{
+    return fail(h, e == cudaErrorMemoryAllocation ? FS_ERR_OUT_OF_MEMORY : FS_ERR_CUDA,
+                std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+template <class T>
+cudaError_t dalloc(T** p, size_t count)
+{
+    *p = nullptr;
+    if (count == 0) count = 1;
+    return cudaMalloc((void**)p, count * sizeof(T));
+}
+
+void clear_graphs(fs_handle* h)
+{
+    for (auto& e : h->graph_cache) cudaGraphExecDestroy(e.exec);
+    h->graph_cache.clear();
+}
+
+cudaError_t ensure_splat_capacity(fs_handle* h, int64_t items)
+{
+    if (items <= h->sw_items) return cudaSuccess;
+    SplatWork& w = h->sw;
+    cudaFree(w.keys_a);
+    cudaFree(w.keys_b);
+    cudaFree(w.vals_a);
+    cudaFree(w.vals_b);
+    cudaFree(w.hist);
+    cudaFree(w.hist_scan);
+    cudaFree(w.scan_tmp);
+    w.keys_a = w.keys_b = nullptr;
+    w.vals_a = w.vals_b = w.hist = w.hist_scan = w.scan_tmp = nullptr;
+    h->sw_items = 0;
+    const size_t hist = splat_hist_ints(items);
+    const size_t hscan = std::max(hist, (size_t)h->ncell + 2);
+    cudaError_t e;
+    if ((e = dalloc(&w.keys_a, (size_t)items)) != cudaSuccess) return e;
+    if ((e = dalloc(&w.keys_b, (size_t)items)) != cudaSuccess) return e;
+    if ((e = dalloc(&w.vals_a, (size_t)items)) != cudaSuccess) return e;
+    if ((e = dalloc(&w.vals_b, (size_t)items)) != cudaSuccess) return e;
+    if ((e = dalloc(&w.hist, hist)) != cudaSuccess) return e;
+    if ((e = dalloc(&w.hist_scan, hscan)) != cudaSuccess) return e;
+    if ((e = dalloc(&w.scan_tmp, scan_tmp_ints((int64_t)hscan))) != cudaSuccess) return e;
+    w.cap_items = items;
+    h->sw_items = items;
+    clear_graphs(h);
+    return cudaSuccess;
+}
+
+cudaError_t ensure_particle_capacity(fs_handle* h, int64_t n)
+{
+    if (n <= h->cap_part) return cudaSuccess;
+    int64_t cap = h->cap_part ? h->cap_part : 4096;
+    while (cap < n) cap *= 2;
+    float* np[7] = {};
+    cudaError_t e = cudaSuccess;
+    for (int k = 0; k < 6 && e == cudaSuccess; ++k) e = dalloc(&np[k], (size_t)cap);
+    if (e == cudaSuccess) e = dalloc(&np[6], (size_t)cap * 4);
+    if (e != cudaSuccess) {
+        for (float* p : np) cudaFree(p);
+        return e;
+    }
+    if (h->n_part > 0) {
+        const size_t bytes = sizeof(float) * (size_t)h->n_part;
+        cudaMemcpyAsync(np[0], h->px, bytes, cudaMemcpyDeviceToDevice, h->stream);
+        cudaMemcpyAsync(np[1], h->py, bytes, cudaMemcpyDeviceToDevice, h->stream);
+        cudaMemcpyAsync(np[2], h->pvx, bytes, cudaMemcpyDeviceToDevice, h->stream);
+        cudaMemcpyAsync(np[3], h->pvy, bytes, cudaMemcpyDeviceToDevice, h->stream);
+    }
+    cudaStreamSynchronize(h->stream);
+    cudaFree(h->px);
+    cudaFree(h->py);
+    cudaFree(h->pvx);
+    cudaFree(h->pvy);
+    cudaFree(h->yu);
+    cudaFree(h->xv);
+    cudaFree(h->staging);
+    h->px = np[0];
+    h->py = np[1];
+    h->pvx = np[2];
+    h->pvy = np[3];
+    h->yu = np[4];
+    h->xv = np[5];
+    h->staging = np[6];
+    h->cap_part = cap;
+    clear_graphs(h);
+    return ensure_splat_capacity(h, std::max<int64_t>(cap, h->ncell));
+}
+
+cudaError_t ensure_sl_scratch(fs_handle* h)
+{
+    if (h->sl[0]) return cudaSuccess;
+    cudaError_t e;
+    for (int k = 0; k < 6; ++k)
+        if ((e = dalloc(&h->sl[k], (size_t)h->ncell)) != cudaSuccess) return e;
+    for (int k = 0; k < 2; ++k)
+        if ((e = dalloc(&h->sl_ok[k], (size_t)h->ncell)) != cudaSuccess) return e;
+    return ensure_splat_capacity(h, std::max<int64_t>(h->cap_part, h->ncell));
+}
+
+float* UF(fs_handle* h) { return h->u[h->front]; }
+float* VF(fs_handle* h) { return h->v[h->front]; }
+float* UB(fs_handle* h) { return h->u[1 - h->front]; }
+float* VB(fs_handle* h) { return h->v[1 - h->front]; }
+
+void mark(fs_handle* h, int k)
+{
+    if (h->timing) cudaEventRecord(h->ev[k], h->stream);
+}
+
+// ---- phases (enqueue only) --------------------------------------------------
+
+void ph_classify(fs_handle* h)
+{
+    const Launch L = h->L();
+    labels_clear(L, h->g, h->labels);
+    labels_from_particles(L, h->g, h->px, h->py, h->n_part, h->labels);
+    labels_finalize(L, h->g, h->labels, h->solid);
+}
+
+void ph_p2g(fs_handle* h)
+{
+    const Launch L = h->L();
+    const Geom& g = h->g;
+    p2g_positions(L, g, h->px, h->py, h->n_part, h->yu, h->xv);
+    const float* vu[2] = {h->pvx, nullptr};
+    float* ou[2] = {h->acc[0], h->acc[1]};
+    ordered_splat(L, g, g.pdx, g.pdy, h->n_part, h->px, h->yu, nullptr, 2, vu, ou, h->sw);
+    const float* vv[2] = {h->pvy, nullptr};
+    float* ov[2] = {h->acc[2], h->acc[3]};
+    ordered_splat(L, g, g.pdx, g.pdy, h->n_part, h->xv, h->py, nullptr, 2, vv, ov, h->sw);
+    p2g_finish(L, g, h->acc[0], h->acc[1], h->acc[2], h->acc[3], UB(h), VB(h));
+    h->front ^= 1;
+}
+
+void ph_save_prev(fs_handle* h) { grid_copy2(h->L(), h->g, UF(h), VF(h), h->u_prev, h->v_prev); }
+void ph_save_diff(fs_handle* h) { grid_diff(h->L(), h->g, UF(h), VF(h), h->u_prev, h->v_prev, h->u_diff, h->v_diff); }
+
+void ph_gravity(fs_handle* h, float dt)
+{
+    const float ax = h->gx * dt, ay = h->gy * dt;  // a * dt in float, as FluidSolver.cpp:289-291
+    gravity(h->L(), h->g, h->labels, UF(h), VF(h), ax, ay);
+}
+
+void ph_dirichlet(fs_handle* h) { dirichlet(h->L(), h->g, h->labels, UF(h), VF(h)); }
+
+void ph_extend(fs_handle* h)
+{
+    const Launch L = h->L();
+    extend_init(L, h->g, h->labels, UF(h), VF(h), UB(h), VB(h), h->vmx[h->vfront], h->vmx[1 - h->vfront],
+                h->vmy[h->vfront], h->vmy[1 - h->vfront]);
+    for (int it = 0; it < h->n_ext; ++it) {
+        extend_sweep(L, h->g, h->labels, UB(h), VB(h), h->vmx[h->vfront], h->vmx[1 - h->vfront], h->vmy[h->vfront],
+                     h->vmy[1 - h->vfront]);
+        h->vfront ^= 1;
+    }
+    h->front ^= 1;
+}
+
+void ph_pressure(fs_handle* h, float dt)
+{
+    const Launch L = h->L();
+    const Geom& g = h->g;
+    count_particles(L, g, h->px, h->py, h->n_part, h->counts32, h->d_warn);
+    fluid_index(L, h->labels, h->ncell, h->fidx, h->cell_of, h->d_nfluid, h->scan_tmp);
+    assemble(L, g, h->labels, h->fidx, h->cell_of, h->d_nfluid, UF(h), VF(h), h->cg_b, h->cg_down, h->cg_up,
+             h->cg_flags, h->counts32, h->counts8);
+    mark(h, FS_T_CG);
+    cg_solve(L, h->cg, h->d_nfluid, h->cg_b, h->diag_tab, h->cg_down, h->cg_up, h->cg_flags, h->off, h->cg_tol,
+             h->cg_maxit, h->d_status);
+    mark(h, FS_T_PROJECT);
+    const float dt_over_rho = dt / h->cfg.density;  // FluidSolver.cpp:471-474: (dt / density) first
+    project(L, g, h->fidx, h->d_nfluid, h->cg.x, UF(h), VF(h), UB(h), VB(h), dt_over_rho);
+    h->front ^= 1;
+}
+
+void ph_g2p(fs_handle* h, int g2p, int adv, float dt)
+{
+    g2p_advect(h->L(), h->g, g2p, adv, h->px, h->py, h->pvx, h->pvy, h->n_part, UF(h), VF(h), h->u_diff, h->v_diff,
+               h->labels, h->pic, dt);
+}
+
+void ph_sl_velocity(fs_handle* h, float dt)
+{
+    const Launch L = h->L();
+    const Geom& g = h->g;
+    sl_faces(L, g, h->labels, UF(h), VF(h), dt, h->sl[0], h->sl[1], h->sl[2], h->sl_ok[0], h->sl[3], h->sl[4],
+             h->sl[5], h->sl_ok[1]);
+    const float* vu[1] = {h->sl[2]};
+    float* ou[1] = {UB(h)};
+    ordered_splat(L, g, g.dx, g.dy, h->ncell, h->sl[0], h->sl[1], h->sl_ok[0], 1, vu, ou, h->sw);
+    const float* vv[1] = {h->sl[5]};
+    float* ov[1] = {VB(h)};
+    ordered_splat(L, g, g.dx, g.dy, h->ncell, h->sl[3], h->sl[4], h->sl_ok[1], 1, vv, ov, h->sw);
+}
+
+void enqueue_phase(fs_handle* h, int ph, float dt)
+{
+    switch (ph) {
+        case FS_PH_CLASSIFY: ph_classify(h); break;
+        case FS_PH_P2G: ph_p2g(h); break;
+        case FS_PH_SAVE_PREV: ph_save_prev(h); break;
+        case FS_PH_GRAVITY: ph_gravity(h, dt); break;
+        case FS_PH_DIRICHLET: ph_dirichlet(h); break;
+        case FS_PH_EXTEND: ph_extend(h); break;
+        case FS_PH_PRESSURE: ph_pressure(h, dt); break;
+        case FS_PH_SAVE_DIFF: ph_save_diff(h); break;
+        case FS_PH_G2P_PICFLIP: ph_g2p(h, G2P_PICFLIP, ADV_NONE, dt); break;
+        case FS_PH_G2P_PIC: ph_g2p(h, G2P_PIC, ADV_NONE, dt); break;
+        case FS_PH_G2P_FLIP: ph_g2p(h, G2P_FLIP, ADV_NONE, dt); break;
+        case FS_PH_ADVECT_SAFE: ph_g2p(h, G2P_NONE, ADV_SAFE, dt); break;
+        case FS_PH_ADVECT: ph_g2p(h, G2P_NONE, ADV_PLAIN, dt); break;
+        case FS_PH_SL_VELOCITY: ph_sl_velocity(h, dt); break;
+        case FS_PH_SL_PARTICLES: ph_g2p(h, G2P_NONE, ADV_RK3, dt); break;
+        case FS_PH_SWAP: h->front ^= 1; break;
+        default: break;
+    }
+}
+
+// FluidSolver::step* (src/FluidSolver.cpp:99-251) as one queued sequence; the
+// grid-to-particle transfer and the particle advection share one kernel.
+void enqueue_step(fs_handle* h, int method, float dt)
+{
+    mark(h, FS_T_CLASSIFY);
+    ph_classify(h);
+    mark(h, FS_T_P2G);
+    if (method == FS_STEP_SEMI_LAGRANGIAN) {
+        mark(h, FS_T_FORCES);
+        ph_sl_velocity(h, dt);
+        ph_gravity(h, dt);
+        ph_dirichlet(h);
+    } else {
+        ph_p2g(h);
+        if (method != FS_STEP_PIC) ph_save_prev(h);
+        mark(h, FS_T_FORCES);
+        ph_gravity(h, dt);
+        ph_dirichlet(h);
+        ph_extend(h);
+    }
+    mark(h, FS_T_ASSEMBLY);
+    ph_pressure(h, dt);
+    ph_dirichlet(h);
+    if (method == FS_STEP_FLIP || method == FS_STEP_PICFLIP) ph_save_diff(h);
+    mark(h, FS_T_G2P);
+    switch (method) {
+        case FS_STEP_SEMI_LAGRANGIAN: ph_g2p(h, G2P_NONE, ADV_RK3, dt); break;
+        case FS_STEP_PIC: ph_g2p(h, G2P_PIC, ADV_PLAIN, dt); break;
+        case FS_STEP_FLIP: ph_g2p(h, G2P_FLIP, ADV_PLAIN, dt); break;
+        default: ph_g2p(h, G2P_PICFLIP, ADV_SAFE, dt); break;
+    }
+    mark(h, FS_NUM_TIMED);
+}
+
+int check_launch(fs_handle* h, const char* what)
+{
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(h, e, what);
+    return FS_OK;
+}
+
+// FluidSolver::validate (src/FluidSolver.cpp:89-97) against the solver's pool,
+// whose copy constructor keeps delta_x for delta_y (src/FluidSolver.cpp:56-62).
+bool validate(const fs_handle* h) { return std::fabs(h->g.dy - h->g.pdy) < 0.0000001; }
+
+const char* kValidateMessage =
+    "Memory pool and fluid domain does not match. Initialize the fluid solver with a memory pool corresponding "
+    "to the right fluid domain!";
+
+void destroy_all(fs_handle* h)
+{
+    if (!h) return;
+    cudaSetDevice(h->device);
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    clear_graphs(h);
+    void* ptrs[] = {h->u[0], h->u[1], h->v[0], h->v[1], h->u_prev, h->v_prev, h->u_diff, h->v_diff, h->labels,
+                    h->solid, h->vmx[0], h->vmx[1], h->vmy[0], h->vmy[1], h->fidx, h->cell_of, h->counts32,
+                    h->counts8, h->acc[0], h->acc[1], h->acc[2], h->acc[3], h->grid_tmp, h->sl[0], h->sl[1],
+                    h->sl[2], h->sl[3], h->sl[4], h->sl[5], h->sl_ok[0], h->sl_ok[1], h->px, h->py, h->pvx,
+                    h->pvy, h->yu, h->xv, h->staging, h->sw.keys_a, h->sw.keys_b, h->sw.vals_a, h->sw.vals_b,
+                    h->sw.hist, h->sw.hist_scan, h->sw.scan_tmp, h->sw.bin_start, h->cg.x, h->cg.r, h->cg.z,
+                    h->cg.p, h->cg.q, h->cg.partials, h->cg.barrier, h->cg.result, h->cg_b, h->cg_down, h->cg_up,
+                    h->cg_flags, h->d_nfluid, h->d_status, h->d_warn, h->scan_tmp};
+    for (void* p : ptrs) cudaFree(p);
+    for (auto& e : h->ev)
+        if (e) cudaEventDestroy(e);
+    if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+}
+
+int device_status(fs_handle* h)
+{
+    unsigned st = 0;
+    cudaError_t e = cudaMemcpyAsync(&st, h->d_status, sizeof(unsigned), cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) return cuda_fail(h, e, "synchronize");
+    if (st & ST_TIMEOUT) return fail(h, FS_ERR_TIMEOUT, "a device-side wait of the CG kernel timed out");
+    if (st & ST_TOO_LARGE) return fail(h, FS_ERR_TOO_LARGE, "too many fluid cells for the CG kernel");
+    if (st & ST_INTERNAL) return fail(h, FS_ERR_INTERNAL, "internal consistency check failed on the device");
+    return FS_OK;
+}
+
+template <class T>
+int copy_out(fs_handle* h, T* host, const T* dev, size_t count)
+{
+    if (!host) return fail(h, FS_ERR_INVALID_ARGUMENT, "null output pointer");
+    cudaError_t e = cudaMemcpyAsync(host, dev, count * sizeof(T), cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) return cuda_fail(h, e, "copy to host");
+    return FS_OK;
+}
+
+template <class T>
+int copy_in(fs_handle* h, T* dev, const T* host, size_t count)
+{
+    if (!host) return fail(h, FS_ERR_INVALID_ARGUMENT, "null input pointer");
+    cudaError_t e = cudaMemcpyAsync(dev, host, count * sizeof(T), cudaMemcpyHostToDevice, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) return cuda_fail(h, e, "copy to device");
+    clear_graphs(h);  // a step graph never depends on data, but keep capture state simple
+    return FS_OK;
+}
+
+float* grid_ptr(fs_handle* h, int which)
+{
+    switch (which) {
+        case FS_U_FRONT: return UF(h);
+        case FS_V_FRONT: return VF(h);
+        case FS_U_BACK: return UB(h);
+        case FS_V_BACK: return VB(h);
+        case FS_U_PREV: return h->u_prev;
+        case FS_V_PREV: return h->v_prev;
+        case FS_U_DIFF: return h->u_diff;
+        case FS_V_DIFF: return h->v_diff;
+        default: return nullptr;
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+void fs_config_init(fs_config* c, int size_x, int size_y)
+{
+    if (!c) return;
+    std::memset(c, 0, sizeof(*c));
+    c->size_x = size_x;
+    c->size_y = size_y;
+    c->length_x = (float)size_x;
+    c->length_y = (float)size_y;
+    c->density = 1.0f;
+    c->pic_ratio = 0.0f;
+    c->gravity_x = 0.0f;
+    c->gravity_y = (float)-9.82;
+    c->cg_max_iterations = 100;
+    c->cg_tolerance = 1.1920928955078125e-07;  // FLT_EPSILON
+    c->extension_iterations = 2;
+    c->device = 0;
+}
+
+const char* fs_last_error(const fs_handle* h) { return h ? h->err.c_str() : g_create_error.c_str(); }
+
+int fs_create(const fs_config* cfg, fs_handle** out)
+{
+    g_create_error.clear();
+    if (!cfg || !out) {
+        g_create_error = "null argument";
+        return FS_ERR_INVALID_ARGUMENT;
+    }
+    *out = nullptr;
+    if (cfg->size_x < 1 || cfg->size_y < 1 || !(cfg->length_x > 0) || !(cfg->length_y > 0) ||
+        !std::isfinite(cfg->length_x) || !std::isfinite(cfg->length_y)) {
+        g_create_error = "invalid grid size or length";
+        return FS_ERR_INVALID_ARGUMENT;
+    }
+    const int64_t ncell = (int64_t)cfg->size_x * cfg->size_y;
+    if (ncell > (int64_t)4096 * 4096 || cfg->size_x > (1 << 20) || cfg->size_y > (1 << 20)) {
+        g_create_error = "grid larger than 16777216 cells";
+        return FS_ERR_TOO_LARGE;
+    }
+    fs_handle* h = new fs_handle();
+    h->cfg = *cfg;
+    h->device = cfg->device;
+    h->ncell = ncell;
+    cudaError_t e = cudaSetDevice(h->device);
+    if (e != cudaSuccess) {
+        g_create_error = std::string("cudaSetDevice: ") + cudaGetErrorString(e);
+        delete h;
+        return FS_ERR_CUDA;
+    }
+    // GridInterface(size, size, length / size, ...) (src/FluidDomain.cpp:62, src/MacGrid.cpp:9)
+    Geom& g = h->g;
+    g.nx = cfg->size_x;
+    g.ny = cfg->size_y;
+    g.dx = cfg->length_x / (float)cfg->size_x;
+    g.dy = cfg->length_y / (float)cfg->size_y;
+    g.lx = (float)g.nx * g.dx;
+    g.ly = (float)g.ny * g.dy;
+    g.pdx = g.dx;
+    g.pdy = g.dx;  // FluidSolverMemoryPool copy keeps delta_x for delta_y (src/FluidSolver.cpp:56-62)
+    h->pic = cfg->pic_ratio;  // stored as given (src/FluidDomain.cpp:64)
+    h->gx = cfg->gravity_x;
+    h->gy = cfg->gravity_y;
+    h->cg_tol = cfg->cg_tolerance;
+    h->cg_maxit = cfg->cg_max_iterations;
+    h->n_ext = cfg->extension_iterations;
+    // Matrix coefficients through double pow() as in src/FluidSolver.cpp:381-410.
+    const double dx2 = std::pow((double)g.dx, 2);
+    h->off = (float)(1 / dx2);
+    for (int n = 0; n < 5; ++n) h->diag_tab[n] = (float)(-n / dx2);
+
+    const size_t N = (size_t)ncell;
+    const int64_t max_chunks = (ncell + 1023) / 1024;
+    bool ok = true;
+    auto A = [&](cudaError_t r) {
+        if (r != cudaSuccess && ok) {
+            ok = false;
+            e = r;
+        }
+    };
+    A(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+    h->own_stream = true;
+    for (int b = 0; b < 2; ++b) {
+        A(dalloc(&h->u[b], N));
+        A(dalloc(&h->v[b], N));
+        A(dalloc(&h->vmx[b], N));
+        A(dalloc(&h->vmy[b], N));
+    }
+    A(dalloc(&h->u_prev, N));
+    A(dalloc(&h->v_prev, N));
+    A(dalloc(&h->u_diff, N));
+    A(dalloc(&h->v_diff, N));
+    A(dalloc(&h->labels, N));
+    A(dalloc(&h->fidx, N));
+    A(dalloc(&h->cell_of, N));
+    A(dalloc(&h->counts32, N));
+    A(dalloc(&h->counts8, N));
+    for (int k = 0; k < 4; ++k) A(dalloc(&h->acc[k], N));
+    A(dalloc(&h->grid_tmp, N));
+    A(dalloc(&h->sw.bin_start, N + 2));
+    A(dalloc(&h->cg.x, N));
+    A(dalloc(&h->cg.r, N));
+    A(dalloc(&h->cg.z, N));
+    A(dalloc(&h->cg.p, N));
+    A(dalloc(&h->cg.q, N));
+    A(dalloc(&h->cg.partials, (size_t)4 * max_chunks));
+    A(dalloc(&h->cg.barrier, 1));
+    A(dalloc(&h->cg.result, 1));
+    A(dalloc(&h->cg_b, N));
+    A(dalloc(&h->cg_down, N));
+    A(dalloc(&h->cg_up, N));
+    A(dalloc(&h->cg_flags, N));
+    A(dalloc(&h->d_nfluid, 1));
+    A(dalloc(&h->d_status, 1));
+    A(dalloc(&h->d_warn, 1));
+    A(dalloc(&h->scan_tmp, scan_tmp_ints(ncell + 2)));
+    for (auto& ev : h->ev) A(cudaEventCreate(&ev));
+    h->cg.max_cells = ncell;
+    if (ok && cg_prepare(h->cg, h->device) != 0) {
+        ok = false;
+        e = cudaErrorInvalidConfiguration;
+    }
+    if (ok) A(ensure_splat_capacity(h, ncell));
+    if (ok) {
+        // Zero-initialised state, as the reference's Grid<T> ctor (include/Grid.h:129-139).
+        for (int b = 0; b < 2; ++b) {
+            A(cudaMemsetAsync(h->u[b], 0, N * 4, h->stream));
+            A(cudaMemsetAsync(h->v[b], 0, N * 4, h->stream));
+            A(cudaMemsetAsync(h->vmx[b], 0, N, h->stream));
+            A(cudaMemsetAsync(h->vmy[b], 0, N, h->stream));
+        }
+        for (float* p : {h->u_prev, h->v_prev, h->u_diff, h->v_diff, h->cg.x}) A(cudaMemsetAsync(p, 0, N * 4, h->stream));
+        A(cudaMemsetAsync(h->fidx, 0, N * 4, h->stream));
+        A(cudaMemsetAsync(h->counts8, 0, N, h->stream));
+        A(cudaMemsetAsync(h->d_nfluid, 0, 4, h->stream));
+        A(cudaMemsetAsync(h->d_status, 0, 4, h->stream));
+        A(cudaMemsetAsync(h->d_warn, 0, 4, h->stream));
+        A(cudaMemsetAsync(h->cg.result, 0, sizeof(CgResult), h->stream));
+        labels_clear(h->L(), h->g, h->labels);  // MacGrid ctor -> clearCellTypeBuffer (src/MacGrid.cpp:24)
+        A(cudaGetLastError());
+        A(cudaStreamSynchronize(h->stream));
+    }
+    if (!ok) {
+        g_create_error = std::string("fs_create: ") + cudaGetErrorString(e);
+        const int code = e == cudaErrorMemoryAllocation ? FS_ERR_OUT_OF_MEMORY : FS_ERR_CUDA;
+        destroy_all(h);
+        return code;
+    }
+    *out = h;
+    return FS_OK;
+}
+
+int fs_destroy(fs_handle* h)
+{
+    destroy_all(h);
+    return FS_OK;
+}
+
+int fs_set_pic_ratio(fs_handle* h, float r)
+{
+    if (!h) return FS_ERR_INVALID_ARGUMENT;
+    // FluidDomain::setPicRatio (src/FluidDomain.cpp:99-102): CLAMP(pic_ratio, 0, 1)
+    const float t = r < 0.0f ? 0.0f : r;
+    h->pic = t > 1.0f ? 1.0f : t;
+    clear_graphs(h);
+    return FS_OK;
+}
+
+int fs_set_gravity(fs_handle* h, float gx, float gy)
+{
+    if (!h) return FS_ERR_INVALID_ARGUMENT;
+    h->gx = gx;
+    h->gy = gy;
+    clear_graphs(h);
+    return FS_OK;
+}
+
+int fs_set_cg(fs_handle* h, double tol, int maxit)
+{
+    if (!h || !(tol >= 0) || maxit < 0) return h ? fail(h, FS_ERR_INVALID_ARGUMENT, "invalid CG settings") : 1;
+    h->cg_tol = tol;
+    h->cg_maxit = maxit;
+    clear_graphs(h);
+    return FS_OK;
+}
+
+int fs_set_extension_iterations(fs_handle* h, int n)
+{
+    if (!h || n < 0) return h ? fail(h, FS_ERR_INVALID_ARGUMENT, "negative extension iterations") : 1;
+    h->n_ext = n;
+    clear_graphs(h);
+    return FS_OK;
+}
+
+int fs_set_solid_mask(fs_handle* h, const uint8_t* mask)
+{
+    if (!h) return FS_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(h->device);
+    clear_graphs(h);
+    if (!mask) {
+        cudaStreamSynchronize(h->stream);
+        cudaFree(h->solid);
+        h->solid = nullptr;
+        return FS_OK;
+    }
+    if (!h->solid) {
+        cudaError_t e = dalloc(&h->solid, (size_t)h->ncell);
+        if (e != cudaSuccess) return cuda_fail(h, e, "solid mask");
+    }
+    return copy_in(h, h->solid, mask, (size_t)h->ncell);
+}
+
+int fs_set_particles(fs_handle* h, const float* xyuv, int64_t n)
+{
+    if (!h || n < 0 || (n > 0 && !xyuv)) return h ? fail(h, FS_ERR_INVALID_ARGUMENT, "invalid particles") : 1;
+    if (n > (int64_t)INT32_MAX) return fail(h, FS_ERR_TOO_LARGE, "more than 2^31-1 particles");
+    cudaSetDevice(h->device);
+    cudaError_t e = ensure_particle_capacity(h, n);
+    if (e != cudaSuccess) return cuda_fail(h, e, "particle storage");
+    if (n > 0) {
+        e = cudaMemcpyAsync(h->staging, xyuv, sizeof(float) * 4 * (size_t)n, cudaMemcpyHostToDevice, h->stream);
+        if (e != cudaSuccess) return cuda_fail(h, e, "particle upload");
+        aos_to_soa(h->L(), h->staging, n, h->px, h->py, h->pvx, h->pvy);
+    }
+    if (n != h->n_part) clear_graphs(h);
+    h->n_part = n;
+    return check_launch(h, "particle upload");
+}
+
+int fs_set_particles_device(fs_handle* h, const float* d_xyuv, int64_t n)
+{
+    if (!h || n < 0 || (n > 0 && !d_xyuv)) return h ? fail(h, FS_ERR_INVALID_ARGUMENT, "invalid particles") : 1;
+    if (((uintptr_t)d_xyuv & 15u) != 0) return fail(h, FS_ERR_INVALID_ARGUMENT, "device particle array not 16-byte aligned");
+    if (n > (int64_t)INT32_MAX) return fail(h, FS_ERR_TOO_LARGE, "more than 2^31-1 particles");
+    cudaSetDevice(h->device);
+    cudaError_t e = ensure_particle_capacity(h, n);
+    if (e != cudaSuccess) return cuda_fail(h, e, "particle storage");
+    if (n > 0) aos_to_soa(h->L(), d_xyuv, n, h->px, h->py, h->pvx, h->pvy);
+    if (n != h->n_part) clear_graphs(h);
+    h->n_part = n;
+    return check_launch(h, "particle upload");
+}
+
+int fs_add_particles(fs_handle* h, const float* xyuv, int64_t n)
+{
+    if (!h || n < 0 || (n > 0 && !xyuv)) return h ? fail(h, FS_ERR_INVALID_ARGUMENT, "invalid particles") : 1;
+    if (n == 0) return FS_OK;
+    const int64_t total = h->n_part + n;
+    if (total > (int64_t)INT32_MAX) return fail(h, FS_ERR_TOO_LARGE, "more than 2^31-1 particles");
+    cudaSetDevice(h->device);
+    cudaError_t e = ensure_particle_capacity(h, total);
+    if (e != cudaSuccess) return cuda_fail(h, e, "particle storage");
+    e = cudaMemcpyAsync(h->staging, xyuv, sizeof(float) * 4 * (size_t)n, cudaMemcpyHostToDevice, h->stream);
+    if (e != cudaSuccess) return cuda_fail(h, e, "particle upload");
+    const int64_t o = h->n_part;
+    aos_to_soa(h->L(), h->staging, n, h->px + o, h->py + o, h->pvx + o, h->pvy + o);
+    h->n_part = total;
+    clear_graphs(h);
+    return check_launch(h, "particle upload");
+}
+
+int fs_num_particles(fs_handle* h, int64_t* n)
+{
+    if (!h || !n) return FS_ERR_INVALID_ARGUMENT;
+    *n = h->n_part;
+    return FS_OK;
+}
+
+int fs_get_particles(fs_handle* h, float* xyuv, int64_t n)
+{
+    if (!h || n != h->n_part) return h ? fail(h, FS_ERR_INVALID_ARGUMENT, "particle count mismatch") : 1;
+    if (n == 0) return FS_OK;
+    cudaSetDevice(h->device);
+    soa_to_aos(h->L(), h->px, h->py, h->pvx, h->pvy, n, h->staging);
+    const int rc = check_launch(h, "particle download");
+    if (rc) return rc;
+    return copy_out(h, xyuv, h->staging, (size_t)n * 4);
+}
+
+int fs_get_particles_device(fs_handle* h, float* d_xyuv, int64_t n)
+{
+    if (!h || n != h->n_part || (n > 0 && !d_xyuv)) return h ? fail(h, FS_ERR_INVALID_ARGUMENT, "particle count mismatch") : 1;
+    if (((uintptr_t)d_xyuv & 15u) != 0) return fail(h, FS_ERR_INVALID_ARGUMENT, "device particle array not 16-byte aligned");
+    if (n == 0) return FS_OK;
+    cudaSetDevice(h->device);
+    soa_to_aos(h->L(), h->px, h->py, h->pvx, h->pvy, n, d_xyuv);
+    return check_launch(h, "particle download");
+}
+
+int fs_get_grid(fs_handle* h, int which, float* out)
+{
+    if (!h) return FS_ERR_INVALID_ARGUMENT;
+    float* p = grid_ptr(h, which);
+    if (!p) return fail(h, FS_ERR_INVALID_ARGUMENT, "unknown grid");
+    cudaSetDevice(h->device);
+    return copy_out(h, out, p, (size_t)h->ncell);
+}
+
+int fs_set_grid(fs_handle* h, int which, const float* in)
+{
+    if (!h) return FS_ERR_INVALID_ARGUMENT;
+    float* p = grid_ptr(h, which);
+    if (!p) return fail(h, FS_ERR_INVALID_ARGUMENT, "unknown grid");
+    cudaSetDevice(h->device);
+    return copy_in(h, p, in, (size_t)h->ncell);
+}
+
+int fs_get_labels(fs_handle* h, uint8_t* out)
+{
+    if (!h) return FS_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(h->device);
+    return copy_out(h, out, h->labels, (size_t)h->ncell);
+}
+
+int fs_set_labels(fs_handle* h, const uint8_t* in)
+{
+    if (!h) return FS_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(h->device);
+    return copy_in(h, h->labels, in, (size_t)h->ncell);
+}
+
+int fs_get_fluid_indices(fs_handle* h, int32_t* out)
+{
+    if (!h) return FS_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(h->device);
+    return copy_out(h, out, h->fidx, (size_t)h->ncell);
+}
+
+int fs_get_particle_counts(fs_handle* h, uint8_t* out)
+{
+    if (!h) return FS_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(h->device);
+    return copy_out(h, out, h->counts8, (size_t)h->ncell);
+}
+
+int fs_get_pressure(fs_handle* h, float* out)
+{
+    if (!h) return FS_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(h->device);
+    pressure_to_grid(h->L(), h->g, h->fidx, h->d_nfluid, h->cg.x, h->grid_tmp);
+    const int rc = check_launch(h, "pressure");
+    if (rc) return rc;
+    return copy_out(h, out, h->grid_tmp, (size_t)h->ncell);
+}
+
+int fs_phase(fs_handle* h, int ph, float dt)
+{
+    if (!h) return FS_ERR_INVALID_ARGUMENT;
+    if (ph < FS_PH_CLASSIFY || ph > FS_PH_SWAP) return fail(h, FS_ERR_INVALID_ARGUMENT, "unknown phase");
+    cudaSetDevice(h->device);
+    if (ph == FS_PH_SL_VELOCITY) {
+        cudaError_t e = ensure_sl_scratch(h);
+        if (e != cudaSuccess) return cuda_fail(h, e, "semi-Lagrangian scratch");
+    }
+    const bool t = h->timing;
+    h->timing = false;
+    enqueue_phase(h, ph, dt);
+    h->timing = t;
+    return check_launch(h, "phase");
+}
+
+int fs_step(fs_handle* h, int method, float dt)
+{
+    if (!h) return FS_ERR_INVALID_ARGUMENT;
+    if (method < FS_STEP_SEMI_LAGRANGIAN || method > FS_STEP_PICFLIP)
+        return fail(h, FS_ERR_INVALID_ARGUMENT, "unknown step method");
+    if (!validate(h)) return fail(h, FS_ERR_VALIDATE, kValidateMessage);
+    cudaSetDevice(h->device);
+    if (method == FS_STEP_SEMI_LAGRANGIAN) {
+        cudaError_t e = ensure_sl_scratch(h);
+        if (e != cudaSuccess) return cuda_fail(h, e, "semi-Lagrangian scratch");
+    }
+    h->timed_valid = h->timing;
+    if (!h->graphs) {
+        enqueue_step(h, method, dt);
+        return check_launch(h, "step");
+    }
+    const uint32_t db = float_bits(dt);
+    for (auto& ge : h->graph_cache) {
+        if (ge.method == method && ge.dt_bits == db && ge.front_in == h->front && ge.vfront_in == h->vfront &&
+            ge.n_part == h->n_part && ge.timing == h->timing) {
+            cudaError_t e = cudaGraphLaunch(ge.exec, h->stream);
+            if (e != cudaSuccess) return cuda_fail(h, e, "graph launch");
+            h->front = ge.front_out;
+            h->vfront = ge.vfront_out;
+            h->launches += ge.kernels;
+            return FS_OK;
+        }
+    }
+    GraphEntry ge{};
+    ge.method = method;
+    ge.dt_bits = db;
+    ge.front_in = h->front;
+    ge.vfront_in = h->vfront;
+    ge.n_part = h->n_part;
+    ge.timing = h->timing;  // event-record nodes of the per-phase timers are part of the graph
+    const int64_t l0 = h->launches;
+    cudaGraph_t graph = nullptr;
+    cudaError_t e = cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return cuda_fail(h, e, "begin capture");
+    enqueue_step(h, method, dt);
+    cudaError_t e_launch = cudaGetLastError();
+    e = cudaStreamEndCapture(h->stream, &graph);
+    ge.front_out = h->front;
+    ge.vfront_out = h->vfront;
+    ge.kernels = h->launches - l0;
+    h->launches = l0;
+    if (e != cudaSuccess || e_launch != cudaSuccess || !graph) {
+        if (graph) cudaGraphDestroy(graph);
+        cudaGetLastError();
+        // Fall back to direct launches for this handle.
+        h->graphs = false;
+        h->front = ge.front_in;
+        h->vfront = ge.vfront_in;
+        enqueue_step(h, method, dt);
+        return check_launch(h, "step");
+    }
+    e = cudaGraphInstantiate(&ge.exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        h->graphs = false;
+        h->front = ge.front_in;
+        h->vfront = ge.vfront_in;
+        enqueue_step(h, method, dt);
+        return check_launch(h, "step");
+    }
+    h->graph_cache.push_back(ge);
+    e = cudaGraphLaunch(ge.exec, h->stream);
+    if (e != cudaSuccess) return cuda_fail(h, e, "graph launch");
+    h->launches += ge.kernels;
+    return FS_OK;
+}
+
+int fs_synchronize(fs_handle* h)
+{
+    if (!h) return FS_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(h->device);
+    return device_status(h);
+}
+
+int fs_get_stats(fs_handle* h, fs_step_stats* out)
+{
+    if (!h || !out) return FS_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(h->device);
+    const int rc = device_status(h);
+    std::memset(out, 0, sizeof(*out));
+    CgResult r{};
+    int32_t nf = 0;
+    unsigned warn = 0;
+    cudaMemcpy(&r, h->cg.result, sizeof(r), cudaMemcpyDeviceToHost);
+    cudaMemcpy(&nf, h->d_nfluid, sizeof(nf), cudaMemcpyDeviceToHost);
+    cudaMemcpy(&warn, h->d_warn, sizeof(warn), cudaMemcpyDeviceToHost);
+    cudaMemsetAsync(h->d_warn, 0, sizeof(unsigned), h->stream);
+    out->cg_iterations = r.iterations;
+    out->n_fluid = nf;
+    out->cg_residual = r.bb > 0 ? std::sqrt(r.rr / r.bb) : 0.0;
+    double thr = h->cg_tol * h->cg_tol * r.bb;
+    if (nf > 0 && r.bb > 0 && r.iterations >= h->cg_maxit && r.rr >= thr) warn |= FS_WARN_CG_NOT_CONVERGED;
+    out->warnings = warn;
+    if (h->timed_valid) {
+        float total = 0.0f;
+        for (int k = 0; k < FS_NUM_TIMED; ++k) {
+            float ms = 0.0f;
+            if (cudaEventElapsedTime(&ms, h->ev[k], h->ev[k + 1]) == cudaSuccess) out->ms_phase[k] = ms;
+            total += out->ms_phase[k];
+        }
+        out->ms_total = total;
+    }
+    cudaGetLastError();
+    return rc;
+}
+
+int fs_set_timing(fs_handle* h, int enable)
+{
+    if (!h) return FS_ERR_INVALID_ARGUMENT;
+    h->timing = enable != 0;
+    return FS_OK;
+}
+
+int fs_set_graphs(fs_handle* h, int enable)
+{
+    if (!h) return FS_ERR_INVALID_ARGUMENT;
+    h->graphs = enable != 0;
+    if (!h->graphs) clear_graphs(h);
+    return FS_OK;
+}
+
+void* fs_get_stream(fs_handle* h) { return h ? (void*)h->stream : nullptr; }
+
+int fs_set_stream(fs_handle* h, void* stream)
+{
+    if (!h) return FS_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(h->device);
+    cudaStreamSynchronize(h->stream);
+    if (h->own_stream) cudaStreamDestroy(h->stream);
+    h->stream = (cudaStream_t)stream;
+    h->own_stream = false;
+    clear_graphs(h);
+    return FS_OK;
+}
+
+int64_t fs_kernel_launches(fs_handle* h) { return h ? h->launches : 0; }
+
+}  // extern "C"

@@ -1,0 +1,486 @@
+// Jacobi-preconditioned conjugate gradient for the pressure Poisson system of
+// FluidSolver::pressureSolve (src/FluidSolver.cpp:363-425), where the
+// reference assembles an Eigen::SparseMatrix and calls
+// Eigen::ConjugateGradient (zero initial guess, diagonal preconditioner,
+// stop when ||r||^2 < tol^2 ||b||^2 or after maxit updates).
+//
+// One persistent cooperative kernel runs the whole solve.  The matrix is never
+// stored: row k of A is rebuilt from the fluid-cell flags (liquid left/right
+// neighbours are k-1/k+1 in the j-major fluid order), the down/up fluid
+// indices and the count of non-solid neighbours.  Floating point follows the
+// oracle exactly:
+//   * vectors and SpMV in float, each product and sum rounded on its own; a
+//     row sums its terms in ascending column order (down, left, centre,
+//     right, up) starting from +0;
+//   * dot products accumulate exact float*float products in double along the
+//     fixed "32-ary stride-halving tree" (groups of 32 consecutive elements,
+//     s = 16..1: a[l] += a[l+s], repeated on the group results) -- a warp
+//     shuffle tree, then a tree over warps (one 1024-element chunk per CTA
+//     pass), then a tree over chunk partials that every CTA evaluates
+//     redundantly after a grid barrier.  The result does not depend on the
+//     launch shape;
+//   * alpha and beta are formed in double and rounded once to float.
+//
+// Per iteration there are two grid barriers (after p.q and after r.r, r.z).
+// The search direction p_new = z + beta p_old is not exchanged through a third
+// barrier: z and p_old of every cell are published to global memory in the
+// previous phase, and each CTA recomputes p_new of the neighbours it needs
+// with the same float operations.  Each CTA keeps the state of its own cells
+// in shared memory (up to KREG chunks of 1024 cells per CTA, ~200 KB) or, for
+// larger systems, streams it from global memory.  Waits are bounded: a CTA that
+// waits longer than about two seconds sets ST_TIMEOUT and every CTA returns.
+#include "fs_internal.h"
+
+namespace fs {
+namespace {
+
+constexpr int CG_THREADS = 1024;
+constexpr int CHUNK = CG_THREADS;
+constexpr int KREG = 8;                   // chunks per CTA kept in shared memory
+constexpr size_t RESIDENT_BYTES = (size_t)KREG * CHUNK * 25;
+constexpr int SINGLE_CTA_CHUNKS = 16;       // systems this small run in one CTA
+constexpr int MAX_CHUNKS = 32 * 1024;       // all-read reduction limit (33.5M cells)
+constexpr uint64_t WAIT_LIMIT_NS = 2000000000ull;
+
+struct CgArgs
+{
+    const int32_t* nfluid;
+    const float* b;
+    const int32_t* down;
+    const int32_t* up;
+    const uint8_t* flags;  // bit 0 left liquid, bit 1 right liquid, bits 2-4 non-solid neighbours
+    float dtab[5];         // diagonal by non-solid count: (float)(-n / dx^2)
+    float itab[5];         // 1 / diagonal, or 1 where the diagonal is 0
+    float off;             // (float)(1 / dx^2)
+    double tol2;
+    int maxit;
+    float *x, *r, *z, *p, *q;  // fluid-index vectors (global)
+    double* partials;          // [2 buffers][2 values][MAX chunks]
+    int max_chunks;
+    unsigned* barrier;
+    unsigned* status;
+    CgResult* result;
+};
+
+struct Smem
+{
+    union {
+        double red[32][32][2];  // level-1 results: [chunk slot][warp][value]
+        double lvlA[1024][2];
+    };
+    double lvlB[32][2];
+    float dtab[5];
+    float itab[5];
+    int flag;
+};
+
+__device__ __forceinline__ double warp_tree(double v)
+{
+#pragma unroll
+    for (int s = 16; s >= 1; s >>= 1) v = dadd(v, __shfl_down_sync(0xffffffffu, v, s));
+    return v;
+}
+
+// Barrier over the active CTAs.  Returns false if any CTA timed out.
+__device__ __forceinline__ bool cta_barrier(const CgArgs& a, bool grid, unsigned& target, Smem& sm)
+{
+    __syncthreads();
+    if (grid && threadIdx.x == 0) {
+        target += gridDim.x;
+        __threadfence();
+        red_release_add_u32(a.barrier, 1u);
+        const uint64_t t0 = globaltimer_ns();
+        while (ld_acquire_u32(a.barrier) < target) {
+            if (globaltimer_ns() - t0 > WAIT_LIMIT_NS) {
+                atomicOr(a.status, ST_TIMEOUT);
+                break;
+            }
+            __nanosleep(32);
+        }
+        __threadfence();
+    }
+    if (threadIdx.x == 0) sm.flag = (*(volatile unsigned*)a.status & ST_TIMEOUT) ? 1 : 0;
+    __syncthreads();
+    return sm.flag == 0;
+}
+
+// Level-1 (warp) tree of NV values for chunk slot `slot`; lane 0 keeps it.
+template <int NV>
+__device__ __forceinline__ void level1(const double (&v)[NV], int slot, Smem& sm)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+        const double t = warp_tree(v[k]);
+        if (lane == 0) sm.red[slot][warp][k] = t;
+    }
+}
+
+// Level-2 trees for slots [0, nslots) -> chunk partials partials[buf][k][chunk0 + slot].
+template <int NV>
+__device__ __forceinline__ void level2(const CgArgs& a, int buf, int chunk0, int nslots, Smem& sm)
+{
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (warp < nslots) {
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            const double t = warp_tree(sm.red[warp][lane][k]);
+            if (lane == 0) __stcg(&a.partials[((size_t)buf * 2 + k) * a.max_chunks + chunk0 + warp], t);
+        }
+    }
+    __syncthreads();
+}
+
+// Levels 3+: every CTA reduces all chunk partials of buffer buf.
+template <int NV>
+__device__ __forceinline__ void reduce_all(const CgArgs& a, int buf, int nchunks, Smem& sm, double (&out)[NV])
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const double* src = a.partials + (size_t)buf * 2 * a.max_chunks;
+    if (nchunks == 1) {
+#pragma unroll
+        for (int k = 0; k < NV; ++k) out[k] = __ldcg(&src[(size_t)k * a.max_chunks]);
+        return;
+    }
+    int n = (nchunks + 31) / 32;
+    for (int g = warp; g < n; g += 32) {
+        const int e = g * 32 + lane;
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            const double v = e < nchunks ? __ldcg(&src[(size_t)k * a.max_chunks + e]) : 0.0;
+            const double t = warp_tree(v);
+            if (lane == 0) sm.lvlA[g][k] = t;
+        }
+    }
+    __syncthreads();
+    bool inA = true;
+    while (n > 1) {
+        const int m = (n + 31) / 32;
+        if (warp < m) {
+            const int e = warp * 32 + lane;
+#pragma unroll
+            for (int k = 0; k < NV; ++k) {
+                double v;
+                if (inA) v = e < n ? sm.lvlA[e][k] : 0.0;
+                else v = e < n ? sm.lvlB[e][k] : 0.0;
+                const double t = warp_tree(v);
+                if (lane == 0) {
+                    if (inA) sm.lvlB[warp][k] = t;
+                    else sm.lvlA[warp][k] = t;
+                }
+            }
+        }
+        __syncthreads();
+        inA = !inA;
+        n = m;
+    }
+#pragma unroll
+    for (int k = 0; k < NV; ++k) out[k] = inA ? sm.lvlA[0][k] : sm.lvlB[0][k];
+    __syncthreads();
+}
+
+// p_new of a cell outside this CTA's range, from its published z and p_old.
+__device__ __forceinline__ float remote_p(const CgArgs& a, int n, bool first, float beta)
+{
+    const float zn = __ldcg(&a.z[n]);
+    return first ? zn : fadd(zn, fmul(beta, __ldcg(&a.p[n])));
+}
+
+// Shared-memory-resident state of this CTA's cells (K > 0): slot s of
+// thread t is element (c0 + s) * CHUNK + t, stored at [s * CHUNK + t].
+struct Resident
+{
+    float* x;
+    float* r;
+    float* zq;  // z, and q between the SpMV and the update
+    float* p;
+    int32_t* dn;
+    int32_t* up;
+    uint8_t* fl;
+};
+
+__device__ __forceinline__ Resident resident(unsigned char* dyn, int K)
+{
+    Resident R;
+    const int n = K * CHUNK;
+    R.x = reinterpret_cast<float*>(dyn);
+    R.r = R.x + n;
+    R.zq = R.r + n;
+    R.p = R.zq + n;
+    R.dn = reinterpret_cast<int32_t*>(R.p + n);
+    R.up = R.dn + n;
+    R.fl = reinterpret_cast<uint8_t*>(R.up + n);
+    return R;
+}
+
+// One CG solve.  K > 0: the CTA's cells (at most K chunks) live in shared
+// memory; K == 0: the state streams from global memory.
+template <int K>
+__device__ void cg_body(const CgArgs& a, Smem& sm, unsigned char* dyn, int nf, int nchunks, bool grid)
+{
+    const int tid = threadIdx.x;
+    const int ncta = grid ? (int)gridDim.x : 1;
+    const int cta = grid ? (int)blockIdx.x : 0;
+    const int c0 = (int)(((int64_t)cta * nchunks) / ncta);
+    const int c1 = (int)(((int64_t)(cta + 1) * nchunks) / ncta);
+    const int kb = c1 - c0;                // chunks owned
+    const int e0 = c0 * CHUNK;             // owned element range [e0, e1)
+    const int e1 = min(c1 * CHUNK, nf);
+    unsigned target = 0;
+    const Resident R = resident(dyn, K > 0 ? K : 1);
+    const float* dtab = sm.dtab;
+    const float* itab = sm.itab;
+
+    // ---- initialisation: x = 0, r = b, z = M^-1 r; bb = r.r, rz = r.z
+    for (int base = 0; base < kb; base += 32) {
+        const int nslot = min(32, kb - base);
+        for (int sl = 0; sl < nslot; ++sl) {
+            const int s = base + sl;
+            const int e = (c0 + s) * CHUNK + tid;
+            double v[2] = {0.0, 0.0};
+            if (e < nf) {
+                const float r = a.b[e];
+                const uint8_t fl = a.flags[e];
+                const float z = fmul(itab[fl >> 2], r);
+                __stcg(&a.z[e], z);
+                v[0] = dmul((double)r, (double)r);
+                v[1] = dmul((double)r, (double)z);
+                if (K > 0) {
+                    const int l = s * CHUNK + tid;
+                    R.x[l] = 0.0f;
+                    R.r[l] = r;
+                    R.zq[l] = z;
+                    R.p[l] = 0.0f;
+                    R.dn[l] = a.down[e];
+                    R.up[l] = a.up[e];
+                    R.fl[l] = fl;
+                } else {
+                    __stcg(&a.x[e], 0.0f);
+                    __stcg(&a.r[e], r);
+                }
+            }
+            level1<2>(v, sl, sm);
+        }
+        level2<2>(a, 0, c0 + base, nslot, sm);
+    }
+    if (!cta_barrier(a, grid, target, sm)) return;
+    double red2[2];
+    reduce_all<2>(a, 0, nchunks, sm, red2);
+    const double bb = red2[0];
+    double rz = red2[1];
+    double rr = bb;
+    int iters = 0;
+    bool done = bb == 0.0;
+    double thr = a.tol2 * bb;
+    if (thr < 2.2250738585072014e-308) thr = 2.2250738585072014e-308;
+    if (!done && rr < thr) done = true;
+
+    bool first = true;
+    float beta = 0.0f;
+    for (int it = 1; !done && it <= a.maxit; ++it) {
+        // ---- phase A: p_new = z + beta p, q = A p_new, partial p.q
+        if (K > 0) {
+            for (int s = 0; s < kb; ++s) {
+                const int l = s * CHUNK + tid;
+                if ((c0 + s) * CHUNK + tid < nf) R.p[l] = first ? R.zq[l] : fadd(R.zq[l], fmul(beta, R.p[l]));
+            }
+            __syncthreads();
+        }
+        for (int base = 0; base < kb; base += 32) {
+            const int nslot = min(32, kb - base);
+            for (int sl = 0; sl < nslot; ++sl) {
+                const int s = base + sl;
+                const int e = (c0 + s) * CHUNK + tid;
+                const int l = s * CHUNK + tid;
+                double v[1] = {0.0};
+                if (e < nf) {
+                    float pe;
+                    unsigned fl;
+                    int dn, up;
+                    if (K > 0) {
+                        pe = R.p[l];
+                        fl = R.fl[l];
+                        dn = R.dn[l];
+                        up = R.up[l];
+                    } else {
+                        pe = remote_p(a, e, first, beta);
+                        fl = a.flags[e];
+                        dn = a.down[e];
+                        up = a.up[e];
+                    }
+                    auto pv = [&](int n) -> float {
+                        if (K > 0 && n >= e0 && n < e1) return R.p[n - e0];
+                        return remote_p(a, n, first, beta);
+                    };
+                    float acc = 0.0f;
+                    if (dn >= 0) acc = fadd(acc, fmul(a.off, pv(dn)));
+                    if (fl & 1u) acc = fadd(acc, fmul(a.off, pv(e - 1)));
+                    acc = fadd(acc, fmul(dtab[fl >> 2], pe));
+                    if (fl & 2u) acc = fadd(acc, fmul(a.off, pv(e + 1)));
+                    if (up >= 0) acc = fadd(acc, fmul(a.off, pv(up)));
+                    v[0] = dmul((double)pe, (double)acc);
+                    if (K > 0) R.zq[l] = acc;  // z is no longer needed: it is folded into p
+                    else __stcg(&a.q[e], acc);
+                }
+                level1<1>(v, sl, sm);
+            }
+            level2<1>(a, 1, c0 + base, nslot, sm);
+        }
+        if (!cta_barrier(a, grid, target, sm)) return;
+        double red1[1];
+        reduce_all<1>(a, 1, nchunks, sm, red1);
+        const float alpha = (float)(rz / red1[0]);
+
+        // ---- phase B: x += alpha p, r -= alpha q, z = M^-1 r; publish z, p; partial r.r, r.z
+        for (int base = 0; base < kb; base += 32) {
+            const int nslot = min(32, kb - base);
+            for (int sl = 0; sl < nslot; ++sl) {
+                const int s = base + sl;
+                const int e = (c0 + s) * CHUNK + tid;
+                double v[2] = {0.0, 0.0};
+                if (e < nf) {
+                    float pn, x, r, q;
+                    unsigned fl;
+                    const int l = s * CHUNK + tid;
+                    if (K > 0) {
+                        pn = R.p[l];
+                        x = R.x[l];
+                        r = R.r[l];
+                        q = R.zq[l];
+                        fl = R.fl[l];
+                    } else {
+                        pn = remote_p(a, e, first, beta);
+                        x = __ldcg(&a.x[e]);
+                        r = __ldcg(&a.r[e]);
+                        q = __ldcg(&a.q[e]);
+                        fl = a.flags[e];
+                    }
+                    x = fadd(x, fmul(alpha, pn));
+                    r = fsub(r, fmul(alpha, q));
+                    const float z = fmul(itab[fl >> 2], r);
+                    if (K > 0) {
+                        R.x[l] = x;
+                        R.r[l] = r;
+                        R.zq[l] = z;
+                    } else {
+                        __stcg(&a.x[e], x);
+                        __stcg(&a.r[e], r);
+                    }
+                    __stcg(&a.z[e], z);
+                    __stcg(&a.p[e], pn);
+                    v[0] = dmul((double)r, (double)r);
+                    v[1] = dmul((double)r, (double)z);
+                }
+                level1<2>(v, sl, sm);
+            }
+            level2<2>(a, 0, c0 + base, nslot, sm);
+        }
+        if (!cta_barrier(a, grid, target, sm)) return;
+        reduce_all<2>(a, 0, nchunks, sm, red2);
+        rr = red2[0];
+        iters = it;
+        if (rr < thr) break;
+        beta = (float)(red2[1] / rz);
+        rz = red2[1];
+        first = false;
+    }
+    // ---- the solution (x stayed 0 if no update ran)
+    if (K > 0) {
+        for (int s = 0; s < kb; ++s) {
+            const int e = (c0 + s) * CHUNK + tid;
+            if (e < nf) a.x[e] = R.x[s * CHUNK + tid];
+        }
+    }
+    if (cta == 0 && tid == 0) {
+        a.result->iterations = iters;
+        a.result->rr = rr;
+        a.result->bb = bb;
+        a.result->status = 0;
+    }
+}
+
+__global__ void __launch_bounds__(CG_THREADS, 1) k_cg(CgArgs a)
+{
+    __shared__ Smem sm;
+    extern __shared__ __align__(16) unsigned char dyn[];
+    const int nf = *a.nfluid;
+    const int nchunks = (nf + CHUNK - 1) / CHUNK;
+    if (threadIdx.x < 5) {
+        sm.dtab[threadIdx.x] = a.dtab[threadIdx.x];
+        sm.itab[threadIdx.x] = a.itab[threadIdx.x];
+    }
+    __syncthreads();
+    if (nchunks == 0) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            a.result->iterations = 0;
+            a.result->rr = 0.0;
+            a.result->bb = 0.0;
+            a.result->status = 0;
+        }
+        return;
+    }
+    if (nchunks > a.max_chunks || nchunks > MAX_CHUNKS) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(a.status, ST_TOO_LARGE);
+        return;
+    }
+    if (nchunks <= SINGLE_CTA_CHUNKS) {
+        if (blockIdx.x != 0) return;
+        if (nchunks <= KREG) cg_body<KREG>(a, sm, dyn, nf, nchunks, false);
+        else cg_body<0>(a, sm, dyn, nf, nchunks, false);
+        return;
+    }
+    const int per_cta = (nchunks + gridDim.x - 1) / gridDim.x;
+    if (per_cta <= KREG) cg_body<KREG>(a, sm, dyn, nf, nchunks, true);
+    else cg_body<0>(a, sm, dyn, nf, nchunks, true);
+}
+
+}  // namespace
+
+int cg_prepare(CgWork& w, int device)
+{
+    int sms = 0, per_sm = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) return -1;
+    if (cudaFuncSetAttribute(k_cg, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)RESIDENT_BYTES) != cudaSuccess)
+        return -1;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cg, CG_THREADS, RESIDENT_BYTES) != cudaSuccess)
+        return -1;
+    if (per_sm < 1) return -1;
+    w.grid = sms;  // one CTA per SM: fewer barrier arrivals
+    return 0;
+}
+
+void cg_solve(const Launch& L, CgWork& w, const int32_t* nfluid, const float* b, const float* diag_tab,
+              const int32_t* down, const int32_t* up, const uint8_t* flags, float off, double tol, int maxit,
+              unsigned* status)
+{
+    CgArgs a;
+    a.nfluid = nfluid;
+    a.b = b;
+    a.down = down;
+    a.up = up;
+    a.flags = flags;
+    for (int k = 0; k < 5; ++k) {
+        a.dtab[k] = diag_tab[k];
+        a.itab[k] = diag_tab[k] != 0.0f ? 1.0f / diag_tab[k] : 1.0f;
+    }
+    a.off = off;
+    a.tol2 = tol * tol;
+    a.maxit = maxit;
+    a.x = w.x;
+    a.r = w.r;
+    a.z = w.z;
+    a.p = w.p;
+    a.q = w.q;
+    a.partials = w.partials;
+    a.max_chunks = (int)((w.max_cells + CHUNK - 1) / CHUNK);
+    a.barrier = w.barrier;
+    a.status = status;
+    a.result = w.result;
+    cudaMemsetAsync(w.barrier, 0, sizeof(unsigned), L.stream);
+    void* args[] = {&a};
+    cudaLaunchCooperativeKernel((const void*)k_cg, dim3(w.grid), dim3(CG_THREADS), args, RESIDENT_BYTES, L.stream);
+    L.count();
+}
+
+}  // namespace fs

@@ -1,0 +1,201 @@
+/* fsgpu -- GB300 (sm_103a) implementation of Fluid_Simulation's per-step
+ * PIC/FLIP + MAC-grid + pressure-projection path, behind a C ABI.
+ *
+ * The reference's boundary for this path is a C++ class API:
+ *   FluidDomain(int, int, MyFloat, MyFloat, MyFloat density, MyFloat pic_ratio)
+ *       (include/FluidDomain.h:40-48, src/FluidDomain.cpp:54-68)
+ *   FluidSolverMemoryPool(const FluidDomain&)  (include/FluidSolver.h:17-22)
+ *   FluidSolver(FluidSolverMemoryPool)         (include/FluidSolver.h:48)
+ *   FluidSolver::step{SemiLagrangian,PIC,FLIP,PICFLIP}(FluidDomain&, MyFloat dt)
+ *       (include/FluidSolver.h:51-54, src/FluidSolver.cpp:99-251)
+ * A handle here is one FluidDomain together with its FluidSolver: the grid,
+ * the marker particles and the solver's scratch pool live in device memory
+ * (HBM) for the handle's lifetime.  The C++ drop-in headers in
+ * fluid_simulation_gb300/dropin keep the reference's class API and call these
+ * functions.
+ *
+ * Conventions: every function returns an int status (FS_OK = 0).  Host
+ * pointers are plain host memory; *_device variants take device pointers.
+ * Work is queued on the handle's CUDA stream; functions that return data to
+ * the host synchronise that stream.  A handle is not thread-safe (nor is the
+ * reference's FluidSolver); distinct handles are independent.  Arrays are
+ * row-major, index i + j * size_x (include/Grid.h:63-67); particles are
+ * interleaved {pos_x, pos_y, vel_x, vel_y} floats, the layout of
+ * MarkerParticle (include/MarkerParticleSet.h:43-50).
+ */
+#ifndef FSGPU_H
+#define FSGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define FS_API __attribute__((visibility("default")))
+#else
+#define FS_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes. */
+#define FS_OK 0
+#define FS_ERR_INVALID_ARGUMENT 1
+#define FS_ERR_VALIDATE 2       /* domain/pool mismatch: the reference throws std::runtime_error
+                                   (src/FluidSolver.cpp:89-107, 215-221) */
+#define FS_ERR_CUDA 3
+#define FS_ERR_TIMEOUT 4        /* a bounded device-side wait gave up */
+#define FS_ERR_TOO_LARGE 5
+#define FS_ERR_INTERNAL 6
+#define FS_ERR_OUT_OF_MEMORY 7
+
+/* Warning bits of fs_step_stats.warnings. */
+#define FS_WARN_PARTICLE_OUTSIDE 1u  /* a particle lay outside the grid when pressureSolve counted
+                                        particles per cell; the reference indexes out of bounds there
+                                        (src/FluidSolver.cpp:353-360), this build skips it */
+#define FS_WARN_CG_NOT_CONVERGED 2u  /* the CG stopped at its iteration limit (the reference ignores
+                                        this, src/FluidSolver.cpp:424-425) */
+
+/* CellType (include/MacGrid.h:14-17). */
+#define FS_LIQUID 0
+#define FS_AIR 1
+#define FS_SOLID 2
+
+/* Grids of MacGrid (include/MacGrid.h:164-176). */
+#define FS_U_FRONT 0
+#define FS_V_FRONT 1
+#define FS_U_BACK 2
+#define FS_V_BACK 3
+#define FS_U_PREV 4
+#define FS_V_PREV 5
+#define FS_U_DIFF 6
+#define FS_V_DIFF 7
+
+/* Step methods: FluidSolver::step* (include/FluidSolver.h:51-54). */
+#define FS_STEP_SEMI_LAGRANGIAN 0
+#define FS_STEP_PIC 1
+#define FS_STEP_FLIP 2
+#define FS_STEP_PICFLIP 3
+
+/* Single phases, in the reference's function granularity. */
+#define FS_PH_CLASSIFY 0       /* FluidDomain::classifyCells(MarkerParticleSet&), src/FluidDomain.cpp:150-180 */
+#define FS_PH_P2G 1            /* FluidSolver::transferVelocityToGridSpread, src/FluidSolver.cpp:873-919 */
+#define FS_PH_SAVE_PREV 2      /* MacGrid::updatePreviousVelocityBuffer, src/MacGrid.cpp:52-56 */
+#define FS_PH_GRAVITY 3        /* FluidSolver::addExternalAcceleration, src/FluidSolver.cpp:276-295 */
+#define FS_PH_DIRICHLET 4      /* FluidSolver::enforceDirichlet, src/FluidSolver.cpp:297-321 */
+#define FS_PH_EXTEND 5         /* FluidSolver::extendVelocityIndividual, src/FluidSolver.cpp:485-622 */
+#define FS_PH_PRESSURE 6       /* FluidSolver::pressureSolve, src/FluidSolver.cpp:323-483 */
+#define FS_PH_SAVE_DIFF 7      /* MacGrid::updateVelocityDiffBuffer, src/MacGrid.cpp:58-70 */
+#define FS_PH_G2P_PICFLIP 8    /* FluidSolver::transferVelocityToParticlesPICFLIP, src/FluidSolver.cpp:945-963 */
+#define FS_PH_G2P_PIC 9        /* FluidSolver::transferVelocityToParticlesPIC, src/FluidSolver.cpp:921-931 */
+#define FS_PH_G2P_FLIP 10      /* FluidSolver::transferVelocityToParticlesFLIP, src/FluidSolver.cpp:933-943 */
+#define FS_PH_ADVECT_SAFE 11   /* MarkerParticleSet::advectAndEnsureOutsideObstacles, src/MarkerParticleSet.cpp:48-62 */
+#define FS_PH_ADVECT 12        /* MarkerParticleSet::advect, src/MarkerParticleSet.cpp:40-46 */
+#define FS_PH_SL_VELOCITY 13   /* FluidSolver::advectVelocitySemiLagrangian, src/FluidSolver.cpp:709-772 */
+#define FS_PH_SL_PARTICLES 14  /* FluidSolver::advectParticlesWithGrid, src/FluidSolver.cpp:774-791 */
+#define FS_PH_SWAP 15          /* MacGrid::swapVelocityBuffers, src/MacGrid.cpp:89-93 */
+
+/* Timed phases reported in fs_step_stats.ms_phase when timing is enabled. */
+#define FS_T_CLASSIFY 0   /* labels */
+#define FS_T_P2G 1        /* particle-to-grid transfer (+ previous-velocity copy) */
+#define FS_T_FORCES 2     /* gravity, Dirichlet, velocity extension, semi-Lagrangian advection */
+#define FS_T_ASSEMBLY 3   /* particle counts, fluid indexing, divergence and matrix rows */
+#define FS_T_CG 4         /* the conjugate-gradient kernel */
+#define FS_T_PROJECT 5    /* pressure-gradient update, second Dirichlet, velocity difference */
+#define FS_T_G2P 6        /* grid-to-particle transfer and particle advection */
+#define FS_NUM_TIMED 7
+
+typedef struct fs_config
+{
+    int size_x, size_y;           /* cells */
+    float length_x, length_y;     /* world size; delta = length / size */
+    float density;                /* FluidDomain density (the projection scales by dt / density) */
+    float pic_ratio;              /* FluidDomain pic_ratio in [0, 1] */
+    float gravity_x, gravity_y;   /* reference: (0, -9.82), src/FluidSolver.cpp:232 */
+    int cg_max_iterations;        /* reference: 100, src/FluidSolver.cpp:81 */
+    double cg_tolerance;          /* reference: FLT_EPSILON (Eigen's default) */
+    int extension_iterations;     /* reference: 2, src/FluidSolver.cpp:234 */
+    int device;                   /* CUDA device ordinal */
+    int reserved[8];
+} fs_config;
+
+typedef struct fs_step_stats
+{
+    int cg_iterations;      /* CG updates performed in the last pressure solve */
+    int n_fluid;            /* fluid (LIQUID) cells in the last pressure solve */
+    double cg_residual;     /* ||r|| / ||b|| at exit */
+    unsigned int warnings;  /* FS_WARN_* bits accumulated since the last query */
+    float ms_total;         /* device time of the last fs_step (timing enabled) */
+    float ms_phase[FS_NUM_TIMED];
+} fs_step_stats;
+
+typedef struct fs_handle fs_handle;
+
+/* Fills *cfg with the reference's defaults for a size_x x size_y grid of
+ * unit cells: density 1, pic_ratio 0, gravity (0, -9.82), CG maxit 100,
+ * tolerance FLT_EPSILON, 2 extension sweeps, device 0. */
+FS_API void fs_config_init(fs_config* cfg, int size_x, int size_y);
+
+/* Creates a domain + solver pair on cfg->device (FluidDomain ctor,
+ * FluidSolverMemoryPool(const FluidDomain&), FluidSolver(pool)). */
+FS_API int fs_create(const fs_config* cfg, fs_handle** out);
+FS_API int fs_destroy(fs_handle* h);
+
+/* Message of the last failure on h, or of the last fs_create failure on this
+ * thread when h is NULL. */
+FS_API const char* fs_last_error(const fs_handle* h);
+
+/* Settings that the reference hard-codes or keeps on FluidDomain. */
+FS_API int fs_set_pic_ratio(fs_handle* h, float pic_ratio); /* FluidDomain::setPicRatio: clamps to [0, 1] */
+FS_API int fs_set_gravity(fs_handle* h, float gx, float gy);
+FS_API int fs_set_cg(fs_handle* h, double tolerance, int max_iterations);
+FS_API int fs_set_extension_iterations(fs_handle* h, int n);
+/* Persistent solid cells re-applied after every classification (extension;
+ * the reference re-labels only the border).  mask: size_x*size_y bytes,
+ * non-zero = solid; NULL clears. */
+FS_API int fs_set_solid_mask(fs_handle* h, const uint8_t* mask);
+
+/* Marker particles (MarkerParticleSet, include/MarkerParticleSet.h:53-78). */
+FS_API int fs_set_particles(fs_handle* h, const float* xyuv, int64_t n);
+FS_API int fs_set_particles_device(fs_handle* h, const float* d_xyuv, int64_t n);
+FS_API int fs_add_particles(fs_handle* h, const float* xyuv, int64_t n);
+FS_API int fs_num_particles(fs_handle* h, int64_t* n);
+FS_API int fs_get_particles(fs_handle* h, float* xyuv, int64_t n);
+FS_API int fs_get_particles_device(fs_handle* h, float* d_xyuv, int64_t n);
+
+/* Grid state (host copies). */
+FS_API int fs_get_grid(fs_handle* h, int which, float* out);
+FS_API int fs_set_grid(fs_handle* h, int which, const float* in);
+FS_API int fs_get_labels(fs_handle* h, uint8_t* out);
+FS_API int fs_set_labels(fs_handle* h, const uint8_t* in);
+FS_API int fs_get_fluid_indices(fs_handle* h, int32_t* out);
+FS_API int fs_get_particle_counts(fs_handle* h, uint8_t* out);
+/* Pressure of the last solve scattered to the grid by fluid index (0 elsewhere). */
+FS_API int fs_get_pressure(fs_handle* h, float* out);
+
+/* One step of the given method (FS_STEP_*), queued on the handle's stream. */
+FS_API int fs_step(fs_handle* h, int method, float dt);
+/* One phase (FS_PH_*), queued on the handle's stream. */
+FS_API int fs_phase(fs_handle* h, int phase, float dt);
+/* Waits for queued work; reports device-side failures (FS_ERR_TIMEOUT ...). */
+FS_API int fs_synchronize(fs_handle* h);
+/* Synchronises and returns the statistics of the last step / pressure solve. */
+FS_API int fs_get_stats(fs_handle* h, fs_step_stats* out);
+
+/* Per-phase CUDA-event timing of fs_step (off by default). */
+FS_API int fs_set_timing(fs_handle* h, int enable);
+/* Replays fs_step through a cached CUDA graph of the whole step (default
+ * on); 0 launches kernel by kernel. */
+FS_API int fs_set_graphs(fs_handle* h, int enable);
+/* The handle's CUDA stream (cudaStream_t) and a way to replace it. */
+FS_API void* fs_get_stream(fs_handle* h);
+FS_API int fs_set_stream(fs_handle* h, void* stream);
+/* Number of this library's kernel launches queued so far on h. */
+FS_API int64_t fs_kernel_launches(fs_handle* h);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

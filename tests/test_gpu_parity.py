@@ -1,0 +1,205 @@
+"""GPU parity: the CUDA path (through the C ABI) against the CPU restatement of
+the reference (oracle/fs_oracle.c, itself pinned bit-exact against the
+reference's own code) and against the fixtures recorded from the reference.
+
+Everything here is compared bit for bit: labels, fluid indices and particle
+counts (integers), and every float array (velocity grids front/back/previous/
+difference, pressure, particle positions and velocities).  The GPU follows
+the reference's float evaluation order, and its CG uses the same fixed-order
+FP64 dot products as the oracle's CG, so no tolerance is needed."""
+import os
+
+import numpy as np
+import pytest
+
+import fluid_simulation_gb300 as fsg
+from fluid_simulation_gb300 import build as fsbuild
+from fluid_simulation_gb300 import scenes
+from oracle import pyoracle as po
+from tests.golden import make_golden as mg
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _built():
+    fsbuild.build()
+    fsg.load_library()
+
+
+def pair(sc, cg_tol=None, cg_maxit=None):
+    tol = sc.cg_tolerance if cg_tol is None else cg_tol
+    maxit = sc.cg_max_iterations if cg_maxit is None else cg_maxit
+    g = fsg.FluidSim(sc.size_x, sc.size_y, sc.length_x, sc.length_y, sc.density, sc.pic_ratio,
+                     cg_tolerance=tol, cg_max_iterations=maxit, gravity=sc.gravity)
+    o = po.OracleSim("restatement", sc.size_x, sc.size_y, sc.length_x, sc.length_y, sc.density, sc.pic_ratio)
+    o.set_cg(tol, maxit)
+    o.set_gravity(*sc.gravity)
+    if sc.solid is not None:
+        g.set_solid_mask(sc.solid)
+        o.set_solid_mask(sc.solid)
+    g.set_particles(sc.particles)
+    o.set_particles(sc.particles)
+    return g, o
+
+
+def assert_same(g_state, o_state, keys=None, where=""):
+    for k in keys or o_state.keys():
+        a, b = g_state[k], o_state[k]
+        assert a.shape == b.shape, (where, k, a.shape, b.shape)
+        if not np.array_equal(a.view(np.uint8), b.view(np.uint8)):
+            bad = np.argwhere(a != b) if a.dtype != np.uint8 or True else None
+            first = tuple(bad[0]) if bad is not None and len(bad) else None
+            raise AssertionError("%s %s differs at %d entries, first %s: gpu %r oracle %r" % (
+                where, k, 0 if bad is None else len(bad), first,
+                None if first is None else a[first], None if first is None else b[first]))
+
+
+@pytest.mark.parametrize("method", [fsg.STEP_PICFLIP, fsg.STEP_PIC, fsg.STEP_FLIP, fsg.STEP_SEMI_LAGRANGIAN])
+def test_step_methods_bit_exact(method):
+    sc = scenes.dam_break_small()
+    g, o = pair(sc, cg_maxit=400)
+    for k in range(12):
+        g.step(method, sc.dt)
+        assert o.step(method, sc.dt) == 0
+        assert_same(g.state(), o.state(), where="method %d step %d" % (method, k))
+
+
+def test_picflip_200_steps_bit_exact_with_graphs():
+    """The 64x64 dam break of the small configuration, 200 steps, replayed
+    through the cached CUDA graph of the step."""
+    sc = scenes.dam_break_small()
+    g, o = pair(sc)
+    for k in range(200):
+        g.step(fsg.STEP_PICFLIP, sc.dt)
+        o.step(po.STEP_PICFLIP, sc.dt)
+        if k % 20 == 19 or k < 3:
+            assert_same(g.state(), o.state(), where="step %d" % k)
+            st = g.stats()
+            it, err, nf = o.cg_stats()
+            assert st["cg_iterations"] == it and st["n_fluid"] == nf
+            assert st["cg_residual"] == pytest.approx(err, rel=1e-12, abs=0)
+
+
+@pytest.mark.parametrize("case", sorted(c for c in mg.CASES if c != "picflip_source64"))
+def test_against_reference_fixtures(case, golden_dir):
+    """The GPU against the states recorded from the reference's own code."""
+    ref = np.load(os.path.join(golden_dir, case + ".npz"))
+    method, steps, scene, opt = mg.CASES[case]
+    sc = scenes.dam_break_small()
+    g = fsg.FluidSim(sc.size_x, sc.size_y, sc.length_x, sc.length_y, sc.density, sc.pic_ratio,
+                     cg_tolerance=sc.cg_tolerance, cg_max_iterations=sc.cg_max_iterations)
+    if "disc" in opt:
+        g.set_solid_mask(scenes.disc_mask(sc.size_x, sc.size_y, *opt["disc"]))
+    g.set_particles(sc.particles)
+    for k in range(1, max(steps) + 1):
+        g.step(method, sc.dt)
+        if k in steps:
+            st = g.state()
+            for key in mg.FULL_KEYS:
+                a, b = st[key], ref["s%d_%s" % (k, key)]
+                assert np.array_equal(a.view(np.uint8), b.view(np.uint8)), (case, k, key)
+
+
+PHASES = [fsg.PH_CLASSIFY, fsg.PH_P2G, fsg.PH_SAVE_PREV, fsg.PH_GRAVITY, fsg.PH_DIRICHLET, fsg.PH_EXTEND,
+          fsg.PH_PRESSURE, fsg.PH_SAVE_DIFF, fsg.PH_G2P_PICFLIP, fsg.PH_G2P_PIC, fsg.PH_G2P_FLIP,
+          fsg.PH_ADVECT_SAFE, fsg.PH_ADVECT, fsg.PH_SL_VELOCITY, fsg.PH_SL_PARTICLES, fsg.PH_SWAP]
+
+
+@pytest.mark.parametrize("ph", PHASES)
+@pytest.mark.parametrize("n", [64, 97])
+def test_single_phase_on_random_state(ph, n):
+    """Each phase from an identical randomised state: random velocities on all
+    eight grids, particles jittered (incl. negative and out-of-grid positions
+    where the reference clamps), a solid obstacle, pic ratio 0.3."""
+    rng = np.random.default_rng(1000 * ph + n)
+    sc = scenes.dam_break_small() if n == 64 else scenes.Scene(
+        n, n, float(n), float(n), 0.005, 0.05, 0.005,
+        scenes.block_particles(n, n, float(n), float(n), 1, n // 2, 1, 2 * n // 3, 5, 7),
+        solid=scenes.disc_mask(n, n, 0.7 * n, 0.3 * n, 0.1 * n), cg_tolerance=1e-6, cg_max_iterations=500)
+    g, o = pair(sc)
+    for s in (g, o):
+        s.step(fsg.STEP_PICFLIP, sc.dt)
+    parts = o.particles()
+    parts[:, 2:] = rng.standard_normal((parts.shape[0], 2)).astype(np.float32)
+    if ph != fsg.PH_PRESSURE:
+        parts[:6, 0] = np.array([-0.3, -2.5, 0.0, n - 0.01, n + 6.0, -1e-8], np.float32)
+        parts[6:9, 1] = np.array([-0.7, n + 0.2, 0.5], np.float32)
+    grids = [rng.standard_normal((n, n)).astype(np.float32) for _ in range(8)]
+    for s in (g, o):
+        for w, arr in enumerate(grids):
+            s.set_grid(w, arr)
+        s.set_particles(parts)
+        s.set_pic_ratio(0.3)
+    g.phase(ph, sc.dt)
+    assert o.phase(ph, sc.dt) == 0
+    assert_same(g.state(), o.state(), where="phase %d" % ph)
+
+
+def test_obstacle_and_gravity_override():
+    n = 80
+    solid = scenes.disc_mask(n, n, 55.0, 20.0, 9.0)
+    sc = scenes.Scene(n, n, float(n), float(n), 0.005, 0.05, 0.005,
+                      scenes.block_particles(n, n, float(n), float(n), 1, 30, 1, 50, 4, 3, solid),
+                      solid=solid, gravity=(0.0, -9.81), cg_tolerance=1e-5, cg_max_iterations=3000)
+    g, o = pair(sc)
+    for k in range(60):
+        g.step(fsg.STEP_PICFLIP, sc.dt)
+        o.step(po.STEP_PICFLIP, sc.dt)
+    assert_same(g.state(), o.state(), where="obstacle")
+
+
+def test_large_grid_one_step_bit_exact():
+    """512x512 dam break with an obstacle (~440k particles), one full step:
+    multi-CTA CG with grid barriers, shared-memory-resident CG state."""
+    sc = scenes.dam_break_large(512)
+    g, o = pair(sc)
+    g.step(fsg.STEP_PICFLIP, sc.dt)
+    o.step(po.STEP_PICFLIP, sc.dt)
+    assert_same(g.state(), o.state(), where="512")
+    st = g.stats()
+    it, err, nf = o.cg_stats()
+    assert (st["cg_iterations"], st["n_fluid"]) == (it, nf)
+    assert st["cg_residual"] < sc.cg_tolerance
+
+
+def test_streaming_cg_matches_oracle():
+    """A fluid region too large for the shared-memory-resident CG (more than
+    8 x 1024 fluid cells per CTA): the streaming variant of the same kernel."""
+    n = 1280
+    sc = scenes.Scene(n, n, float(n), float(n), 0.01, 0.05, 0.01,
+                      scenes.block_particles(n, n, float(n), float(n), 1, n - 1, 1, n - 1, 1, 11),
+                      cg_tolerance=1e-3, cg_max_iterations=60)
+    g, o = pair(sc)
+    g.step(fsg.STEP_PICFLIP, sc.dt)
+    o.step(po.STEP_PICFLIP, sc.dt)
+    st = g.stats()
+    it, err, nf = o.cg_stats()
+    assert nf > 8 * 1024 * 152
+    assert (st["cg_iterations"], st["n_fluid"]) == (it, nf)
+    assert_same(g.state(), o.state(), keys=["pressure", "u_front", "v_front", "labels", "particles"], where="1280")
+
+
+def test_non_square_cells_rejected_like_reference():
+    g = fsg.FluidSim(32, 16, 32.0, 32.0, 0.005, 0.05)
+    with pytest.raises(fsg.FsError) as ei:
+        g.step(fsg.STEP_PICFLIP, 0.005)
+    assert ei.value.code == 2
+
+
+def test_empty_domain_and_no_fluid():
+    """No particles: no fluid cell, the pressure solve returns before solving
+    and swapping (src/FluidSolver.cpp:347-350)."""
+    sc = scenes.dam_break_small()
+    sc.particles = sc.particles[:0]
+    g, o = pair(sc)
+    rng = np.random.default_rng(5)
+    grids = [rng.standard_normal((64, 64)).astype(np.float32) for _ in range(8)]
+    for s in (g, o):
+        for w, arr in enumerate(grids):
+            s.set_grid(w, arr)
+    for _ in range(3):
+        g.step(fsg.STEP_PICFLIP, sc.dt)
+        o.step(po.STEP_PICFLIP, sc.dt)
+    assert_same(g.state(), o.state(), where="empty")
+    assert g.stats()["n_fluid"] == 0
