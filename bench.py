@@ -47,6 +47,7 @@ def parse():
     ap.add_argument("--impl", choices=["gpu", "reference"], default="gpu")
     ap.add_argument("--size", type=int, default=1024)
     ap.add_argument("--cpu-budget", type=float, default=150.0, help="seconds of CPU work for CPU timings")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample (profiling runs)")
     return ap.parse_args()
 
 
@@ -327,8 +328,11 @@ def run_gpu(args, rank, world, local_rank):
     traffic = read_traffic()
     # CPU baseline: the oracle on the state at the start of the timed region
     kind = cpu_oracle_kind()
-    o = cpu_sim_from_state(sc, kind, grids0, parts0)
-    ctimes = time_cpu_steps(o, sc, 1, args.cpu_budget)
+    if args.no_cpu:
+        ctimes = [float("nan")]
+    else:
+        o = cpu_sim_from_state(sc, kind, grids0, parts0)
+        ctimes = time_cpu_steps(o, sc, 1, args.cpu_budget)
     cpu_value = sc.cells * len(ctimes) / sum(ctimes)
     clocks = clk.summary()
     line = {

@@ -27,6 +27,7 @@ STEP_SEMI_LAGRANGIAN, STEP_PIC, STEP_FLIP, STEP_PICFLIP = range(4)
 (PH_CLASSIFY, PH_P2G, PH_SAVE_PREV, PH_GRAVITY, PH_DIRICHLET, PH_EXTEND, PH_PRESSURE, PH_SAVE_DIFF,
  PH_G2P_PICFLIP, PH_G2P_PIC, PH_G2P_FLIP, PH_ADVECT_SAFE, PH_ADVECT, PH_SL_VELOCITY, PH_SL_PARTICLES,
  PH_SWAP) = range(16)
+CG_FLOAT, CG_DOUBLE = 0, 1
 TIMED_PHASES = ("classify", "p2g", "forces", "assembly", "cg", "project", "g2p")
 
 
@@ -40,7 +41,8 @@ class fs_config(C.Structure):
     _fields_ = [("size_x", C.c_int), ("size_y", C.c_int), ("length_x", C.c_float), ("length_y", C.c_float),
                 ("density", C.c_float), ("pic_ratio", C.c_float), ("gravity_x", C.c_float),
                 ("gravity_y", C.c_float), ("cg_max_iterations", C.c_int), ("cg_tolerance", C.c_double),
-                ("extension_iterations", C.c_int), ("device", C.c_int), ("reserved", C.c_int * 8)]
+                ("extension_iterations", C.c_int), ("device", C.c_int), ("cg_precision", C.c_int),
+                ("reserved", C.c_int * 7)]
 
 
 class fs_step_stats(C.Structure):
@@ -58,6 +60,7 @@ SIGNATURES = {
     "fs_set_pic_ratio": (_i, [_vp, _f]),
     "fs_set_gravity": (_i, [_vp, _f, _f]),
     "fs_set_cg": (_i, [_vp, _d, _i]),
+    "fs_set_cg_precision": (_i, [_vp, _i]),
     "fs_set_extension_iterations": (_i, [_vp, _i]),
     "fs_set_solid_mask": (_i, [_vp, _vp]),
     "fs_set_particles": (_i, [_vp, _vp, _i64]),
@@ -167,6 +170,10 @@ class FluidSim:
     # settings
     def set_cg(self, tol: float, maxit: int) -> None:
         self._check(self.lib.fs_set_cg(self.h, float(tol), int(maxit)))
+
+    def set_cg_precision(self, precision: int) -> None:
+        """CG_FLOAT (0, the reference's precision) or CG_DOUBLE (1)."""
+        self._check(self.lib.fs_set_cg_precision(self.h, int(precision)))
 
     def set_gravity(self, gx: float, gy: float) -> None:
         self._check(self.lib.fs_set_gravity(self.h, gx, gy))

@@ -12,14 +12,17 @@
 //   * vectors and SpMV in float, each product and sum rounded on its own; a
 //     row sums its terms in ascending column order (down, left, centre,
 //     right, up) starting from +0;
-//   * dot products accumulate exact float*float products in double along the
-//     fixed "32-ary stride-halving tree" (groups of 32 consecutive elements,
-//     s = 16..1: a[l] += a[l+s], repeated on the group results) -- a warp
-//     shuffle tree, then a tree over warps (one 1024-element chunk per CTA
-//     pass), then a tree over chunk partials that every CTA evaluates
-//     redundantly after a grid barrier.  The result does not depend on the
-//     launch shape;
-//   * alpha and beta are formed in double and rounded once to float.
+//   * dot products sum their terms along the fixed "32-ary stride-halving
+//     tree" (groups of 32 consecutive elements, s = 16..1: a[l] += a[l+s],
+//     repeated on the group results) -- a warp shuffle tree, then a tree over
+//     warps (one 1024-element chunk per CTA pass), then a tree over chunk
+//     partials that every CTA evaluates redundantly after a grid barrier.  The
+//     result does not depend on the launch shape.  Two precisions (template
+//     parameter R): float products, sums, alpha, beta and threshold -- the
+//     precision of the reference's Eigen VectorXf CG, and the default; or
+//     exact float*float products summed in double with alpha and beta rounded
+//     once to float.  GB300's FP64 rate is a small fraction of its FP32 rate,
+//     so the double variant costs FP64 issue slots in every reduction.
 //
 // Per iteration there are two grid barriers (after p.q and after r.r, r.z).
 // The search direction p_new = z + beta p_old is not exchanged through a third
@@ -52,8 +55,9 @@ struct CgArgs
     float dtab[5];         // diagonal by non-solid count: (float)(-n / dx^2)
     float itab[5];         // 1 / diagonal, or 1 where the diagonal is 0
     float off;             // (float)(1 / dx^2)
-    double tol2;
+    double tol;
     int maxit;
+    int fp64;                  // 0: float dot products, 1: double
     float *x, *r, *z, *p, *q;  // fluid-index vectors (global)
     double* partials;          // [2 buffers][2 values][MAX chunks]
     int max_chunks;
@@ -67,77 +71,115 @@ struct Smem
     union {
         double red[32][32][2];  // level-1 results: [chunk slot][warp][value]
         double lvlA[1024][2];
+        float redf[32][32][2];
+        float lvlAf[1024][2];
     };
-    double lvlB[32][2];
+    union {
+        double lvlB[32][2];
+        float lvlBf[32][2];
+    };
     float dtab[5];
     float itab[5];
     int flag;
 };
 
-__device__ __forceinline__ double warp_tree(double v)
+// Arithmetic of the reduction type R, each operation rounded on its own.
+template <typename R> struct Ar;
+template <> struct Ar<float>
+{
+    static __device__ __forceinline__ float add(float a, float b) { return fadd(a, b); }
+    static __device__ __forceinline__ float mul(float a, float b) { return fmul(a, b); }
+    static __device__ __forceinline__ float prod(float a, float b) { return fmul(a, b); }
+    static __device__ __forceinline__ float ratio(float a, float b) { return fdiv(a, b); }
+    static __device__ __forceinline__ float tiny() { return 1.17549435e-38f; }
+    static __device__ __forceinline__ float& red(Smem& s, int a, int b, int k) { return s.redf[a][b][k]; }
+    static __device__ __forceinline__ float& lvlA(Smem& s, int a, int k) { return s.lvlAf[a][k]; }
+    static __device__ __forceinline__ float& lvlB(Smem& s, int a, int k) { return s.lvlBf[a][k]; }
+};
+template <> struct Ar<double>
+{
+    static __device__ __forceinline__ double add(double a, double b) { return dadd(a, b); }
+    static __device__ __forceinline__ double mul(double a, double b) { return dmul(a, b); }
+    static __device__ __forceinline__ double prod(float a, float b) { return dmul((double)a, (double)b); }
+    static __device__ __forceinline__ float ratio(double a, double b) { return (float)(a / b); }
+    static __device__ __forceinline__ double tiny() { return 2.2250738585072014e-308; }
+    static __device__ __forceinline__ double& red(Smem& s, int a, int b, int k) { return s.red[a][b][k]; }
+    static __device__ __forceinline__ double& lvlA(Smem& s, int a, int k) { return s.lvlA[a][k]; }
+    static __device__ __forceinline__ double& lvlB(Smem& s, int a, int k) { return s.lvlB[a][k]; }
+};
+
+template <typename R>
+__device__ __forceinline__ R warp_tree(R v)
 {
 #pragma unroll
-    for (int s = 16; s >= 1; s >>= 1) v = dadd(v, __shfl_down_sync(0xffffffffu, v, s));
+    for (int s = 16; s >= 1; s >>= 1) v = Ar<R>::add(v, __shfl_down_sync(0xffffffffu, v, s));
     return v;
 }
 
-// Barrier over the active CTAs.  Returns false if any CTA timed out.
+// Barrier over the active CTAs.  Thread 0 arrives with a release reduction on
+// the counter (bar.sync first makes the CTA's writes part of what it
+// releases) and spins with acquire loads; the closing bar.sync hands the
+// acquired view to the other threads, which read shared data with ld.cg.
+// Returns false if this CTA gave up waiting (after WAIT_LIMIT_NS); a CTA that
+// gives up returns, so every other CTA also gives up at its next barrier.
 __device__ __forceinline__ bool cta_barrier(const CgArgs& a, bool grid, unsigned& target, Smem& sm)
 {
     __syncthreads();
     if (grid && threadIdx.x == 0) {
         target += gridDim.x;
-        __threadfence();
         red_release_add_u32(a.barrier, 1u);
-        const uint64_t t0 = globaltimer_ns();
-        while (ld_acquire_u32(a.barrier) < target) {
-            if (globaltimer_ns() - t0 > WAIT_LIMIT_NS) {
-                atomicOr(a.status, ST_TIMEOUT);
-                break;
+        int ok = 1;
+        if (ld_acquire_u32(a.barrier) < target) {
+            const uint64_t t0 = globaltimer_ns();
+            while (ld_acquire_u32(a.barrier) < target) {
+                if (globaltimer_ns() - t0 > WAIT_LIMIT_NS) {
+                    atomicOr(a.status, ST_TIMEOUT);
+                    ok = 0;
+                    break;
+                }
             }
-            __nanosleep(32);
         }
-        __threadfence();
+        sm.flag = ok;
     }
-    if (threadIdx.x == 0) sm.flag = (*(volatile unsigned*)a.status & ST_TIMEOUT) ? 1 : 0;
     __syncthreads();
-    return sm.flag == 0;
+    return !grid || sm.flag != 0;
 }
 
 // Level-1 (warp) tree of NV values for chunk slot `slot`; lane 0 keeps it.
-template <int NV>
-__device__ __forceinline__ void level1(const double (&v)[NV], int slot, Smem& sm)
+template <typename R, int NV>
+__device__ __forceinline__ void level1(const R (&v)[NV], int slot, Smem& sm)
 {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
     for (int k = 0; k < NV; ++k) {
-        const double t = warp_tree(v[k]);
-        if (lane == 0) sm.red[slot][warp][k] = t;
+        const R t = warp_tree<R>(v[k]);
+        if (lane == 0) Ar<R>::red(sm, slot, warp, k) = t;
     }
 }
 
-// Level-2 trees for slots [0, nslots) -> chunk partials partials[buf][k][chunk0 + slot].
-template <int NV>
+// Level-2 trees for slots [0, nslots) -> chunk partials part[buf][k][chunk0 + slot].
+template <typename R, int NV>
 __device__ __forceinline__ void level2(const CgArgs& a, int buf, int chunk0, int nslots, Smem& sm)
 {
     __syncthreads();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    R* part = reinterpret_cast<R*>(a.partials);
     if (warp < nslots) {
 #pragma unroll
         for (int k = 0; k < NV; ++k) {
-            const double t = warp_tree(sm.red[warp][lane][k]);
-            if (lane == 0) __stcg(&a.partials[((size_t)buf * 2 + k) * a.max_chunks + chunk0 + warp], t);
+            const R t = warp_tree<R>(Ar<R>::red(sm, warp, lane, k));
+            if (lane == 0) __stcg(&part[((size_t)buf * 2 + k) * a.max_chunks + chunk0 + warp], t);
         }
     }
     __syncthreads();
 }
 
 // Levels 3+: every CTA reduces all chunk partials of buffer buf.
-template <int NV>
-__device__ __forceinline__ void reduce_all(const CgArgs& a, int buf, int nchunks, Smem& sm, double (&out)[NV])
+template <typename R, int NV>
+__device__ __forceinline__ void reduce_all(const CgArgs& a, int buf, int nchunks, Smem& sm, R (&out)[NV])
 {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const double* src = a.partials + (size_t)buf * 2 * a.max_chunks;
+    const R* src = reinterpret_cast<const R*>(a.partials) + (size_t)buf * 2 * a.max_chunks;
     if (nchunks == 1) {
 #pragma unroll
         for (int k = 0; k < NV; ++k) out[k] = __ldcg(&src[(size_t)k * a.max_chunks]);
@@ -148,9 +190,9 @@ __device__ __forceinline__ void reduce_all(const CgArgs& a, int buf, int nchunks
         const int e = g * 32 + lane;
 #pragma unroll
         for (int k = 0; k < NV; ++k) {
-            const double v = e < nchunks ? __ldcg(&src[(size_t)k * a.max_chunks + e]) : 0.0;
-            const double t = warp_tree(v);
-            if (lane == 0) sm.lvlA[g][k] = t;
+            const R v = e < nchunks ? __ldcg(&src[(size_t)k * a.max_chunks + e]) : R(0);
+            const R t = warp_tree<R>(v);
+            if (lane == 0) Ar<R>::lvlA(sm, g, k) = t;
         }
     }
     __syncthreads();
@@ -161,13 +203,13 @@ __device__ __forceinline__ void reduce_all(const CgArgs& a, int buf, int nchunks
             const int e = warp * 32 + lane;
 #pragma unroll
             for (int k = 0; k < NV; ++k) {
-                double v;
-                if (inA) v = e < n ? sm.lvlA[e][k] : 0.0;
-                else v = e < n ? sm.lvlB[e][k] : 0.0;
-                const double t = warp_tree(v);
+                R v;
+                if (inA) v = e < n ? Ar<R>::lvlA(sm, e, k) : R(0);
+                else v = e < n ? Ar<R>::lvlB(sm, e, k) : R(0);
+                const R t = warp_tree<R>(v);
                 if (lane == 0) {
-                    if (inA) sm.lvlB[warp][k] = t;
-                    else sm.lvlA[warp][k] = t;
+                    if (inA) Ar<R>::lvlB(sm, warp, k) = t;
+                    else Ar<R>::lvlA(sm, warp, k) = t;
                 }
             }
         }
@@ -176,7 +218,7 @@ __device__ __forceinline__ void reduce_all(const CgArgs& a, int buf, int nchunks
         n = m;
     }
 #pragma unroll
-    for (int k = 0; k < NV; ++k) out[k] = inA ? sm.lvlA[0][k] : sm.lvlB[0][k];
+    for (int k = 0; k < NV; ++k) out[k] = inA ? Ar<R>::lvlA(sm, 0, k) : Ar<R>::lvlB(sm, 0, k);
     __syncthreads();
 }
 
@@ -216,7 +258,7 @@ __device__ __forceinline__ Resident resident(unsigned char* dyn, int K)
 
 // One CG solve.  K > 0: the CTA's cells (at most K chunks) live in shared
 // memory; K == 0: the state streams from global memory.
-template <int K>
+template <int K, typename R>
 __device__ void cg_body(const CgArgs& a, Smem& sm, unsigned char* dyn, int nf, int nchunks, bool grid)
 {
     const int tid = threadIdx.x;
@@ -228,7 +270,7 @@ __device__ void cg_body(const CgArgs& a, Smem& sm, unsigned char* dyn, int nf, i
     const int e0 = c0 * CHUNK;             // owned element range [e0, e1)
     const int e1 = min(c1 * CHUNK, nf);
     unsigned target = 0;
-    const Resident R = resident(dyn, K > 0 ? K : 1);
+    const Resident RS = resident(dyn, K > 0 ? K : 1);
     const float* dtab = sm.dtab;
     const float* itab = sm.itab;
 
@@ -238,42 +280,43 @@ __device__ void cg_body(const CgArgs& a, Smem& sm, unsigned char* dyn, int nf, i
         for (int sl = 0; sl < nslot; ++sl) {
             const int s = base + sl;
             const int e = (c0 + s) * CHUNK + tid;
-            double v[2] = {0.0, 0.0};
+            R v[2] = {R(0), R(0)};
             if (e < nf) {
                 const float r = a.b[e];
                 const uint8_t fl = a.flags[e];
                 const float z = fmul(itab[fl >> 2], r);
                 __stcg(&a.z[e], z);
-                v[0] = dmul((double)r, (double)r);
-                v[1] = dmul((double)r, (double)z);
+                v[0] = Ar<R>::prod(r, r);
+                v[1] = Ar<R>::prod(r, z);
                 if (K > 0) {
                     const int l = s * CHUNK + tid;
-                    R.x[l] = 0.0f;
-                    R.r[l] = r;
-                    R.zq[l] = z;
-                    R.p[l] = 0.0f;
-                    R.dn[l] = a.down[e];
-                    R.up[l] = a.up[e];
-                    R.fl[l] = fl;
+                    RS.x[l] = 0.0f;
+                    RS.r[l] = r;
+                    RS.zq[l] = z;
+                    RS.p[l] = 0.0f;
+                    RS.dn[l] = a.down[e];
+                    RS.up[l] = a.up[e];
+                    RS.fl[l] = fl;
                 } else {
                     __stcg(&a.x[e], 0.0f);
                     __stcg(&a.r[e], r);
                 }
             }
-            level1<2>(v, sl, sm);
+            level1<R, 2>(v, sl, sm);
         }
-        level2<2>(a, 0, c0 + base, nslot, sm);
+        level2<R, 2>(a, 0, c0 + base, nslot, sm);
     }
     if (!cta_barrier(a, grid, target, sm)) return;
-    double red2[2];
-    reduce_all<2>(a, 0, nchunks, sm, red2);
-    const double bb = red2[0];
-    double rz = red2[1];
-    double rr = bb;
+    R red2[2];
+    reduce_all<R, 2>(a, 0, nchunks, sm, red2);
+    const R bb = red2[0];
+    R rz = red2[1];
+    R rr = bb;
     int iters = 0;
-    bool done = bb == 0.0;
-    double thr = a.tol2 * bb;
-    if (thr < 2.2250738585072014e-308) thr = 2.2250738585072014e-308;
+    bool done = bb == R(0);
+    const R tolr = (R)a.tol;
+    R thr = Ar<R>::mul(Ar<R>::mul(tolr, tolr), bb);
+    if (thr < Ar<R>::tiny()) thr = Ar<R>::tiny();
     if (!done && rr < thr) done = true;
 
     bool first = true;
@@ -283,7 +326,7 @@ __device__ void cg_body(const CgArgs& a, Smem& sm, unsigned char* dyn, int nf, i
         if (K > 0) {
             for (int s = 0; s < kb; ++s) {
                 const int l = s * CHUNK + tid;
-                if ((c0 + s) * CHUNK + tid < nf) R.p[l] = first ? R.zq[l] : fadd(R.zq[l], fmul(beta, R.p[l]));
+                if ((c0 + s) * CHUNK + tid < nf) RS.p[l] = first ? RS.zq[l] : fadd(RS.zq[l], fmul(beta, RS.p[l]));
             }
             __syncthreads();
         }
@@ -293,16 +336,16 @@ __device__ void cg_body(const CgArgs& a, Smem& sm, unsigned char* dyn, int nf, i
                 const int s = base + sl;
                 const int e = (c0 + s) * CHUNK + tid;
                 const int l = s * CHUNK + tid;
-                double v[1] = {0.0};
+                R v[1] = {R(0)};
                 if (e < nf) {
                     float pe;
                     unsigned fl;
                     int dn, up;
                     if (K > 0) {
-                        pe = R.p[l];
-                        fl = R.fl[l];
-                        dn = R.dn[l];
-                        up = R.up[l];
+                        pe = RS.p[l];
+                        fl = RS.fl[l];
+                        dn = RS.dn[l];
+                        up = RS.up[l];
                     } else {
                         pe = remote_p(a, e, first, beta);
                         fl = a.flags[e];
@@ -310,7 +353,7 @@ __device__ void cg_body(const CgArgs& a, Smem& sm, unsigned char* dyn, int nf, i
                         up = a.up[e];
                     }
                     auto pv = [&](int n) -> float {
-                        if (K > 0 && n >= e0 && n < e1) return R.p[n - e0];
+                        if (K > 0 && n >= e0 && n < e1) return RS.p[n - e0];
                         return remote_p(a, n, first, beta);
                     };
                     float acc = 0.0f;
@@ -319,18 +362,18 @@ __device__ void cg_body(const CgArgs& a, Smem& sm, unsigned char* dyn, int nf, i
                     acc = fadd(acc, fmul(dtab[fl >> 2], pe));
                     if (fl & 2u) acc = fadd(acc, fmul(a.off, pv(e + 1)));
                     if (up >= 0) acc = fadd(acc, fmul(a.off, pv(up)));
-                    v[0] = dmul((double)pe, (double)acc);
-                    if (K > 0) R.zq[l] = acc;  // z is no longer needed: it is folded into p
+                    v[0] = Ar<R>::prod(pe, acc);
+                    if (K > 0) RS.zq[l] = acc;  // z is no longer needed: it is folded into p
                     else __stcg(&a.q[e], acc);
                 }
-                level1<1>(v, sl, sm);
+                level1<R, 1>(v, sl, sm);
             }
-            level2<1>(a, 1, c0 + base, nslot, sm);
+            level2<R, 1>(a, 1, c0 + base, nslot, sm);
         }
         if (!cta_barrier(a, grid, target, sm)) return;
-        double red1[1];
-        reduce_all<1>(a, 1, nchunks, sm, red1);
-        const float alpha = (float)(rz / red1[0]);
+        R red1[1];
+        reduce_all<R, 1>(a, 1, nchunks, sm, red1);
+        const float alpha = Ar<R>::ratio(rz, red1[0]);
 
         // ---- phase B: x += alpha p, r -= alpha q, z = M^-1 r; publish z, p; partial r.r, r.z
         for (int base = 0; base < kb; base += 32) {
@@ -338,17 +381,17 @@ __device__ void cg_body(const CgArgs& a, Smem& sm, unsigned char* dyn, int nf, i
             for (int sl = 0; sl < nslot; ++sl) {
                 const int s = base + sl;
                 const int e = (c0 + s) * CHUNK + tid;
-                double v[2] = {0.0, 0.0};
+                R v[2] = {R(0), R(0)};
                 if (e < nf) {
                     float pn, x, r, q;
                     unsigned fl;
                     const int l = s * CHUNK + tid;
                     if (K > 0) {
-                        pn = R.p[l];
-                        x = R.x[l];
-                        r = R.r[l];
-                        q = R.zq[l];
-                        fl = R.fl[l];
+                        pn = RS.p[l];
+                        x = RS.x[l];
+                        r = RS.r[l];
+                        q = RS.zq[l];
+                        fl = RS.fl[l];
                     } else {
                         pn = remote_p(a, e, first, beta);
                         x = __ldcg(&a.x[e]);
@@ -360,28 +403,28 @@ __device__ void cg_body(const CgArgs& a, Smem& sm, unsigned char* dyn, int nf, i
                     r = fsub(r, fmul(alpha, q));
                     const float z = fmul(itab[fl >> 2], r);
                     if (K > 0) {
-                        R.x[l] = x;
-                        R.r[l] = r;
-                        R.zq[l] = z;
+                        RS.x[l] = x;
+                        RS.r[l] = r;
+                        RS.zq[l] = z;
                     } else {
                         __stcg(&a.x[e], x);
                         __stcg(&a.r[e], r);
                     }
                     __stcg(&a.z[e], z);
                     __stcg(&a.p[e], pn);
-                    v[0] = dmul((double)r, (double)r);
-                    v[1] = dmul((double)r, (double)z);
+                    v[0] = Ar<R>::prod(r, r);
+                    v[1] = Ar<R>::prod(r, z);
                 }
-                level1<2>(v, sl, sm);
+                level1<R, 2>(v, sl, sm);
             }
-            level2<2>(a, 0, c0 + base, nslot, sm);
+            level2<R, 2>(a, 0, c0 + base, nslot, sm);
         }
         if (!cta_barrier(a, grid, target, sm)) return;
-        reduce_all<2>(a, 0, nchunks, sm, red2);
+        reduce_all<R, 2>(a, 0, nchunks, sm, red2);
         rr = red2[0];
         iters = it;
         if (rr < thr) break;
-        beta = (float)(red2[1] / rz);
+        beta = Ar<R>::ratio(red2[1], rz);
         rz = red2[1];
         first = false;
     }
@@ -389,13 +432,13 @@ __device__ void cg_body(const CgArgs& a, Smem& sm, unsigned char* dyn, int nf, i
     if (K > 0) {
         for (int s = 0; s < kb; ++s) {
             const int e = (c0 + s) * CHUNK + tid;
-            if (e < nf) a.x[e] = R.x[s * CHUNK + tid];
+            if (e < nf) a.x[e] = RS.x[s * CHUNK + tid];
         }
     }
     if (cta == 0 && tid == 0) {
         a.result->iterations = iters;
-        a.result->rr = rr;
-        a.result->bb = bb;
+        a.result->rr = (double)rr;
+        a.result->bb = (double)bb;
         a.result->status = 0;
     }
 }
@@ -424,15 +467,17 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(CgArgs a)
         if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(a.status, ST_TOO_LARGE);
         return;
     }
-    if (nchunks <= SINGLE_CTA_CHUNKS) {
-        if (blockIdx.x != 0) return;
-        if (nchunks <= KREG) cg_body<KREG>(a, sm, dyn, nf, nchunks, false);
-        else cg_body<0>(a, sm, dyn, nf, nchunks, false);
-        return;
+    const bool grid = nchunks > SINGLE_CTA_CHUNKS;
+    if (!grid && blockIdx.x != 0) return;
+    const int per_cta = grid ? (nchunks + gridDim.x - 1) / gridDim.x : nchunks;
+    const bool resident = per_cta <= KREG;
+    if (a.fp64) {
+        if (resident) cg_body<KREG, double>(a, sm, dyn, nf, nchunks, grid);
+        else cg_body<0, double>(a, sm, dyn, nf, nchunks, grid);
+    } else {
+        if (resident) cg_body<KREG, float>(a, sm, dyn, nf, nchunks, grid);
+        else cg_body<0, float>(a, sm, dyn, nf, nchunks, grid);
     }
-    const int per_cta = (nchunks + gridDim.x - 1) / gridDim.x;
-    if (per_cta <= KREG) cg_body<KREG>(a, sm, dyn, nf, nchunks, true);
-    else cg_body<0>(a, sm, dyn, nf, nchunks, true);
 }
 
 }  // namespace
@@ -452,7 +497,7 @@ int cg_prepare(CgWork& w, int device)
 
 void cg_solve(const Launch& L, CgWork& w, const int32_t* nfluid, const float* b, const float* diag_tab,
               const int32_t* down, const int32_t* up, const uint8_t* flags, float off, double tol, int maxit,
-              unsigned* status)
+              int fp64, unsigned* status)
 {
     CgArgs a;
     a.nfluid = nfluid;
@@ -465,8 +510,9 @@ void cg_solve(const Launch& L, CgWork& w, const int32_t* nfluid, const float* b,
         a.itab[k] = diag_tab[k] != 0.0f ? 1.0f / diag_tab[k] : 1.0f;
     }
     a.off = off;
-    a.tol2 = tol * tol;
+    a.tol = tol;
     a.maxit = maxit;
+    a.fp64 = fp64;
     a.x = w.x;
     a.r = w.r;
     a.z = w.z;

@@ -117,15 +117,16 @@ struct CgResult
 struct CgWork
 {
     float *x, *r, *z, *p, *q;
-    double* partials;   // 3 * 2 * max_chunks
+    double* partials;   // [2 buffers][2 values][max_chunks] (float or double)
     unsigned* barrier;  // grid barrier counter (reset by cg_solve)
     CgResult* result;
     int64_t max_cells;
     int grid;           // co-resident CTAs of the cooperative launch
 };
 int cg_prepare(CgWork& w, int device);  // picks the cooperative grid size
-void cg_solve(const Launch& L, CgWork& w, const int32_t* nfluid, const float* b, const float* diag,
+// fp64: 0 = float dot products (the reference's precision), 1 = double.
+void cg_solve(const Launch& L, CgWork& w, const int32_t* nfluid, const float* b, const float* diag_tab,
               const int32_t* down, const int32_t* up, const uint8_t* flags, float off, double tol, int maxit,
-              unsigned* status);
+              int fp64, unsigned* status);
 
 }  // namespace fs

@@ -96,6 +96,13 @@ extern "C" {
 #define FS_PH_SL_PARTICLES 14  /* FluidSolver::advectParticlesWithGrid, src/FluidSolver.cpp:774-791 */
 #define FS_PH_SWAP 15          /* MacGrid::swapVelocityBuffers, src/MacGrid.cpp:89-93 */
 
+/* Precision of the CG dot products.  FS_CG_FLOAT sums float products in
+ * float, the precision of the reference's Eigen::ConjugateGradient over
+ * VectorXf; FS_CG_DOUBLE sums exact float*float products in double.  Both use
+ * one fixed summation order, so results are reproducible run to run. */
+#define FS_CG_FLOAT 0
+#define FS_CG_DOUBLE 1
+
 /* Timed phases reported in fs_step_stats.ms_phase when timing is enabled. */
 #define FS_T_CLASSIFY 0   /* labels */
 #define FS_T_P2G 1        /* particle-to-grid transfer (+ previous-velocity copy) */
@@ -117,7 +124,8 @@ typedef struct fs_config
     double cg_tolerance;          /* reference: FLT_EPSILON (Eigen's default) */
     int extension_iterations;     /* reference: 2, src/FluidSolver.cpp:234 */
     int device;                   /* CUDA device ordinal */
-    int reserved[8];
+    int cg_precision;             /* FS_CG_FLOAT (default) or FS_CG_DOUBLE */
+    int reserved[7];
 } fs_config;
 
 typedef struct fs_step_stats
@@ -150,6 +158,7 @@ FS_API const char* fs_last_error(const fs_handle* h);
 FS_API int fs_set_pic_ratio(fs_handle* h, float pic_ratio); /* FluidDomain::setPicRatio: clamps to [0, 1] */
 FS_API int fs_set_gravity(fs_handle* h, float gx, float gy);
 FS_API int fs_set_cg(fs_handle* h, double tolerance, int max_iterations);
+FS_API int fs_set_cg_precision(fs_handle* h, int precision);
 FS_API int fs_set_extension_iterations(fs_handle* h, int n);
 /* Persistent solid cells re-applied after every classification (extension;
  * the reference re-labels only the border).  mask: size_x*size_y bytes,

@@ -24,9 +24,14 @@
 // (oracle/fs_oracle.c) and the GPU path can reproduce it bit for bit:
 //   * vectors and the SpMV are in the scalar type (float), with every product
 //     and sum rounded separately (build with -ffp-contract=off);
-//   * dot products and norms are accumulated in double by the fixed
-//     "32-ary shuffle tree" order of fs_rsum32() below;
-//   * alpha and beta are formed in double and rounded once to the scalar.
+//   * dot products and norms sum their terms along the fixed "32-ary
+//     stride-halving tree" of fs_rsum32() below, in one of two precisions
+//     (fs_cg_precision()):
+//       FS_CG_FLOAT (default, the reference's own precision: Eigen's
+//         VectorXf dot products are float) -- float products, float tree,
+//         alpha, beta and the threshold tol^2 ||b||^2 in float;
+//       FS_CG_DOUBLE -- exact float*float products summed in double, alpha
+//         and beta formed in double and rounded once to float;
 // The SpMV walks the self-adjoint matrix built from the lower triangle
 // (Eigen's default UpLo = Lower) and sums the entries of each row in
 // ascending column order, starting from +0.
@@ -49,16 +54,17 @@ typedef std::ptrdiff_t Index;
 // consecutive values (zero padded), reduce each group by the stride-halving
 // tree (s = 16, 8, 4, 2, 1: a[l] += a[l + s]), and repeat on the group
 // results until one value is left.  Destroys its input.
-inline double fs_rsum32(std::vector<double>& a, Index n)
+template <typename T>
+inline T fs_rsum32(std::vector<T>& a, Index n)
 {
     if (n <= 0) return 0.0;
     while (n > 1) {
         Index groups = (n + 31) / 32;
         for (Index g = 0; g < groups; ++g) {
-            double t[32];
+            T t[32];
             for (int l = 0; l < 32; ++l) {
                 Index k = g * 32 + l;
-                t[l] = k < n ? a[k] : 0.0;
+                t[l] = k < n ? a[k] : T(0);
             }
             for (int s = 16; s >= 1; s >>= 1)
                 for (int l = 0; l < s; ++l) t[l] = t[l] + t[l + s];
@@ -141,6 +147,13 @@ private:
     std::vector<Entry> entries_;
 };
 
+enum { FS_CG_FLOAT = 0, FS_CG_DOUBLE = 1 };
+inline int& fs_cg_precision()
+{
+    static int p = FS_CG_FLOAT;
+    return p;
+}
+
 struct FsCgRecord
 {
     // Last solve of any ConjugateGradient in this process, kept for the
@@ -201,14 +214,22 @@ public:
     template <typename Rhs>
     Rhs solve(const Rhs& b)
     {
+        if (fs_cg_precision() == FS_CG_DOUBLE) return solve_t<Rhs, double>(b);
+        return solve_t<Rhs, float>(b);
+    }
+
+    // R: accumulation type of the dot products (float or double).
+    template <typename Rhs, typename R>
+    Rhs solve_t(const Rhs& b)
+    {
         const Index n = n_;
         Rhs x(n);
-        std::vector<double> scratch(static_cast<size_t>(n > 0 ? n : 1));
+        std::vector<R> scratch(static_cast<size_t>(n > 0 ? n : 1));
         auto dot = [&](const std::vector<Scalar>& a, const std::vector<Scalar>& c) {
             for (Index k = 0; k < n; ++k)
                 scratch[static_cast<size_t>(k)] =
-                    static_cast<double>(a[static_cast<size_t>(k)]) * static_cast<double>(c[static_cast<size_t>(k)]);
-            return fs_rsum32(scratch, n);
+                    static_cast<R>(a[static_cast<size_t>(k)]) * static_cast<R>(c[static_cast<size_t>(k)]);
+            return fs_rsum32<R>(scratch, n);
         };
         std::vector<Scalar> r(static_cast<size_t>(n)), p(static_cast<size_t>(n)),
             q(static_cast<size_t>(n)), z(static_cast<size_t>(n)), xv(static_cast<size_t>(n), Scalar(0));
@@ -216,22 +237,24 @@ public:
 
         iters_ = 0;
         error_ = 0.0;
-        const double bb = dot(r, r);
-        if (bb == 0.0) {
+        const R bb = dot(r, r);
+        if (bb == R(0)) {
             record(xv);
             return x;
         }
-        double thr = tol_ * tol_ * bb;
-        if (thr < std::numeric_limits<double>::min()) thr = std::numeric_limits<double>::min();
-        double rr = bb;
+        const R tol = static_cast<R>(tol_);
+        R thr = tol * tol;
+        thr = thr * bb;
+        if (thr < std::numeric_limits<R>::min()) thr = std::numeric_limits<R>::min();
+        R rr = bb;
         if (rr < thr) {
-            error_ = std::sqrt(rr / bb);
+            error_ = std::sqrt(static_cast<double>(rr) / static_cast<double>(bb));
             record(xv);
             return x;
         }
         for (Index k = 0; k < n; ++k)
             p[static_cast<size_t>(k)] = inv_diag_[static_cast<size_t>(k)] * r[static_cast<size_t>(k)];
-        double rz = dot(r, p);
+        R rz = dot(r, p);
         const Index maxit = maxIterations();
         for (Index it = 1; it <= maxit; ++it) {
             for (Index k = 0; k < n; ++k) {
@@ -242,7 +265,7 @@ public:
                 }
                 q[static_cast<size_t>(k)] = acc;
             }
-            const double pq = dot(p, q);
+            const R pq = dot(p, q);
             const Scalar alpha = static_cast<Scalar>(rz / pq);
             for (Index k = 0; k < n; ++k) {
                 Scalar ap = alpha * p[static_cast<size_t>(k)];
@@ -255,7 +278,7 @@ public:
             if (rr < thr) break;
             for (Index k = 0; k < n; ++k)
                 z[static_cast<size_t>(k)] = inv_diag_[static_cast<size_t>(k)] * r[static_cast<size_t>(k)];
-            const double rz_new = dot(r, z);
+            const R rz_new = dot(r, z);
             const Scalar beta = static_cast<Scalar>(rz_new / rz);
             rz = rz_new;
             for (Index k = 0; k < n; ++k) {
@@ -263,7 +286,7 @@ public:
                 p[static_cast<size_t>(k)] = z[static_cast<size_t>(k)] + bp;
             }
         }
-        error_ = std::sqrt(rr / bb);
+        error_ = std::sqrt(static_cast<double>(rr) / static_cast<double>(bb));
         for (Index k = 0; k < n; ++k) x[k] = xv[static_cast<size_t>(k)];
         record(xv);
         return x;

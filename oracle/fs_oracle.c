@@ -44,6 +44,7 @@ struct fso_sim
     int n_ext;
     double cg_tol;
     int cg_maxit;
+    int cg_double;        /* dot-product precision: 0 float, 1 double */
     int use_stock;
 
     float* u[2];
@@ -74,6 +75,7 @@ struct fso_sim
     float *cg_b, *cg_x, *cg_r, *cg_p, *cg_q, *cg_z, *cg_diag, *cg_inv;
     int32_t *cg_down, *cg_up, *cg_left, *cg_right;
     double* cg_acc;
+    float* cg_accf;
 };
 
 #define IDX(s, i, j) ((size_t)(i) + (size_t)(j) * (size_t)(s)->nx)
@@ -219,6 +221,7 @@ fso_sim* fso_create(int nx, int ny, float lx, float ly, float density, float pic
     s->cg_left = (int32_t*)xcalloc(n, sizeof(int32_t));
     s->cg_right = (int32_t*)xcalloc(n, sizeof(int32_t));
     s->cg_acc = (double*)xcalloc(n, sizeof(double));
+    s->cg_accf = (float*)xcalloc(n, sizeof(float));
     /* MacGrid ctor clears the cell types (MacGrid.cpp:24 -> :32-50). */
     for (int j = 0; j < ny; ++j)
         for (int i = 0; i < nx; ++i)
@@ -241,7 +244,7 @@ void fso_destroy(fso_sim* s)
     free(s->part); free(s->pressure); free(s->src);
     free(s->cg_b); free(s->cg_x); free(s->cg_r); free(s->cg_p); free(s->cg_q); free(s->cg_z);
     free(s->cg_diag); free(s->cg_inv); free(s->cg_down); free(s->cg_up); free(s->cg_left);
-    free(s->cg_right); free(s->cg_acc);
+    free(s->cg_right); free(s->cg_acc); free(s->cg_accf);
     free(s);
 }
 
@@ -250,6 +253,7 @@ void fso_set_cg(fso_sim* s, double tol, int maxit)
     s->cg_tol = tol;
     s->cg_maxit = maxit;
 }
+void fso_set_cg_precision(fso_sim* s, int precision) { s->cg_double = precision != 0; }
 void fso_set_gravity(fso_sim* s, float gx, float gy)
 {
     s->gx = gx;
@@ -549,10 +553,39 @@ static double rsum32(double* a, int64_t n)
     return a[0];
 }
 
-static double dot(fso_sim* s, const float* a, const float* b, int n)
+/* The same tree in float. */
+static float rsum32f(float* a, int64_t n)
+{
+    if (n <= 0) return 0.0f;
+    while (n > 1) {
+        const int64_t groups = (n + 31) / 32;
+        for (int64_t g = 0; g < groups; ++g) {
+            float t[32];
+            for (int l = 0; l < 32; ++l) {
+                const int64_t k = g * 32 + l;
+                t[l] = k < n ? a[k] : 0.0f;
+            }
+            for (int st = 16; st >= 1; st >>= 1)
+                for (int l = 0; l < st; ++l) t[l] = t[l] + t[l + st];
+            a[g] = t[0];
+        }
+        n = groups;
+    }
+    return a[0];
+}
+
+/* Exact float*float products summed in double. */
+static double dot_d(fso_sim* s, const float* a, const float* b, int n)
 {
     for (int k = 0; k < n; ++k) s->cg_acc[k] = (double)a[k] * (double)b[k];
     return rsum32(s->cg_acc, n);
+}
+
+/* Float products summed in float (the precision of Eigen's VectorXf::dot). */
+static float dot_f(fso_sim* s, const float* a, const float* b, int n)
+{
+    for (int k = 0; k < n; ++k) s->cg_accf[k] = a[k] * b[k];
+    return rsum32f(s->cg_accf, n);
 }
 
 /* q = A p, each row summed in ascending column order from +0:
@@ -572,7 +605,49 @@ static void spmv(fso_sim* s, const float* p, float* q, int n, float off)
 }
 
 /* Jacobi-preconditioned CG, zero initial guess (the published algorithm that
- * Eigen::ConjugateGradient implements; FluidSolver.cpp:423-425). */
+ * Eigen::ConjugateGradient implements; FluidSolver.cpp:423-425).  R is the
+ * accumulation type of the dot products and of alpha / beta / the stopping
+ * threshold (float: the reference's precision; double: the FP64 variant). */
+#define FSO_CG_BODY(R, DOT, RMIN)                                              \
+    do {                                                                       \
+        const R bb = DOT(s, r, r, n);                                          \
+        if (bb == (R)0) return;                                                \
+        const R tolr = (R)s->cg_tol;                                           \
+        R thr = tolr * tolr;                                                   \
+        thr = thr * bb;                                                        \
+        if (thr < RMIN) thr = RMIN;                                            \
+        R rr = bb;                                                             \
+        if (rr < thr) {                                                        \
+            s->cg_error = sqrt((double)rr / (double)bb);                       \
+            return;                                                            \
+        }                                                                      \
+        for (int k = 0; k < n; ++k) p[k] = s->cg_inv[k] * r[k];                \
+        R rz = DOT(s, r, p, n);                                                \
+        for (int it = 1; it <= s->cg_maxit; ++it) {                            \
+            spmv(s, p, q, n, off);                                             \
+            const R pq = DOT(s, p, q, n);                                      \
+            const float alpha = (float)(rz / pq);                              \
+            for (int k = 0; k < n; ++k) {                                      \
+                float t = alpha * p[k];                                        \
+                x[k] = x[k] + t;                                               \
+                t = alpha * q[k];                                              \
+                r[k] = r[k] - t;                                               \
+            }                                                                  \
+            rr = DOT(s, r, r, n);                                              \
+            s->cg_iters = it;                                                  \
+            if (rr < thr) break;                                               \
+            for (int k = 0; k < n; ++k) z[k] = s->cg_inv[k] * r[k];            \
+            const R rz_new = DOT(s, r, z, n);                                  \
+            const float beta = (float)(rz_new / rz);                           \
+            rz = rz_new;                                                       \
+            for (int k = 0; k < n; ++k) {                                      \
+                const float t = beta * p[k];                                   \
+                p[k] = z[k] + t;                                               \
+            }                                                                  \
+        }                                                                      \
+        s->cg_error = sqrt((double)rr / (double)bb);                           \
+    } while (0)
+
 static void cg_solve(fso_sim* s, int n, float off)
 {
     float *b = s->cg_b, *x = s->cg_x, *r = s->cg_r, *p = s->cg_p, *q = s->cg_q, *z = s->cg_z;
@@ -584,40 +659,8 @@ static void cg_solve(fso_sim* s, int n, float off)
     }
     s->cg_iters = 0;
     s->cg_error = 0.0;
-    const double bb = dot(s, r, r, n);
-    if (bb == 0.0) return;
-    double thr = s->cg_tol * s->cg_tol * bb;
-    if (thr < DBL_MIN) thr = DBL_MIN;
-    double rr = bb;
-    if (rr < thr) {
-        s->cg_error = sqrt(rr / bb);
-        return;
-    }
-    for (int k = 0; k < n; ++k) p[k] = s->cg_inv[k] * r[k];
-    double rz = dot(s, r, p, n);
-    for (int it = 1; it <= s->cg_maxit; ++it) {
-        spmv(s, p, q, n, off);
-        const double pq = dot(s, p, q, n);
-        const float alpha = (float)(rz / pq);
-        for (int k = 0; k < n; ++k) {
-            float t = alpha * p[k];
-            x[k] = x[k] + t;
-            t = alpha * q[k];
-            r[k] = r[k] - t;
-        }
-        rr = dot(s, r, r, n);
-        s->cg_iters = it;
-        if (rr < thr) break;
-        for (int k = 0; k < n; ++k) z[k] = s->cg_inv[k] * r[k];
-        const double rz_new = dot(s, r, z, n);
-        const float beta = (float)(rz_new / rz);
-        rz = rz_new;
-        for (int k = 0; k < n; ++k) {
-            const float t = beta * p[k];
-            p[k] = z[k] + t;
-        }
-    }
-    s->cg_error = sqrt(rr / bb);
+    if (s->cg_double) FSO_CG_BODY(double, dot_d, DBL_MIN);
+    else FSO_CG_BODY(float, dot_f, FLT_MIN);
 }
 
 /* FluidSolver::pressureSolve (FluidSolver.cpp:323-483). */

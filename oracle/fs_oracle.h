@@ -76,6 +76,10 @@ void fso_destroy(fso_sim* s);
 /* Pressure-solve settings; the reference fixes maxit = 100 (FluidSolver.cpp:81)
  * and leaves the tolerance at machine epsilon. */
 void fso_set_cg(fso_sim* s, double tolerance, int max_iterations);
+/* Precision of the CG dot products: 0 = float (the reference's, default),
+ * 1 = double (exact products summed in double).  Same fixed summation tree
+ * either way.  In the reference build the setting is process-wide. */
+void fso_set_cg_precision(fso_sim* s, int precision);
 /* Gravity; the reference hard-codes (0, -9.82) (FluidSolver.cpp:232). */
 void fso_set_gravity(fso_sim* s, float gx, float gy);
 /* Extension sweeps; the reference hard-codes 2 (FluidSolver.cpp:234). */

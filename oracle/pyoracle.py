@@ -47,6 +47,7 @@ def _lib(kind: str) -> C.CDLL:
         "fso_destroy": (None, [vp]),
         "fso_set_cg": (None, [vp, d, i]),
         "fso_set_gravity": (None, [vp, f, f]),
+        "fso_set_cg_precision": (None, [vp, i]),
         "fso_set_extension_iterations": (None, [vp, i]),
         "fso_set_solid_mask": (None, [vp, vp]),
         "fso_set_use_stock": (None, [vp, i]),
@@ -104,6 +105,10 @@ class OracleSim:
     # settings
     def set_cg(self, tol: float, maxit: int) -> None:
         self.lib.fso_set_cg(self.h, float(tol), int(maxit))
+
+    def set_cg_precision(self, precision: int) -> None:
+        """0: float dot products (the reference's precision); 1: double."""
+        self.lib.fso_set_cg_precision(self.h, int(precision))
 
     def set_gravity(self, gx: float, gy: float) -> None:
         self.lib.fso_set_gravity(self.h, gx, gy)

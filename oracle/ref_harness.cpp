@@ -158,6 +158,11 @@ void fso_set_cg(fso_sim* s, double tol, int maxit)
     s->solver._cg_solver.setMaxIterations(maxit);
 }
 
+void fso_set_cg_precision(fso_sim*, int precision)
+{
+    Eigen::fs_cg_precision() = precision ? Eigen::FS_CG_DOUBLE : Eigen::FS_CG_FLOAT;
+}
+
 void fso_set_gravity(fso_sim* s, float gx, float gy)
 {
     s->gx = gx;

@@ -27,13 +27,15 @@ def _built():
     fsg.load_library()
 
 
-def pair(sc, cg_tol=None, cg_maxit=None):
+def pair(sc, cg_tol=None, cg_maxit=None, precision=fsg.CG_FLOAT):
     tol = sc.cg_tolerance if cg_tol is None else cg_tol
     maxit = sc.cg_max_iterations if cg_maxit is None else cg_maxit
     g = fsg.FluidSim(sc.size_x, sc.size_y, sc.length_x, sc.length_y, sc.density, sc.pic_ratio,
                      cg_tolerance=tol, cg_max_iterations=maxit, gravity=sc.gravity)
     o = po.OracleSim("restatement", sc.size_x, sc.size_y, sc.length_x, sc.length_y, sc.density, sc.pic_ratio)
     o.set_cg(tol, maxit)
+    g.set_cg_precision(precision)
+    o.set_cg_precision(precision)
     o.set_gravity(*sc.gravity)
     if sc.solid is not None:
         g.set_solid_mask(sc.solid)
@@ -65,11 +67,12 @@ def test_step_methods_bit_exact(method):
         assert_same(g.state(), o.state(), where="method %d step %d" % (method, k))
 
 
-def test_picflip_200_steps_bit_exact_with_graphs():
+@pytest.mark.parametrize("precision", [fsg.CG_FLOAT, fsg.CG_DOUBLE])
+def test_picflip_200_steps_bit_exact_with_graphs(precision):
     """The 64x64 dam break of the small configuration, 200 steps, replayed
-    through the cached CUDA graph of the step."""
+    through the cached CUDA graph of the step; both CG precisions."""
     sc = scenes.dam_break_small()
-    g, o = pair(sc)
+    g, o = pair(sc, precision=precision)
     for k in range(200):
         g.step(fsg.STEP_PICFLIP, sc.dt)
         o.step(po.STEP_PICFLIP, sc.dt)
@@ -149,11 +152,12 @@ def test_obstacle_and_gravity_override():
     assert_same(g.state(), o.state(), where="obstacle")
 
 
-def test_large_grid_one_step_bit_exact():
-    """512x512 dam break with an obstacle (~440k particles), one full step:
+@pytest.mark.parametrize("precision", [fsg.CG_FLOAT, fsg.CG_DOUBLE])
+def test_large_grid_one_step_bit_exact(precision):
+    """512x512 dam break with an obstacle (~430k particles), one full step:
     multi-CTA CG with grid barriers, shared-memory-resident CG state."""
     sc = scenes.dam_break_large(512)
-    g, o = pair(sc)
+    g, o = pair(sc, precision=precision)
     g.step(fsg.STEP_PICFLIP, sc.dt)
     o.step(po.STEP_PICFLIP, sc.dt)
     assert_same(g.state(), o.state(), where="512")
@@ -163,14 +167,15 @@ def test_large_grid_one_step_bit_exact():
     assert st["cg_residual"] < sc.cg_tolerance
 
 
-def test_streaming_cg_matches_oracle():
+@pytest.mark.parametrize("precision", [fsg.CG_FLOAT, fsg.CG_DOUBLE])
+def test_streaming_cg_matches_oracle(precision):
     """A fluid region too large for the shared-memory-resident CG (more than
     8 x 1024 fluid cells per CTA): the streaming variant of the same kernel."""
     n = 1280
     sc = scenes.Scene(n, n, float(n), float(n), 0.01, 0.05, 0.01,
                       scenes.block_particles(n, n, float(n), float(n), 1, n - 1, 1, n - 1, 1, 11),
                       cg_tolerance=1e-3, cg_max_iterations=60)
-    g, o = pair(sc)
+    g, o = pair(sc, precision=precision)
     g.step(fsg.STEP_PICFLIP, sc.dt)
     o.step(po.STEP_PICFLIP, sc.dt)
     st = g.stats()
