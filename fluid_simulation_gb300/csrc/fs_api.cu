@@ -407,7 +407,15 @@ int device_status(fs_handle* h)
     cudaError_t e = cudaMemcpyAsync(&st, h->d_status, sizeof(unsigned), cudaMemcpyDeviceToHost, h->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
     if (e != cudaSuccess) return cuda_fail(h, e, "synchronize");
-    if (st & ST_TIMEOUT) return fail(h, FS_ERR_TIMEOUT, "a device-side wait of the CG kernel timed out");
+    if (st & ST_TIMEOUT) {
+        // The aborted solve did not advance the tag sequence; clear its tagged
+        // partials so that none of them can match a later solve's tags.
+        const int64_t max_chunks = (h->ncell + 1023) / 1024;
+        cudaMemsetAsync(h->cg.partials, 0, sizeof(double) * 8 * (size_t)max_chunks, h->stream);
+        cudaMemsetAsync(h->d_status, 0, sizeof(unsigned), h->stream);
+        cudaStreamSynchronize(h->stream);
+        return fail(h, FS_ERR_TIMEOUT, "a device-side wait of the CG kernel timed out");
+    }
     if (st & ST_TOO_LARGE) return fail(h, FS_ERR_TOO_LARGE, "too many fluid cells for the CG kernel");
     if (st & ST_INTERNAL) return fail(h, FS_ERR_INTERNAL, "internal consistency check failed on the device");
     return FS_OK;
@@ -557,7 +565,7 @@ int fs_create(const fs_config* cfg, fs_handle** out)
     A(dalloc(&h->cg.z, N));
     A(dalloc(&h->cg.p, N));
     A(dalloc(&h->cg.q, N));
-    A(dalloc(&h->cg.partials, (size_t)4 * max_chunks));
+    A(dalloc(&h->cg.partials, (size_t)8 * max_chunks));
     A(dalloc(&h->cg.barrier, 1));
     A(dalloc(&h->cg.result, 1));
     A(dalloc(&h->cg_b, N));
@@ -590,6 +598,8 @@ int fs_create(const fs_config* cfg, fs_handle** out)
         A(cudaMemsetAsync(h->d_status, 0, 4, h->stream));
         A(cudaMemsetAsync(h->d_warn, 0, 4, h->stream));
         A(cudaMemsetAsync(h->cg.result, 0, sizeof(CgResult), h->stream));
+        A(cudaMemsetAsync(h->cg.partials, 0, sizeof(double) * 8 * (size_t)max_chunks, h->stream));
+        A(cudaMemsetAsync(h->cg.barrier, 0, sizeof(unsigned), h->stream));
         labels_clear(h->L(), h->g, h->labels);  // MacGrid ctor -> clearCellTypeBuffer (src/MacGrid.cpp:24)
         A(cudaGetLastError());
         A(cudaStreamSynchronize(h->stream));

@@ -117,8 +117,8 @@ struct CgResult
 struct CgWork
 {
     float *x, *r, *z, *p, *q;
-    double* partials;   // [2 buffers][2 values][max_chunks] (float or double)
-    unsigned* barrier;  // grid barrier counter (reset by cg_solve)
+    double* partials;   // tagged partial words, 8 per chunk (zeroed once at allocation)
+    unsigned* barrier;  // reduction sequence number; persists across launches (zeroed at allocation)
     CgResult* result;
     int64_t max_cells;
     int grid;           // co-resident CTAs of the cooperative launch
