@@ -24,22 +24,14 @@
 //     once to float.  GB300's FP64 rate is a small fraction of its FP32 rate,
 //     so the double variant costs FP64 issue slots in every reduction.
 //
-// Per iteration there are two grid-wide exchanges (p.q, then r.r and r.z),
-// and each is a single round trip through L2: every chunk partial is
-// published as one 64-bit word {value, tag} with a release store, and every
-// CTA polls the partials it needs with acquire loads until their tags equal
-// the tag of the current reduction.  The data exchange is the barrier; there
-// is no separate counter.  Tags are a sequence number that persists across
-// launches (base read at kernel start, advanced by the number of reductions
-// at exit), so a slot left over from an earlier reduction or launch never
-// matches.  The search direction p_new = z + beta p_old is not exchanged
-// through a third round: z and p_old of every cell are published in the
+// Per iteration there are two grid barriers (after p.q and after r.r, r.z).
+// The search direction p_new = z + beta p_old is not exchanged through a third
+// barrier: z and p_old of every cell are published to global memory in the
 // previous phase, and each CTA recomputes p_new of the neighbours it needs
 // with the same float operations.  Each CTA keeps the state of its own cells
 // in shared memory (up to KREG chunks of 1024 cells per CTA, ~200 KB) or, for
-// larger systems, streams it from global memory.  Waits are bounded: a thread
-// that polls longer than about two seconds sets ST_TIMEOUT and its CTA
-// returns; every other CTA then gives up at its next exchange.
+// larger systems, streams it from global memory.  Waits are bounded: a CTA that
+// waits longer than about two seconds sets ST_TIMEOUT and every CTA returns.
 #include "fs_internal.h"
 
 namespace fs {
@@ -67,9 +59,9 @@ struct CgArgs
     int maxit;
     int fp64;                  // 0: float dot products, 1: double
     float *x, *r, *z, *p, *q;  // fluid-index vectors (global)
-    unsigned long long* partials;  // tagged words: [2 buffers][2 values][2 halves][max chunks]
+    double* partials;          // [2 buffers][2 values][MAX chunks]
     int max_chunks;
-    unsigned* seq;                 // reduction sequence number, persists across launches
+    unsigned* barrier;
     unsigned* status;
     CgResult* result;
 };
@@ -124,59 +116,33 @@ __device__ __forceinline__ R warp_tree(R v)
     return v;
 }
 
-__device__ __forceinline__ void st_release_u64(unsigned long long* p, unsigned long long v)
+// Barrier over the active CTAs.  Thread 0 arrives with a release reduction on
+// the counter (bar.sync first makes the CTA's writes part of what it
+// releases) and spins with acquire loads; the closing bar.sync hands the
+// acquired view to the other threads, which read shared data with ld.cg.
+// Returns false if this CTA gave up waiting (after WAIT_LIMIT_NS); a CTA that
+// gives up returns, so every other CTA also gives up at its next barrier.
+__device__ __forceinline__ bool cta_barrier(const CgArgs& a, bool grid, unsigned& target, Smem& sm)
 {
-    asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
-}
-
-__device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long long* p)
-{
-    unsigned long long v;
-    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
-    return v;
-}
-
-// Tagged encoding of one partial: float -> one word, double -> two words.
-template <typename R> struct Tagged;
-template <> struct Tagged<float>
-{
-    static __device__ __forceinline__ void put(unsigned long long* slot, size_t half_stride, float v, unsigned tag)
-    {
-        st_release_u64(slot, ((unsigned long long)tag << 32) | __float_as_uint(v));
+    __syncthreads();
+    if (grid && threadIdx.x == 0) {
+        target += gridDim.x;
+        red_release_add_u32(a.barrier, 1u);
+        int ok = 1;
+        if (ld_acquire_u32(a.barrier) < target) {
+            const uint64_t t0 = globaltimer_ns();
+            while (ld_acquire_u32(a.barrier) < target) {
+                if (globaltimer_ns() - t0 > WAIT_LIMIT_NS) {
+                    atomicOr(a.status, ST_TIMEOUT);
+                    ok = 0;
+                    break;
+                }
+            }
+        }
+        sm.flag = ok;
     }
-    // Returns false until the slot carries `tag`.
-    static __device__ __forceinline__ bool get(const unsigned long long* slot, size_t half_stride, unsigned tag,
-                                               float& v)
-    {
-        const unsigned long long w = ld_acquire_u64(slot);
-        if ((unsigned)(w >> 32) != tag) return false;
-        v = __uint_as_float((unsigned)w);
-        return true;
-    }
-};
-template <> struct Tagged<double>
-{
-    static __device__ __forceinline__ void put(unsigned long long* slot, size_t half_stride, double v, unsigned tag)
-    {
-        const unsigned long long b = (unsigned long long)__double_as_longlong(v);
-        st_release_u64(slot, ((unsigned long long)tag << 32) | (b & 0xffffffffull));
-        st_release_u64(slot + half_stride, ((unsigned long long)tag << 32) | (b >> 32));
-    }
-    static __device__ __forceinline__ bool get(const unsigned long long* slot, size_t half_stride, unsigned tag,
-                                               double& v)
-    {
-        const unsigned long long lo = ld_acquire_u64(slot);
-        const unsigned long long hi = ld_acquire_u64(slot + half_stride);
-        if ((unsigned)(lo >> 32) != tag || (unsigned)(hi >> 32) != tag) return false;
-        v = __longlong_as_double((long long)((hi << 32) | (lo & 0xffffffffull)));
-        return true;
-    }
-};
-
-// Slot of chunk c, value k, buffer buf.
-__device__ __forceinline__ unsigned long long* slot_of(const CgArgs& a, int buf, int k, int c)
-{
-    return a.partials + ((size_t)(buf * 2 + k) * 2) * a.max_chunks + c;
+    __syncthreads();
+    return !grid || sm.flag != 0;
 }
 
 // Level-1 (warp) tree of NV values for chunk slot `slot`; lane 0 keeps it.
@@ -191,75 +157,55 @@ __device__ __forceinline__ void level1(const R (&v)[NV], int slot, Smem& sm)
     }
 }
 
-// Level-2 trees for slots [0, nslots) -> the tagged chunk partials of
-// chunks chunk0 + slot.  The bar.sync before the release stores makes every
-// write of the CTA so far (z, p publishes) part of what they release.
+// Level-2 trees for slots [0, nslots) -> chunk partials part[buf][k][chunk0 + slot].
 template <typename R, int NV>
-__device__ __forceinline__ void level2(const CgArgs& a, int buf, int chunk0, int nslots, unsigned tag, Smem& sm)
+__device__ __forceinline__ void level2(const CgArgs& a, int buf, int chunk0, int nslots, Smem& sm)
 {
     __syncthreads();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    R* part = reinterpret_cast<R*>(a.partials);
     if (warp < nslots) {
 #pragma unroll
         for (int k = 0; k < NV; ++k) {
             const R t = warp_tree<R>(Ar<R>::red(sm, warp, lane, k));
-            if (lane == 0) Tagged<R>::put(slot_of(a, buf, k, chunk0 + warp), a.max_chunks, t, tag);
+            if (lane == 0) __stcg(&part[((size_t)buf * 2 + k) * a.max_chunks + chunk0 + warp], t);
         }
     }
     __syncthreads();
 }
 
-// Levels 3+: every CTA waits for and reduces all chunk partials of buffer
-// buf carrying `tag`.  Thread t polls chunk t (t + 1024, ...), so warp w holds
-// the level-3 group of chunks 32w..32w+31 in its lanes.  Returns false if
-// this CTA gave up waiting.
+// Levels 3+: every CTA reduces all chunk partials of buffer buf.
 template <typename R, int NV>
-__device__ __forceinline__ bool reduce_all(const CgArgs& a, int buf, int nchunks, unsigned tag, Smem& sm,
-                                           R (&out)[NV])
+__device__ __forceinline__ void reduce_all(const CgArgs& a, int buf, int nchunks, Smem& sm, R (&out)[NV])
 {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    int bad = 0;
-    const int n = (nchunks + 31) / 32;  // level-3 groups
+    const R* src = reinterpret_cast<const R*>(a.partials) + (size_t)buf * 2 * a.max_chunks;
+    if (nchunks == 1) {
+#pragma unroll
+        for (int k = 0; k < NV; ++k) out[k] = __ldcg(&src[(size_t)k * a.max_chunks]);
+        return;
+    }
+    int n = (nchunks + 31) / 32;
     for (int g = warp; g < n; g += 32) {
         const int e = g * 32 + lane;
-        R v[NV];
 #pragma unroll
-        for (int k = 0; k < NV; ++k) v[k] = R(0);
-        if (e < nchunks && !bad) {
-            const uint64_t t0 = globaltimer_ns();
-#pragma unroll
-            for (int k = 0; k < NV; ++k) {
-                while (!bad && !Tagged<R>::get(slot_of(a, buf, k, e), a.max_chunks, tag, v[k])) {
-                    if (globaltimer_ns() - t0 > WAIT_LIMIT_NS) bad = 1;
-                }
-            }
-        }
-        if (g < n && nchunks > 1) {
-#pragma unroll
-            for (int k = 0; k < NV; ++k) {
-                const R t = warp_tree<R>(v[k]);
-                if (lane == 0) Ar<R>::lvlA(sm, g, k) = t;
-            }
-        } else if (nchunks == 1 && g == 0 && lane == 0) {
-#pragma unroll
-            for (int k = 0; k < NV; ++k) Ar<R>::lvlA(sm, 0, k) = v[k];
+        for (int k = 0; k < NV; ++k) {
+            const R v = e < nchunks ? __ldcg(&src[(size_t)k * a.max_chunks + e]) : R(0);
+            const R t = warp_tree<R>(v);
+            if (lane == 0) Ar<R>::lvlA(sm, g, k) = t;
         }
     }
-    if (__syncthreads_or(bad)) {
-        if (threadIdx.x == 0) atomicOr(a.status, ST_TIMEOUT);
-        return false;
-    }
-    int m = nchunks > 1 ? n : 1;
+    __syncthreads();
     bool inA = true;
-    while (m > 1) {
-        const int mm = (m + 31) / 32;
-        if (warp < mm) {
+    while (n > 1) {
+        const int m = (n + 31) / 32;
+        if (warp < m) {
             const int e = warp * 32 + lane;
 #pragma unroll
             for (int k = 0; k < NV; ++k) {
                 R v;
-                if (inA) v = e < m ? Ar<R>::lvlA(sm, e, k) : R(0);
-                else v = e < m ? Ar<R>::lvlB(sm, e, k) : R(0);
+                if (inA) v = e < n ? Ar<R>::lvlA(sm, e, k) : R(0);
+                else v = e < n ? Ar<R>::lvlB(sm, e, k) : R(0);
                 const R t = warp_tree<R>(v);
                 if (lane == 0) {
                     if (inA) Ar<R>::lvlB(sm, warp, k) = t;
@@ -269,12 +215,11 @@ __device__ __forceinline__ bool reduce_all(const CgArgs& a, int buf, int nchunks
         }
         __syncthreads();
         inA = !inA;
-        m = mm;
+        n = m;
     }
 #pragma unroll
     for (int k = 0; k < NV; ++k) out[k] = inA ? Ar<R>::lvlA(sm, 0, k) : Ar<R>::lvlB(sm, 0, k);
     __syncthreads();
-    return true;
 }
 
 // p_new of a cell outside this CTA's range, from its published z and p_old.
@@ -324,8 +269,7 @@ __device__ void cg_body(const CgArgs& a, Smem& sm, unsigned char* dyn, int nf, i
     const int kb = c1 - c0;                // chunks owned
     const int e0 = c0 * CHUNK;             // owned element range [e0, e1)
     const int e1 = min(c1 * CHUNK, nf);
-    const unsigned seq0 = __ldcg(a.seq);  // this launch's reductions use tags seq0 + 1, seq0 + 2, ...
-    unsigned tag = seq0;
+    unsigned target = 0;
     const Resident RS = resident(dyn, K > 0 ? K : 1);
     const float* dtab = sm.dtab;
     const float* itab = sm.itab;
@@ -360,11 +304,11 @@ __device__ void cg_body(const CgArgs& a, Smem& sm, unsigned char* dyn, int nf, i
             }
             level1<R, 2>(v, sl, sm);
         }
-        level2<R, 2>(a, 0, c0 + base, nslot, tag + 1, sm);
+        level2<R, 2>(a, 0, c0 + base, nslot, sm);
     }
-    ++tag;
+    if (!cta_barrier(a, grid, target, sm)) return;
     R red2[2];
-    if (!reduce_all<R, 2>(a, 0, nchunks, tag, sm, red2)) return;
+    reduce_all<R, 2>(a, 0, nchunks, sm, red2);
     const R bb = red2[0];
     R rz = red2[1];
     R rr = bb;
@@ -424,11 +368,11 @@ __device__ void cg_body(const CgArgs& a, Smem& sm, unsigned char* dyn, int nf, i
                 }
                 level1<R, 1>(v, sl, sm);
             }
-            level2<R, 1>(a, 1, c0 + base, nslot, tag + 1, sm);
+            level2<R, 1>(a, 1, c0 + base, nslot, sm);
         }
-        ++tag;
+        if (!cta_barrier(a, grid, target, sm)) return;
         R red1[1];
-        if (!reduce_all<R, 1>(a, 1, nchunks, tag, sm, red1)) return;
+        reduce_all<R, 1>(a, 1, nchunks, sm, red1);
         const float alpha = Ar<R>::ratio(rz, red1[0]);
 
         // ---- phase B: x += alpha p, r -= alpha q, z = M^-1 r; publish z, p; partial r.r, r.z
@@ -473,10 +417,10 @@ __device__ void cg_body(const CgArgs& a, Smem& sm, unsigned char* dyn, int nf, i
                 }
                 level1<R, 2>(v, sl, sm);
             }
-            level2<R, 2>(a, 0, c0 + base, nslot, tag + 1, sm);
+            level2<R, 2>(a, 0, c0 + base, nslot, sm);
         }
-        ++tag;
-        if (!reduce_all<R, 2>(a, 0, nchunks, tag, sm, red2)) return;
+        if (!cta_barrier(a, grid, target, sm)) return;
+        reduce_all<R, 2>(a, 0, nchunks, sm, red2);
         rr = red2[0];
         iters = it;
         if (rr < thr) break;
@@ -492,7 +436,6 @@ __device__ void cg_body(const CgArgs& a, Smem& sm, unsigned char* dyn, int nf, i
         }
     }
     if (cta == 0 && tid == 0) {
-        *a.seq = tag;  // every CTA read seq0 before publishing its first partial
         a.result->iterations = iters;
         a.result->rr = (double)rr;
         a.result->bb = (double)bb;
@@ -575,11 +518,12 @@ void cg_solve(const Launch& L, CgWork& w, const int32_t* nfluid, const float* b,
     a.z = w.z;
     a.p = w.p;
     a.q = w.q;
-    a.partials = reinterpret_cast<unsigned long long*>(w.partials);
+    a.partials = w.partials;
     a.max_chunks = (int)((w.max_cells + CHUNK - 1) / CHUNK);
-    a.seq = w.barrier;
+    a.barrier = w.barrier;
     a.status = status;
     a.result = w.result;
+    cudaMemsetAsync(w.barrier, 0, sizeof(unsigned), L.stream);
     void* args[] = {&a};
     cudaLaunchCooperativeKernel((const void*)k_cg, dim3(w.grid), dim3(CG_THREADS), args, RESIDENT_BYTES, L.stream);
     L.count();
