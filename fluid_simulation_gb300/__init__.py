@@ -85,6 +85,8 @@ SIGNATURES = {
     "fs_get_stream": (_vp, [_vp]),
     "fs_set_stream": (_i, [_vp, _vp]),
     "fs_kernel_launches": (_i64, [_vp]),
+    "fs_pressure_solve_noalloc": (_i, [_i, _i, _f, _f, _vp, _vp, _vp, _d, _i, _i, _vp, C.POINTER(_i),
+                                       C.POINTER(_d), _vp]),
 }
 
 _LIB: C.CDLL | None = None

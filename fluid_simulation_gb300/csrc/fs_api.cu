@@ -17,6 +17,12 @@ namespace {
 
 thread_local std::string g_create_error;
 
+}  // namespace
+
+void fs::set_thread_error(const char* msg) { g_create_error = msg ? msg : ""; }
+
+namespace {
+
 struct GraphEntry
 {
     int method;

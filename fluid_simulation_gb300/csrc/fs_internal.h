@@ -9,6 +9,9 @@
 
 namespace fs {
 
+// Sets the message fs_last_error(NULL) returns on this thread.
+void set_thread_error(const char* msg);
+
 struct Launch
 {
     cudaStream_t stream;

@@ -203,6 +203,34 @@ FS_API int fs_set_stream(fs_handle* h, void* stream);
 /* Number of this library's kernel launches queued so far on h. */
 FS_API int64_t fs_kernel_launches(fs_handle* h);
 
+/* Allocation-free pressure solve.  No counterpart in the reference: this is
+ * FluidSolver::pressureSolve's fluid indexing, assembly and conjugate gradient
+ * for callers that cannot allocate device memory -- an application that owns
+ * all device memory and forbids cudaMalloc/cudaFree once running (a real-time
+ * frame loop, where an allocation can stall the device), or a plugin living
+ * in a host application's fixed memory budget.  Such callers cannot use
+ * fs_create, which allocates every grid of a handle.
+ *
+ * Inputs are device pointers to size_x * size_y cells: labels (FS_LIQUID /
+ * FS_AIR / FS_SOLID with a SOLID border, as classification leaves them) and
+ * the front velocities u, v; the output is the pressure of every cell
+ * (0 outside fluid), as fs_get_pressure reports after FS_PH_PRESSURE.  The
+ * velocity update is left to the caller.  Work is queued on `stream`
+ * (cudaStream_t, NULL = default stream); when cg_iterations or cg_residual
+ * is non-NULL the call synchronises the stream to report them.
+ *
+ * Limit: size_x * size_y <= 16384 cells (e.g. 128 x 128); larger grids
+ * return FS_ERR_TOO_LARGE.  All scratch lives in one static device array of
+ * about 0.75 MB that every GPU loading this library holds until exit.  The
+ * first call on a device looks up that array's address (cudaGetSymbolAddress)
+ * and must come before any stream capture.  Calls share the array: calls
+ * whose work overlaps on the GPU race.  Messages go to fs_last_error(NULL). */
+FS_API int fs_pressure_solve_noalloc(int size_x, int size_y, float length_x, float length_y,
+                                     const uint8_t* labels, const float* u, const float* v,
+                                     double cg_tolerance, int cg_max_iterations, int cg_precision,
+                                     float* pressure, int* cg_iterations, double* cg_residual,
+                                     void* stream);
+
 #ifdef __cplusplus
 }
 #endif
