@@ -103,5 +103,17 @@ def build_dropin(force: bool = False) -> str | None:
     return DROPIN_LIB
 
 
+def build_example(name: str = "dam_break") -> str:
+    """Compiles dropin/examples/<name>.cpp, a program written against the
+    reference's class API, against the drop-in headers and libraries."""
+    build()
+    src = os.path.join(DROPIN, "examples", name + ".cpp")
+    exe = os.path.join(BUILD, name + "_gpu")
+    if _stale(exe, [src, DROPIN_LIB, LIB]):
+        _run(["g++", "-std=c++14", "-O2", "-I", os.path.join(DROPIN, "include"), "-I", os.path.join(ROOT, "include"),
+              src, "-o", exe, "-L", BUILD, "-lfsgpu_dropin", "-lfsgpu", "-Wl,-rpath," + BUILD])
+    return exe
+
+
 if __name__ == "__main__":
     print(build(force="--force" in sys.argv, verbose=True, ptxas_info="--ptxas" in sys.argv))

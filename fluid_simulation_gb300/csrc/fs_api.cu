@@ -631,26 +631,27 @@ int fs_set_pic_ratio(fs_handle* h, float r)
     if (!h) return FS_ERR_INVALID_ARGUMENT;
     // FluidDomain::setPicRatio (src/FluidDomain.cpp:99-102): CLAMP(pic_ratio, 0, 1)
     const float t = r < 0.0f ? 0.0f : r;
-    h->pic = t > 1.0f ? 1.0f : t;
-    clear_graphs(h);
+    const float v = t > 1.0f ? 1.0f : t;
+    if (float_bits(v) != float_bits(h->pic)) clear_graphs(h);
+    h->pic = v;
     return FS_OK;
 }
 
 int fs_set_gravity(fs_handle* h, float gx, float gy)
 {
     if (!h) return FS_ERR_INVALID_ARGUMENT;
+    if (float_bits(gx) != float_bits(h->gx) || float_bits(gy) != float_bits(h->gy)) clear_graphs(h);
     h->gx = gx;
     h->gy = gy;
-    clear_graphs(h);
     return FS_OK;
 }
 
 int fs_set_cg(fs_handle* h, double tol, int maxit)
 {
     if (!h || !(tol >= 0) || maxit < 0) return h ? fail(h, FS_ERR_INVALID_ARGUMENT, "invalid CG settings") : 1;
+    if (tol != h->cg_tol || maxit != h->cg_maxit) clear_graphs(h);
     h->cg_tol = tol;
     h->cg_maxit = maxit;
-    clear_graphs(h);
     return FS_OK;
 }
 
@@ -658,16 +659,17 @@ int fs_set_cg_precision(fs_handle* h, int precision)
 {
     if (!h || (precision != FS_CG_FLOAT && precision != FS_CG_DOUBLE))
         return h ? fail(h, FS_ERR_INVALID_ARGUMENT, "unknown CG precision") : FS_ERR_INVALID_ARGUMENT;
-    h->cg_fp64 = precision == FS_CG_DOUBLE ? 1 : 0;
-    clear_graphs(h);
+    const int fp64 = precision == FS_CG_DOUBLE ? 1 : 0;
+    if (fp64 != h->cg_fp64) clear_graphs(h);
+    h->cg_fp64 = fp64;
     return FS_OK;
 }
 
 int fs_set_extension_iterations(fs_handle* h, int n)
 {
     if (!h || n < 0) return h ? fail(h, FS_ERR_INVALID_ARGUMENT, "negative extension iterations") : 1;
+    if (n != h->n_ext) clear_graphs(h);
     h->n_ext = n;
-    clear_graphs(h);
     return FS_OK;
 }
 

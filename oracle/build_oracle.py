@@ -86,6 +86,22 @@ def build_reference(force: bool = False) -> str | None:
     return REFERENCE_SO
 
 
+def build_reference_program(src: str, name: str) -> str | None:
+    """Compiles a program written against the reference's class API with the
+    reference's own sources (same stand-in and flags as libfsref.so) into
+    oracle/_ref/<name>; None without the reference checkout."""
+    if build_reference() is None:
+        return None
+    ref = reference_dir()
+    exe = os.path.join(REF_DIR, name)
+    objs = [os.path.join(REF_DIR, n + ".o") for n in REFERENCE_SOURCES]
+    if _newer(exe, [src] + objs + [__file__]):
+        return exe
+    inc = ["-I", os.path.join(HERE, "eigen_shim"), "-I", os.path.join(ref, "include")]
+    _run(["g++", "-std=c++14", *FLAGS, "-w", *inc, src, *objs, "-o", exe])
+    return exe
+
+
 def main(argv: list[str]) -> int:
     force = "--force" in argv
     print("restatement:", build_restatement(force))
