@@ -28,6 +28,7 @@ STEP_SEMI_LAGRANGIAN, STEP_PIC, STEP_FLIP, STEP_PICFLIP = range(4)
  PH_G2P_PICFLIP, PH_G2P_PIC, PH_G2P_FLIP, PH_ADVECT_SAFE, PH_ADVECT, PH_SL_VELOCITY, PH_SL_PARTICLES,
  PH_SWAP) = range(16)
 CG_FLOAT, CG_DOUBLE = 0, 1
+POISSON_FP32, POISSON_FP64, POISSON_MIXED = 0, 1, 2
 TIMED_PHASES = ("classify", "p2g", "forces", "assembly", "cg", "project", "g2p")
 
 
@@ -43,6 +44,11 @@ class fs_config(C.Structure):
                 ("gravity_y", C.c_float), ("cg_max_iterations", C.c_int), ("cg_tolerance", C.c_double),
                 ("extension_iterations", C.c_int), ("device", C.c_int), ("cg_precision", C.c_int),
                 ("reserved", C.c_int * 7)]
+
+
+class fs_poisson_stats(C.Structure):
+    _fields_ = [("outer_iterations", C.c_int), ("inner_iterations", C.c_int), ("residual", C.c_double),
+                ("ms", C.c_float)]
 
 
 class fs_step_stats(C.Structure):
@@ -85,6 +91,12 @@ SIGNATURES = {
     "fs_get_stream": (_vp, [_vp]),
     "fs_set_stream": (_i, [_vp, _vp]),
     "fs_kernel_launches": (_i64, [_vp]),
+    "fs_poisson_create": (_i, [_i, _i, _f, _f, _i, C.POINTER(_vp)]),
+    "fs_poisson_destroy": (_i, [_vp]),
+    "fs_poisson_set_problem": (_i, [_vp, _vp, _vp]),
+    "fs_poisson_solve": (_i, [_vp, _i, _d, _i, _d, _i, C.POINTER(fs_poisson_stats)]),
+    "fs_poisson_get_solution": (_i, [_vp, _vp]),
+    "fs_poisson_kernel_launches": (_i64, [_vp]),
     "fs_pressure_solve_noalloc": (_i, [_i, _i, _f, _f, _vp, _vp, _vp, _d, _i, _i, _vp, C.POINTER(_i),
                                        C.POINTER(_d), _vp]),
 }
@@ -288,3 +300,49 @@ class FluidSim:
         s["pressure"] = self.pressure()
         s["particles"] = self.particles()
         return s
+
+
+class PoissonSolver:
+    """Pressure projection alone on the GPU (fs_poisson_*): labels + double rhs in,
+    double pressure out, by the FP32, FP64 or mixed-precision method."""
+
+    def __init__(self, size_x: int, size_y: int, length_x: float, length_y: float, device: int = 0):
+        self.lib = load_library()
+        h = C.c_void_p()
+        rc = self.lib.fs_poisson_create(size_x, size_y, length_x, length_y, device, C.byref(h))
+        if rc != FS_OK:
+            raise FsError(rc, self.lib.fs_last_error(None).decode())
+        self.h = h
+        self.nx, self.ny = size_x, size_y
+
+    def _check(self, rc: int) -> None:
+        if rc != FS_OK:
+            raise FsError(rc, self.lib.fs_last_error(None).decode())
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            self.lib.fs_poisson_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_problem(self, labels: np.ndarray, rhs: np.ndarray) -> None:
+        lab = np.ascontiguousarray(labels, dtype=np.uint8).reshape(self.ny, self.nx)
+        b = np.ascontiguousarray(rhs, dtype=np.float64).reshape(self.ny, self.nx)
+        self._check(self.lib.fs_poisson_set_problem(self.h, _ptr(lab), _ptr(b)))
+
+    def solve(self, method: int, tol: float, maxit: int, inner_tol: float = 1e-3,
+              inner_precision: int = CG_FLOAT) -> dict:
+        st = fs_poisson_stats()
+        self._check(self.lib.fs_poisson_solve(self.h, method, tol, maxit, inner_tol, inner_precision, C.byref(st)))
+        return {"outer_iterations": st.outer_iterations, "inner_iterations": st.inner_iterations,
+                "residual": st.residual, "ms": st.ms}
+
+    def solution(self) -> np.ndarray:
+        out = np.empty((self.ny, self.nx), np.float64)
+        self._check(self.lib.fs_poisson_get_solution(self.h, _ptr(out)))
+        return out

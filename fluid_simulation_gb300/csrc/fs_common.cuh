@@ -67,6 +67,43 @@ __device__ __forceinline__ uint8_t cell_type(const uint8_t* __restrict__ lab, co
     return lab[i + j * g.nx];
 }
 
+// Row of the pressure matrix for fluid cell c = (i, j) (src/FluidSolver.cpp:369-410):
+// flags bit 0 / bit 1 = liquid left / right neighbour (fluid indices k-1 / k+1
+// in the j-major order), bits 2-4 = number of non-solid neighbours n (the
+// diagonal is -n / dx^2); down / up = fluid indices of the liquid cells below /
+// above, or -1.  A LIQUID cell on the grid border (impossible after
+// classification) would make the reference read outside the grid; such
+// neighbours are skipped.
+__device__ __forceinline__ void matrix_row(const uint8_t* __restrict__ lab, const Geom& g,
+                                           const int32_t* __restrict__ fidx, int64_t c, int i, int j, uint8_t& flags,
+                                           int32_t& down, int32_t& up)
+{
+    int nns = 0;
+    uint8_t fl = 0;
+    down = up = -1;
+    uint8_t ct = cell_type(lab, g, i - 1, j);
+    if (ct != SOLID) {
+        if (ct == LIQUID && i > 0) fl |= 1;
+        ++nns;
+    }
+    ct = cell_type(lab, g, i + 1, j);
+    if (ct != SOLID) {
+        if (ct == LIQUID && i < g.nx - 1) fl |= 2;
+        ++nns;
+    }
+    ct = cell_type(lab, g, i, j - 1);
+    if (ct != SOLID) {
+        if (ct == LIQUID && j > 0) down = fidx[c - g.nx];
+        ++nns;
+    }
+    ct = cell_type(lab, g, i, j + 1);
+    if (ct != SOLID) {
+        if (ct == LIQUID && j < g.ny - 1) up = fidx[c + g.nx];
+        ++nns;
+    }
+    flags = (uint8_t)(fl | (nns << 2));
+}
+
 // Grid::valueInterpolated (include/Grid.h:117-144); +1 neighbour formed after clamping.
 __device__ __forceinline__ float value_interp(const float* __restrict__ grid, const Geom& g, float gdx, float gdy,
                                               float x, float y)

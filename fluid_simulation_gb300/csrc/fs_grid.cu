@@ -216,34 +216,7 @@ __global__ void k_assemble(Geom g, const uint8_t* __restrict__ lab, const int32_
     if (t >= nf) return;
     const int64_t c = cell_of[t];
     const int i = (int)(c % g.nx), j = (int)(c / g.nx);
-    int nns = 0;
-    uint8_t fl = 0;
-    int32_t dn = -1, upi = -1;
-    uint8_t ct = cell_type(lab, g, i - 1, j);
-    if (ct != SOLID) {
-        if (ct == LIQUID && i > 0) fl |= 1;
-        ++nns;
-    }
-    ct = cell_type(lab, g, i + 1, j);
-    if (ct != SOLID) {
-        if (ct == LIQUID && i < g.nx - 1) fl |= 2;
-        ++nns;
-    }
-    // A LIQUID cell on the grid border (impossible after classification) would
-    // make the reference read outside the grid; such neighbours are skipped.
-    ct = cell_type(lab, g, i, j - 1);
-    if (ct != SOLID) {
-        if (ct == LIQUID && j > 0) dn = fidx[c - g.nx];
-        ++nns;
-    }
-    ct = cell_type(lab, g, i, j + 1);
-    if (ct != SOLID) {
-        if (ct == LIQUID && j < g.ny - 1) upi = fidx[c + g.nx];
-        ++nns;
-    }
-    flags[t] = (uint8_t)(fl | (nns << 2));
-    down[t] = dn;
-    up[t] = upi;
+    matrix_row(lab, g, fidx, c, i, j, flags[t], down[t], up[t]);
     const float u1 = i < g.nx - 1 ? uf[c + 1] : 0.0f;
     const float v1 = j < g.ny - 1 ? vf[c + g.nx] : 0.0f;
     const float ddx = fdiv(fsub(u1, uf[c]), g.dx);

@@ -115,3 +115,37 @@ def dam_break_large(n: int = 1024, seed: int = 0xC2) -> Scene:
                  cg_tolerance=1e-5, cg_max_iterations=100000,
                  description="dam break %dx%d + disc r=%g, 4 particles/cell, CG 1e-5" % (n, n, r),
                  meta={"block": [1, 1 + w, 1, 1 + w], "disc": [cx, cy, r], "seed": seed})
+
+
+def projection_problem(n: int = 4096, seed: int = 0xC5, solid_fraction: float = 0.05):
+    """Pressure projection alone: an n x n fluid-filled domain, solid border and
+    Bernoulli(solid_fraction) interior solids (seeded), fluid cells with no
+    non-solid neighbour turned solid (their matrix row would be zero), and a
+    right-hand side of i.i.d. N(0, 1) values (Box-Muller on the SplitMix64
+    stream) with the mean of every 4-connected fluid component removed, so
+    that each component -- a pure Neumann problem, as nothing is AIR -- is
+    consistent.  Returns (labels uint8, rhs float64)."""
+    from scipy import ndimage
+
+    LIQUID, SOLID = 0, 2
+    u = uniform01(seed, n * n).reshape(n, n)
+    labels = np.where(u < solid_fraction, SOLID, LIQUID).astype(np.uint8)
+    labels[0, :] = labels[-1, :] = SOLID
+    labels[:, 0] = labels[:, -1] = SOLID
+    fluid = labels == LIQUID
+    nb = np.zeros_like(fluid, dtype=np.int32)
+    nb[1:, :] += fluid[:-1, :]
+    nb[:-1, :] += fluid[1:, :]
+    nb[:, 1:] += fluid[:, :-1]
+    nb[:, :-1] += fluid[:, 1:]
+    labels[fluid & (nb == 0)] = SOLID
+    fluid = labels == LIQUID
+    u1 = uniform01(seed ^ 0x5EED, n * n).astype(np.float64).reshape(n, n)
+    u2 = uniform01(seed ^ 0xBEEF, n * n).astype(np.float64).reshape(n, n)
+    g = np.sqrt(-2.0 * np.log(1.0 - u1)) * np.cos(2.0 * np.pi * u2)
+    comp, ncomp = ndimage.label(fluid, structure=[[0, 1, 0], [1, 1, 1], [0, 1, 0]])
+    sums = ndimage.sum(g, comp, index=np.arange(1, ncomp + 1))
+    counts = ndimage.sum(np.ones_like(g), comp, index=np.arange(1, ncomp + 1))
+    means = np.concatenate([[0.0], sums / counts])
+    rhs = np.where(fluid, g - means[comp], 0.0)
+    return labels, rhs

@@ -203,6 +203,42 @@ FS_API int fs_set_stream(fs_handle* h, void* stream);
 /* Number of this library's kernel launches queued so far on h. */
 FS_API int64_t fs_kernel_launches(fs_handle* h);
 
+/* Pressure projection alone (no particles; BASELINE configs[4]-style use): the
+ * Poisson system of FluidSolver::pressureSolve (src/FluidSolver.cpp:363-425)
+ * built from a label grid (FS_LIQUID = unknown, FS_AIR = pressure 0,
+ * FS_SOLID = wall), with a double right-hand side per cell, solved by
+ *   FS_POISSON_FP32   the step's CG: float vectors, dots per inner_precision;
+ *   FS_POISSON_FP64   CG with double vectors, SpMV and dots;
+ *   FS_POISSON_MIXED  FP64 iterative refinement (x and b - A x in double)
+ *                     around float-vector CG corrections solved to
+ *                     inner_tolerance.
+ * tolerance is the relative residual ||b - A x|| / ||b|| (for MIXED and FP64
+ * measured in double; for FP32 in the CG's own precision).  A fluid
+ * component with no AIR neighbour is singular: its right-hand side must sum
+ * to zero. */
+#define FS_POISSON_FP32 0
+#define FS_POISSON_FP64 1
+#define FS_POISSON_MIXED 2
+
+typedef struct fs_poisson fs_poisson;
+typedef struct fs_poisson_stats
+{
+    int outer_iterations;  /* refinement steps (1 for FP32 / FP64) */
+    int inner_iterations;  /* CG updates in total */
+    double residual;       /* final ||b - A x|| / ||b||, evaluated in double */
+    float ms;              /* device time of the solve */
+} fs_poisson_stats;
+
+FS_API int fs_poisson_create(int size_x, int size_y, float length_x, float length_y, int device, fs_poisson** out);
+FS_API int fs_poisson_destroy(fs_poisson* p);
+/* labels and rhs: host arrays of size_x * size_y (row-major); rhs is read on LIQUID cells. */
+FS_API int fs_poisson_set_problem(fs_poisson* p, const uint8_t* labels, const double* rhs);
+FS_API int fs_poisson_solve(fs_poisson* p, int method, double tolerance, int max_iterations, double inner_tolerance,
+                            int inner_precision, fs_poisson_stats* stats);
+/* The solution on every cell (0 outside fluid), host array of doubles. */
+FS_API int fs_poisson_get_solution(fs_poisson* p, double* out);
+FS_API int64_t fs_poisson_kernel_launches(const fs_poisson* p);
+
 /* Allocation-free pressure solve.  No counterpart in the reference: this is
  * FluidSolver::pressureSolve's fluid indexing, assembly and conjugate gradient
  * for callers that cannot allocate device memory -- an application that owns

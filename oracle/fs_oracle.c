@@ -74,6 +74,7 @@ struct fso_sim
     /* CG scratch */
     float *cg_b, *cg_x, *cg_r, *cg_p, *cg_q, *cg_z, *cg_diag, *cg_inv;
     int32_t *cg_down, *cg_up, *cg_left, *cg_right;
+    uint8_t* cg_nns;      /* non-solid neighbours of each fluid cell */
     double* cg_acc;
     float* cg_accf;
 };
@@ -220,6 +221,7 @@ fso_sim* fso_create(int nx, int ny, float lx, float ly, float density, float pic
     s->cg_up = (int32_t*)xcalloc(n, sizeof(int32_t));
     s->cg_left = (int32_t*)xcalloc(n, sizeof(int32_t));
     s->cg_right = (int32_t*)xcalloc(n, sizeof(int32_t));
+    s->cg_nns = (uint8_t*)xcalloc(n, 1);
     s->cg_acc = (double*)xcalloc(n, sizeof(double));
     s->cg_accf = (float*)xcalloc(n, sizeof(float));
     /* MacGrid ctor clears the cell types (MacGrid.cpp:24 -> :32-50). */
@@ -244,7 +246,7 @@ void fso_destroy(fso_sim* s)
     free(s->part); free(s->pressure); free(s->src);
     free(s->cg_b); free(s->cg_x); free(s->cg_r); free(s->cg_p); free(s->cg_q); free(s->cg_z);
     free(s->cg_diag); free(s->cg_inv); free(s->cg_down); free(s->cg_up); free(s->cg_left);
-    free(s->cg_right); free(s->cg_acc); free(s->cg_accf);
+    free(s->cg_right); free(s->cg_acc); free(s->cg_accf); free(s->cg_nns);
     free(s);
 }
 
@@ -663,8 +665,10 @@ static void cg_solve(fso_sim* s, int n, float off)
     else FSO_CG_BODY(float, dot_f, FLT_MIN);
 }
 
-/* FluidSolver::pressureSolve (FluidSolver.cpp:323-483). */
-static void ph_pressure(fso_sim* s, float dt)
+/* Fluid indexing (FluidSolver.cpp:329-346; the particle counts are reset) and
+ * the matrix rows of :363-416 (off-diagonal and diagonal in float through
+ * double pow(), as the reference).  Returns the number of fluid cells. */
+static int index_and_assemble(fso_sim* s)
 {
     const int nx = s->nx, ny = s->ny;
     int nf = 0;
@@ -676,21 +680,6 @@ static void ph_pressure(fso_sim* s, float dt)
             s->counts[c] = 0;
         }
     s->n_fluid = nf;
-    if (nf == 0) {
-        s->cg_iters = 0;
-        s->cg_error = 0.0;
-        return;
-    }
-    /* :353-360 -- unclamped; out-of-range indices are undefined behaviour in
-     * the reference and are skipped here. */
-    for (int64_t k = 0; k < s->n_part; ++k) {
-        const float px = s->part[4 * k], py = s->part[4 * k + 1];
-        const int x = (int)((px / s->lx) * nx);
-        const int y = (int)((py / s->ly) * ny);
-        if (x >= 0 && x < nx && y >= 0 && y < ny) s->counts[IDX(s, x, y)]++;
-    }
-    /* :363-416.  Coefficients go through double pow(), as in the reference. */
-    const float off = (float)(1 / pow(s->dx, 2));
     const float* uf = UF(s);
     const float* vf = VF(s);
     for (int j = 0; j < ny; ++j)
@@ -717,6 +706,7 @@ static void ph_pressure(fso_sim* s, float dt)
                 nns++;
             }
             s->cg_diag[k] = (float)(-nns / pow(s->dx, 2));
+            s->cg_nns[k] = (uint8_t)nns;
             /* MacGrid::divVelX + divVelY (MacGrid.h:98-111). */
             float ddx = uf[IDX(s, i + 1, j)] - uf[c];
             ddx = ddx / s->dx;
@@ -724,6 +714,30 @@ static void ph_pressure(fso_sim* s, float dt)
             ddy = ddy / s->dy;
             s->cg_b[k] = ddx + ddy;
         }
+    return nf;
+}
+
+/* FluidSolver::pressureSolve (FluidSolver.cpp:323-483). */
+static void ph_pressure(fso_sim* s, float dt)
+{
+    const int nx = s->nx, ny = s->ny;
+    const int nf = index_and_assemble(s);
+    if (nf == 0) {
+        s->cg_iters = 0;
+        s->cg_error = 0.0;
+        return;
+    }
+    /* :353-360 -- unclamped; out-of-range indices are undefined behaviour in
+     * the reference and are skipped here. */
+    for (int64_t k = 0; k < s->n_part; ++k) {
+        const float px = s->part[4 * k], py = s->part[4 * k + 1];
+        const int x = (int)((px / s->lx) * nx);
+        const int y = (int)((py / s->ly) * ny);
+        if (x >= 0 && x < nx && y >= 0 && y < ny) s->counts[IDX(s, x, y)]++;
+    }
+    const float off = (float)(1 / pow(s->dx, 2));
+    const float* uf = UF(s);
+    const float* vf = VF(s);
     cg_solve(s, nf, off);
     memcpy(s->pressure, s->cg_x, (size_t)nf * sizeof(float));
 
@@ -1047,4 +1061,147 @@ void fso_update(fso_sim* s, float dt)
         }
         f->time_since_last += dt;
     }
+}
+
+
+/* ---- pressure projection alone (the GPU's fs_poisson_*) ------------------- */
+
+/* Row of A in double: ascending column order from +0 (as spmv()). */
+static double row64(const fso_sim* s, const double* v, int k, double off, const double* dtab)
+{
+    double acc = 0.0, t;
+    if (s->cg_down[k] >= 0) { t = off * v[s->cg_down[k]]; acc = acc + t; }
+    if (s->cg_left[k] >= 0) { t = off * v[s->cg_left[k]]; acc = acc + t; }
+    t = dtab[s->cg_nns[k]] * v[k];
+    acc = acc + t;
+    if (s->cg_right[k] >= 0) { t = off * v[s->cg_right[k]]; acc = acc + t; }
+    if (s->cg_up[k] >= 0) { t = off * v[s->cg_up[k]]; acc = acc + t; }
+    return acc;
+}
+
+static double dot64v(double* acc, const double* a, const double* b, int n)
+{
+    for (int k = 0; k < n; ++k) acc[k] = a[k] * b[k];
+    return rsum32(acc, n);
+}
+
+/* CG with double vectors, SpMV and dots (the GPU's k_cg64). */
+static void cg64(fso_sim* s, int n, const double* b, double* x, double tol, int maxit, double off,
+                 const double* dtab, const double* itab, int* iters_out)
+{
+    double* r = (double*)xcalloc((size_t)n, sizeof(double));
+    double* z = (double*)xcalloc((size_t)n, sizeof(double));
+    double* p = (double*)xcalloc((size_t)n, sizeof(double));
+    double* q = (double*)xcalloc((size_t)n, sizeof(double));
+    double* acc = (double*)xcalloc((size_t)n, sizeof(double));
+    for (int k = 0; k < n; ++k) {
+        x[k] = 0.0;
+        r[k] = b[k];
+        z[k] = itab[s->cg_nns[k]] * r[k];
+    }
+    int iters = 0;
+    const double bb = dot64v(acc, r, r, n);
+    double rz = dot64v(acc, r, z, n), rr = bb;
+    double thr = tol * tol;
+    thr = thr * bb;
+    if (thr < DBL_MIN) thr = DBL_MIN;
+    if (bb != 0.0 && !(rr < thr)) {
+        for (int k = 0; k < n; ++k) p[k] = z[k];
+        for (int it = 1; it <= maxit; ++it) {
+            for (int k = 0; k < n; ++k) q[k] = row64(s, p, k, off, dtab);
+            const double alpha = rz / dot64v(acc, p, q, n);
+            for (int k = 0; k < n; ++k) {
+                double t = alpha * p[k];
+                x[k] = x[k] + t;
+                t = alpha * q[k];
+                r[k] = r[k] - t;
+                z[k] = itab[s->cg_nns[k]] * r[k];
+            }
+            rr = dot64v(acc, r, r, n);
+            const double rz_new = dot64v(acc, r, z, n);
+            iters = it;
+            if (rr < thr) break;
+            const double beta = rz_new / rz;
+            rz = rz_new;
+            for (int k = 0; k < n; ++k) {
+                const double t = beta * p[k];
+                p[k] = z[k] + t;
+            }
+        }
+    }
+    *iters_out = iters;
+    free(r); free(z); free(p); free(q); free(acc);
+}
+
+int fso_poisson_solve(int nx, int ny, float lx, float ly, const uint8_t* labels, const double* rhs, int method,
+                      double tol, int maxit, double inner_tol, int inner_precision, double* x_out,
+                      int* outer_out, int* inner_out, double* residual_out)
+{
+    fso_sim* s = fso_create(nx, ny, lx, ly, 1.0f, 0.0f);
+    memcpy(s->labels, labels, (size_t)nx * ny);
+    const int nf = index_and_assemble(s);
+    const double dx2 = pow(s->dx, 2);
+    const float off32 = (float)(1 / dx2);
+    const double off64 = 1.0 / dx2;
+    double dtab[5], itab[5];
+    for (int k = 0; k < 5; ++k) {
+        dtab[k] = -k / dx2;
+        itab[k] = k ? 1.0 / dtab[k] : 1.0;
+    }
+    double* b = (double*)xcalloc((size_t)nf, sizeof(double));
+    double* x = (double*)xcalloc((size_t)nf, sizeof(double));
+    double* r = (double*)xcalloc((size_t)nf, sizeof(double));
+    double* acc = (double*)xcalloc((size_t)nf, sizeof(double));
+    for (int j = 0; j < ny; ++j)
+        for (int i = 0; i < nx; ++i) {
+            const int k = s->fidx[IDX(s, i, j)];
+            if (k >= 0) b[k] = rhs[IDX(s, i, j)];
+        }
+    int outer = 0, inner = 0;
+    s->cg_double = inner_precision != 0;
+    if (method == 0) { /* float CG */
+        for (int k = 0; k < nf; ++k) s->cg_b[k] = (float)b[k];
+        s->cg_tol = tol;
+        s->cg_maxit = maxit;
+        cg_solve(s, nf, off32);
+        for (int k = 0; k < nf; ++k) x[k] = (double)s->cg_x[k];
+        outer = 1;
+        inner = s->cg_iters;
+    } else if (method == 1) { /* FP64 CG */
+        cg64(s, nf, b, x, tol, maxit, off64, dtab, itab, &inner);
+        outer = 1;
+    } else { /* FP64 refinement around float CG corrections */
+        for (int k = 0; k < nf; ++k) r[k] = b[k];
+        const double bb = dot64v(acc, b, b, nf);
+        const double thr = tol * tol * bb;
+        double rr = bb;
+        s->cg_tol = inner_tol;
+        s->cg_maxit = maxit;
+        for (int it = 0; it < 64; ++it) {
+            if (!(rr >= thr) || bb == 0.0) break;
+            for (int k = 0; k < nf; ++k) s->cg_b[k] = (float)r[k];
+            cg_solve(s, nf, off32);
+            for (int k = 0; k < nf; ++k) x[k] = x[k] + (double)s->cg_x[k];
+            for (int k = 0; k < nf; ++k) r[k] = b[k] - row64(s, x, k, off64, dtab);
+            const double rr_new = dot64v(acc, r, r, nf);
+            inner += s->cg_iters;
+            outer = it + 1;
+            if (s->cg_iters == 0) break;
+            rr = rr_new;
+        }
+    }
+    /* final residual in double */
+    for (int k = 0; k < nf; ++k) r[k] = b[k] - row64(s, x, k, off64, dtab);
+    const double rr = dot64v(acc, r, r, nf), bb = dot64v(acc, b, b, nf);
+    for (int j = 0; j < ny; ++j)
+        for (int i = 0; i < nx; ++i) {
+            const int k = s->fidx[IDX(s, i, j)];
+            x_out[IDX(s, i, j)] = k >= 0 ? x[k] : 0.0;
+        }
+    if (outer_out) *outer_out = outer;
+    if (inner_out) *inner_out = inner;
+    if (residual_out) *residual_out = bb > 0 ? sqrt(rr / bb) : 0.0;
+    free(b); free(x); free(r); free(acc);
+    fso_destroy(s);
+    return nf;
 }

@@ -117,6 +117,15 @@ void fso_add_source(fso_sim* s, float x_min, float x_max, float y_min, float y_m
                     int max_spawns);
 void fso_update(fso_sim* s, float dt);
 
+/* Pressure projection alone (the GPU's fs_poisson_*), restatement only:
+ * method 0 float CG (dots per inner_precision), 1 double CG, 2 double
+ * iterative refinement around float CG corrections solved to inner_tol.
+ * x_out: size_x * size_y doubles (0 outside fluid).  Returns the fluid count. */
+int fso_poisson_solve(int size_x, int size_y, float length_x, float length_y, const uint8_t* labels,
+                      const double* rhs, int method, double tol, int max_iterations, double inner_tol,
+                      int inner_precision, double* x_out, int* outer_iterations, int* inner_iterations,
+                      double* residual);
+
 /* Name of the implementation ("restatement" or "reference"). */
 const char* fso_kind(void);
 

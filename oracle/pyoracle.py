@@ -68,6 +68,8 @@ def _lib(kind: str) -> C.CDLL:
         "fso_add_source": (None, [vp, f, f, f, f, f, f, f, f, f, i]),
         "fso_update": (None, [vp, f]),
         "fso_kind": (C.c_char_p, []),
+        "fso_poisson_solve": (i, [i, i, f, f, vp, vp, i, d, i, d, i, vp, C.POINTER(i), C.POINTER(i),
+                                  C.POINTER(d)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -79,6 +81,21 @@ def _lib(kind: str) -> C.CDLL:
 
 def _ptr(a: np.ndarray) -> int:
     return a.ctypes.data
+
+
+def poisson_solve(labels: np.ndarray, rhs: np.ndarray, length_x: float, length_y: float, method: int, tol: float,
+                  maxit: int, inner_tol: float = 1e-3, inner_precision: int = 0) -> tuple[np.ndarray, dict]:
+    """The restatement of the GPU's pressure-projection solver (fs_poisson_*)."""
+    lib = _lib("restatement")
+    ny, nx = labels.shape
+    lab = np.ascontiguousarray(labels, dtype=np.uint8)
+    b = np.ascontiguousarray(rhs, dtype=np.float64)
+    x = np.empty((ny, nx), np.float64)
+    outer, inner, res = C.c_int(), C.c_int(), C.c_double()
+    nf = lib.fso_poisson_solve(nx, ny, length_x, length_y, _ptr(lab), _ptr(b), method, tol, maxit, inner_tol,
+                               inner_precision, _ptr(x), C.byref(outer), C.byref(inner), C.byref(res))
+    return x, {"n_fluid": nf, "outer_iterations": outer.value, "inner_iterations": inner.value,
+               "residual": res.value}
 
 
 class OracleSim:

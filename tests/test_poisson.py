@@ -1,0 +1,129 @@
+"""Pressure projection alone (fs_poisson_*): the FP32, FP64 and mixed
+(FP64 iterative refinement around float CG) methods on seeded fluid-filled
+domains with random solid cells, against the CPU restatement
+(oracle fso_poisson_solve, bit for bit) and against an FP64 direct solve
+(scipy) for the error each method leaves."""
+import numpy as np
+import pytest
+
+from fluid_simulation_gb300 import scenes
+from oracle import pyoracle as po
+
+
+def _system(labels, rhs):
+    """Sparse A (the reference's matrix, unit cells) and b over fluid cells."""
+    import scipy.sparse as sp
+
+    ny, nx = labels.shape
+    fluid = labels == 0
+    idx = -np.ones(labels.shape, np.int64)
+    idx[fluid] = np.arange(fluid.sum())
+    rows, cols, vals = [], [], []
+    jj, ii = np.nonzero(fluid)
+    k = idx[jj, ii]
+    diag = np.zeros(k.size)
+    for dj, di in ((0, -1), (0, 1), (-1, 0), (1, 0)):
+        nj, ni = jj + dj, ii + di
+        nl = labels[nj, ni]
+        nonsolid = nl != 2
+        diag -= nonsolid
+        liq = nl == 0
+        rows.append(k[liq])
+        cols.append(idx[nj[liq], ni[liq]])
+        vals.append(np.ones(liq.sum()))
+    rows.append(k)
+    cols.append(k)
+    vals.append(diag)
+    n = int(fluid.sum())
+    A = sp.csr_matrix((np.concatenate(vals), (np.concatenate(rows), np.concatenate(cols))), shape=(n, n))
+    return A, rhs[fluid], fluid
+
+
+def test_problem_generator_is_consistent():
+    labels, rhs = scenes.projection_problem(96, seed=3)
+    A, b, fluid = _system(labels, rhs)
+    assert abs(b.sum()) < 1e-9 * np.abs(b).sum()
+    assert fluid.mean() > 0.85
+    assert np.all(np.asarray(A.diagonal()) < 0)  # no zero-diagonal cell left
+
+
+@pytest.mark.parametrize("method", [0, 1, 2])
+def test_restatement_residuals(method):
+    labels, rhs = scenes.projection_problem(64, seed=11)
+    tol = 1e-5 if method == 0 else 1e-10
+    x, st = po.poisson_solve(labels, rhs, 64.0, 64.0, method, tol, 20000, inner_tol=1e-3)
+    A, b, fluid = _system(labels, rhs)
+    r = b - A @ x[fluid]
+    assert np.linalg.norm(r) / np.linalg.norm(b) < (3e-5 if method == 0 else 1e-9)
+    assert st["residual"] < (1e-4 if method == 0 else 1e-10)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("shape", [(64, 64), (200, 130)])
+@pytest.mark.parametrize("method,inner_precision", [(0, 0), (0, 1), (1, 0), (2, 0), (2, 1)])
+def test_gpu_matches_restatement_bit_exact(shape, method, inner_precision):
+    import fluid_simulation_gb300 as fsg
+    from fluid_simulation_gb300 import build as fsbuild
+
+    fsbuild.build()
+    nx, ny = shape
+    labels, rhs = scenes.projection_problem(max(nx, ny), seed=21)
+    labels, rhs = np.ascontiguousarray(labels[:ny, :nx]), np.ascontiguousarray(rhs[:ny, :nx])
+    labels[-1, :] = 2
+    labels[:, -1] = 2
+    rhs[labels != 0] = 0.0
+    # the cut changed components: make every one consistent again
+    from scipy import ndimage
+    comp, nc = ndimage.label(labels == 0, structure=[[0, 1, 0], [1, 1, 1], [0, 1, 0]])
+    means = np.concatenate([[0.0], ndimage.mean(rhs, comp, index=np.arange(1, nc + 1))])
+    rhs = np.where(labels == 0, rhs - means[comp], 0.0)
+    tol = 1e-5 if method == 0 else 1e-10
+    ps = fsg.PoissonSolver(nx, ny, float(nx), float(ny))
+    ps.set_problem(labels, rhs)
+    st = ps.solve(method, tol, 20000, inner_tol=1e-3, inner_precision=inner_precision)
+    x = ps.solution()
+    xo, so = po.poisson_solve(labels, rhs, float(nx), float(ny), method, tol, 20000, inner_tol=1e-3,
+                              inner_precision=inner_precision)
+    assert (st["outer_iterations"], st["inner_iterations"]) == (so["outer_iterations"], so["inner_iterations"])
+    assert st["residual"] == so["residual"]
+    assert np.array_equal(x.view(np.uint64), xo.view(np.uint64))
+
+
+@pytest.mark.gpu
+def test_gpu_methods_error_against_fp64_direct_solve():
+    """Error of each method against an FP64 direct solve (pinned to zero mean
+    per component, where the solution is unique)."""
+    import scipy.sparse.linalg as spla
+    from scipy import ndimage
+
+    import fluid_simulation_gb300 as fsg
+    from fluid_simulation_gb300 import build as fsbuild
+
+    fsbuild.build()
+    n = 128
+    labels, rhs = scenes.projection_problem(n, seed=5)
+    A, b, fluid = _system(labels, rhs)
+    comp, nc = ndimage.label(fluid, structure=[[0, 1, 0], [1, 1, 1], [0, 1, 0]])
+    cidx = comp[fluid]
+    # singular per component: pin one unknown per component, then remove means
+    pins = np.array([np.nonzero(cidx == c)[0][0] for c in range(1, nc + 1)])
+    keep = np.ones(b.size, bool)
+    keep[pins] = False
+    xd = np.zeros(b.size)
+    xd[keep] = spla.spsolve(A[keep][:, keep].tocsc(), b[keep])
+
+    def demean(v):
+        m = ndimage.mean(v, cidx, index=np.arange(1, nc + 1))
+        return v - m[cidx - 1]
+
+    xd = demean(xd)
+    ps = fsg.PoissonSolver(n, n, float(n), float(n))
+    ps.set_problem(labels, rhs)
+    errs = {}
+    for name, method, tol in (("fp32", 0, 1e-5), ("fp64", 1, 1e-10), ("mixed", 2, 1e-10)):
+        st = ps.solve(method, tol, 50000, inner_tol=1e-3)
+        x = demean(ps.solution()[fluid])
+        errs[name] = np.linalg.norm(x - xd) / np.linalg.norm(xd)
+        assert st["residual"] < (2e-5 if method == 0 else 1e-10), (name, st)
+    assert errs["fp64"] < 1e-8 and errs["mixed"] < 1e-8, errs
+    assert errs["fp32"] < 1e-2, errs
