@@ -71,7 +71,10 @@ def _lib(kind: str) -> C.CDLL:
         "fso_poisson_solve": (i, [i, i, f, f, vp, vp, i, d, i, d, i, vp, C.POINTER(i), C.POINTER(i),
                                   C.POINTER(d)]),
     }
+    optional = {"fso_poisson_solve"}   # restatement only: the reference has no standalone solve
     for name, (res, args) in sig.items():
+        if name in optional and not hasattr(lib, name):
+            continue
         fn = getattr(lib, name)
         fn.restype = res
         fn.argtypes = args
