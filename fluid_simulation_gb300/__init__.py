@@ -97,6 +97,26 @@ SIGNATURES = {
     "fs_poisson_solve": (_i, [_vp, _i, _d, _i, _d, _i, C.POINTER(fs_poisson_stats)]),
     "fs_poisson_get_solution": (_i, [_vp, _vp]),
     "fs_poisson_kernel_launches": (_i64, [_vp]),
+    "fs_batch_create": (_i, [_i, C.POINTER(fs_config), C.POINTER(_vp)]),
+    "fs_batch_destroy": (_i, [_vp]),
+    "fs_batch_last_error": (C.c_char_p, [_vp]),
+    "fs_batch_size": (_i, [_vp]),
+    "fs_batch_set_particles": (_i, [_vp, _i, _vp, _i64]),
+    "fs_batch_num_particles": (_i, [_vp, _i, C.POINTER(_i64)]),
+    "fs_batch_get_particles": (_i, [_vp, _i, _vp, _i64]),
+    "fs_batch_set_solid_mask": (_i, [_vp, _i, _vp]),
+    "fs_batch_get_grid": (_i, [_vp, _i, _i, _vp]),
+    "fs_batch_get_labels": (_i, [_vp, _i, _vp]),
+    "fs_batch_get_pressure": (_i, [_vp, _i, _vp]),
+    "fs_batch_step": (_i, [_vp, _i, _f]),
+    "fs_batch_synchronize": (_i, [_vp]),
+    "fs_batch_get_stats": (_i, [_vp, _i, C.POINTER(fs_step_stats)]),
+    "fs_batch_tune": (_i, [_vp, _i, _f, _i, _vp]),
+    "fs_batch_set_tuning": (_i, [_vp, _i]),
+    "fs_batch_get_tuning": (_i, [_vp]),
+    "fs_batch_set_graphs": (_i, [_vp, _i]),
+    "fs_batch_get_stream": (_vp, [_vp]),
+    "fs_batch_kernel_launches": (_i64, [_vp]),
     "fs_pressure_solve_noalloc": (_i, [_i, _i, _f, _f, _vp, _vp, _vp, _d, _i, _i, _vp, C.POINTER(_i),
                                        C.POINTER(_d), _vp]),
 }
@@ -299,6 +319,137 @@ class FluidSim:
         s["particle_counts"] = self.particle_counts()
         s["pressure"] = self.pressure()
         s["particles"] = self.particles()
+        return s
+
+
+def scene_config(lib: C.CDLL, sc, device: int = 0) -> fs_config:
+    """The fs_config of a Scene (fluid_simulation_gb300.scenes)."""
+    cfg = fs_config()
+    lib.fs_config_init(C.byref(cfg), sc.size_x, sc.size_y)
+    cfg.length_x, cfg.length_y = sc.length_x, sc.length_y
+    cfg.density, cfg.pic_ratio, cfg.device = sc.density, sc.pic_ratio, device
+    cfg.cg_tolerance, cfg.cg_max_iterations = sc.cg_tolerance, sc.cg_max_iterations
+    cfg.gravity_x, cfg.gravity_y = sc.gravity
+    return cfg
+
+
+class FluidBatch:
+    """Many independent FluidDomain + FluidSolver pairs stepped together (fs_batch_*)."""
+
+    def __init__(self, configs: list, device: int = 0):
+        self.lib = load_library()
+        n = len(configs)
+        arr = (fs_config * n)(*configs)
+        h = C.c_void_p()
+        rc = self.lib.fs_batch_create(n, arr, C.byref(h))
+        if rc != FS_OK:
+            raise FsError(rc, self.lib.fs_batch_last_error(None).decode())
+        self.h = h
+        self.shapes = [(c.size_y, c.size_x) for c in configs]
+
+    @classmethod
+    def from_scenes(cls, scenes: list, device: int = 0) -> "FluidBatch":
+        lib = load_library()
+        b = cls([scene_config(lib, sc, device) for sc in scenes], device)
+        for s, sc in enumerate(scenes):
+            if sc.solid is not None:
+                b.set_solid_mask(s, sc.solid)
+            b.set_particles(s, sc.particles)
+        return b
+
+    def __len__(self) -> int:
+        return len(self.shapes)
+
+    def _check(self, rc: int) -> None:
+        if rc != FS_OK:
+            raise FsError(rc, self.lib.fs_batch_last_error(self.h).decode())
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            self.lib.fs_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_particles(self, sim: int, xyuv: np.ndarray) -> None:
+        a = np.ascontiguousarray(xyuv, dtype=np.float32).reshape(-1, 4)
+        self._check(self.lib.fs_batch_set_particles(self.h, sim, _ptr(a), a.shape[0]))
+
+    def num_particles(self, sim: int) -> int:
+        n = C.c_int64()
+        self._check(self.lib.fs_batch_num_particles(self.h, sim, C.byref(n)))
+        return n.value
+
+    def particles(self, sim: int) -> np.ndarray:
+        n = self.num_particles(sim)
+        out = np.empty((n, 4), np.float32)
+        self._check(self.lib.fs_batch_get_particles(self.h, sim, _ptr(out), n))
+        return out
+
+    def set_solid_mask(self, sim: int, mask: np.ndarray | None) -> None:
+        if mask is None:
+            self._check(self.lib.fs_batch_set_solid_mask(self.h, sim, None))
+        else:
+            m = np.ascontiguousarray(mask, dtype=np.uint8).reshape(self.shapes[sim])
+            self._check(self.lib.fs_batch_set_solid_mask(self.h, sim, _ptr(m)))
+
+    def grid(self, sim: int, which: int) -> np.ndarray:
+        out = np.empty(self.shapes[sim], np.float32)
+        self._check(self.lib.fs_batch_get_grid(self.h, sim, which, _ptr(out)))
+        return out
+
+    def labels(self, sim: int) -> np.ndarray:
+        out = np.empty(self.shapes[sim], np.uint8)
+        self._check(self.lib.fs_batch_get_labels(self.h, sim, _ptr(out)))
+        return out
+
+    def pressure(self, sim: int) -> np.ndarray:
+        out = np.empty(self.shapes[sim], np.float32)
+        self._check(self.lib.fs_batch_get_pressure(self.h, sim, _ptr(out)))
+        return out
+
+    def step(self, method: int, dt: float) -> None:
+        self._check(self.lib.fs_batch_step(self.h, method, dt))
+
+    def synchronize(self) -> None:
+        self._check(self.lib.fs_batch_synchronize(self.h))
+
+    def stats(self, sim: int) -> dict:
+        s = fs_step_stats()
+        self._check(self.lib.fs_batch_get_stats(self.h, sim, C.byref(s)))
+        return {"cg_iterations": s.cg_iterations, "n_fluid": s.n_fluid, "cg_residual": s.cg_residual,
+                "warnings": s.warnings}
+
+    def tune(self, method: int, dt: float, steps: int = 2) -> dict:
+        ms = (C.c_float * 4)()
+        self._check(self.lib.fs_batch_tune(self.h, method, dt, steps, ms))
+        return {"chunks_per_cta": self.lib.fs_batch_get_tuning(self.h),
+                "ms_per_step": dict(zip((1, 2, 4, 8), list(ms)))}
+
+    def set_tuning(self, chunks_per_cta: int) -> None:
+        self._check(self.lib.fs_batch_set_tuning(self.h, chunks_per_cta))
+
+    def set_graphs(self, on: bool) -> None:
+        self._check(self.lib.fs_batch_set_graphs(self.h, int(on)))
+
+    def stream(self) -> int:
+        return self.lib.fs_batch_get_stream(self.h) or 0
+
+    def kernel_launches(self) -> int:
+        return self.lib.fs_batch_kernel_launches(self.h)
+
+    def state(self, sim: int) -> dict[str, np.ndarray]:
+        s = {name: self.grid(sim, w) for name, w in (("u_front", U_FRONT), ("v_front", V_FRONT),
+                                                      ("u_back", U_BACK), ("v_back", V_BACK),
+                                                      ("u_prev", U_PREV), ("v_prev", V_PREV),
+                                                      ("u_diff", U_DIFF), ("v_diff", V_DIFF))}
+        s["labels"] = self.labels(sim)
+        s["pressure"] = self.pressure(sim)
+        s["particles"] = self.particles(sim)
         return s
 
 

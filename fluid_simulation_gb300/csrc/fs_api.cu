@@ -9,7 +9,7 @@
 #include <string>
 #include <vector>
 
-#include "fs_internal.h"
+#include "fs_step.h"
 
 using namespace fs;
 
@@ -223,152 +223,85 @@ float* VF(fs_handle* h) { return h->v[h->front]; }
 float* UB(fs_handle* h) { return h->u[1 - h->front]; }
 float* VB(fs_handle* h) { return h->v[1 - h->front]; }
 
-void mark(fs_handle* h, int k)
+Seg seg(const fs_handle* h)
 {
+    Seg s{};
+    s.g = h->g;
+    s.np = h->n_part;
+    s.pic = h->pic;
+    s.rho = h->cfg.density;
+    s.gx = h->gx;
+    s.gy = h->gy;
+    return s;
+}
+
+Domain domain(const fs_handle* h) { return Domain::single(seg(h)); }
+
+void solve_hook(void* owner, const Launch& L)
+{
+    fs_handle* h = static_cast<fs_handle*>(owner);
+    cg_solve(L, h->cg, h->d_nfluid, h->cg_b, h->diag_tab, h->cg_down, h->cg_up, h->cg_flags, h->off, h->cg_tol,
+             h->cg_maxit, h->cg_fp64, h->d_status);
+}
+
+void mark_hook(void* owner, int k)
+{
+    fs_handle* h = static_cast<fs_handle*>(owner);
     if (h->timing) cudaEventRecord(h->ev[k], h->stream);
 }
 
-// ---- phases (enqueue only) --------------------------------------------------
-
-void ph_classify(fs_handle* h)
+// The handle's device arrays as the shared step code sees them.
+StepState state(fs_handle* h)
 {
-    const Launch L = h->L();
-    labels_clear(L, h->g, h->labels);
-    labels_from_particles(L, h->g, h->px, h->py, h->n_part, h->labels);
-    labels_finalize(L, h->g, h->labels, h->solid);
-}
-
-void ph_p2g(fs_handle* h)
-{
-    const Launch L = h->L();
-    const Geom& g = h->g;
-    p2g_positions(L, g, h->px, h->py, h->n_part, h->yu, h->xv);
-    const float* vu[2] = {h->pvx, nullptr};
-    float* ou[2] = {h->acc[0], h->acc[1]};
-    ordered_splat(L, g, g.pdx, g.pdy, h->n_part, h->px, h->yu, nullptr, 2, vu, ou, h->sw);
-    const float* vv[2] = {h->pvy, nullptr};
-    float* ov[2] = {h->acc[2], h->acc[3]};
-    ordered_splat(L, g, g.pdx, g.pdy, h->n_part, h->xv, h->py, nullptr, 2, vv, ov, h->sw);
-    p2g_finish(L, g, h->acc[0], h->acc[1], h->acc[2], h->acc[3], UB(h), VB(h));
-    h->front ^= 1;
-}
-
-void ph_save_prev(fs_handle* h) { grid_copy2(h->L(), h->g, UF(h), VF(h), h->u_prev, h->v_prev); }
-void ph_save_diff(fs_handle* h) { grid_diff(h->L(), h->g, UF(h), VF(h), h->u_prev, h->v_prev, h->u_diff, h->v_diff); }
-
-void ph_gravity(fs_handle* h, float dt)
-{
-    const float ax = h->gx * dt, ay = h->gy * dt;  // a * dt in float, as FluidSolver.cpp:289-291
-    gravity(h->L(), h->g, h->labels, UF(h), VF(h), ax, ay);
-}
-
-void ph_dirichlet(fs_handle* h) { dirichlet(h->L(), h->g, h->labels, UF(h), VF(h)); }
-
-void ph_extend(fs_handle* h)
-{
-    const Launch L = h->L();
-    extend_init(L, h->g, h->labels, UF(h), VF(h), UB(h), VB(h), h->vmx[h->vfront], h->vmx[1 - h->vfront],
-                h->vmy[h->vfront], h->vmy[1 - h->vfront]);
-    for (int it = 0; it < h->n_ext; ++it) {
-        extend_sweep(L, h->g, h->labels, UB(h), VB(h), h->vmx[h->vfront], h->vmx[1 - h->vfront], h->vmy[h->vfront],
-                     h->vmy[1 - h->vfront]);
-        h->vfront ^= 1;
+    StepState st{};
+    st.d = domain(h);
+    st.front = &h->front;
+    st.vfront = &h->vfront;
+    for (int b = 0; b < 2; ++b) {
+        st.u[b] = h->u[b];
+        st.v[b] = h->v[b];
+        st.vmx[b] = h->vmx[b];
+        st.vmy[b] = h->vmy[b];
+        st.sl_ok[b] = h->sl_ok[b];
     }
-    h->front ^= 1;
+    st.u_prev = h->u_prev;
+    st.v_prev = h->v_prev;
+    st.u_diff = h->u_diff;
+    st.v_diff = h->v_diff;
+    st.labels = h->labels;
+    st.solid = h->solid;
+    st.fidx = h->fidx;
+    st.cell_of = h->cell_of;
+    st.counts32 = h->counts32;
+    st.counts8 = h->counts8;
+    for (int k = 0; k < 4; ++k) st.acc[k] = h->acc[k];
+    for (int k = 0; k < 6; ++k) st.sl[k] = h->sl[k];
+    st.px = h->px;
+    st.py = h->py;
+    st.pvx = h->pvx;
+    st.pvy = h->pvy;
+    st.yu = h->yu;
+    st.xv = h->xv;
+    st.sw = &h->sw;
+    st.cg_b = h->cg_b;
+    st.cg_down = h->cg_down;
+    st.cg_up = h->cg_up;
+    st.cg_flags = h->cg_flags;
+    st.cg_x = h->cg.x;
+    st.nfluid = h->d_nfluid;
+    st.warn = h->d_warn;
+    st.index_tmp = h->scan_tmp;
+    st.n_ext = h->n_ext;
+    st.solve = solve_hook;
+    st.mark = mark_hook;
+    st.owner = h;
+    return st;
 }
 
-void ph_pressure(fs_handle* h, float dt)
+void run_step(fs_handle* h, int method, float dt)
 {
-    const Launch L = h->L();
-    const Geom& g = h->g;
-    count_particles(L, g, h->px, h->py, h->n_part, h->counts32, h->d_warn);
-    fluid_index(L, h->labels, h->ncell, h->fidx, h->cell_of, h->d_nfluid, h->scan_tmp);
-    assemble(L, g, h->labels, h->fidx, h->cell_of, h->d_nfluid, UF(h), VF(h), h->cg_b, h->cg_down, h->cg_up,
-             h->cg_flags, h->counts32, h->counts8);
-    mark(h, FS_T_CG);
-    cg_solve(L, h->cg, h->d_nfluid, h->cg_b, h->diag_tab, h->cg_down, h->cg_up, h->cg_flags, h->off, h->cg_tol,
-             h->cg_maxit, h->cg_fp64, h->d_status);
-    mark(h, FS_T_PROJECT);
-    const float dt_over_rho = dt / h->cfg.density;  // FluidSolver.cpp:471-474: (dt / density) first
-    project(L, g, h->fidx, h->d_nfluid, h->cg.x, UF(h), VF(h), UB(h), VB(h), dt_over_rho);
-    h->front ^= 1;
-}
-
-void ph_g2p(fs_handle* h, int g2p, int adv, float dt)
-{
-    g2p_advect(h->L(), h->g, g2p, adv, h->px, h->py, h->pvx, h->pvy, h->n_part, UF(h), VF(h), h->u_diff, h->v_diff,
-               h->labels, h->pic, dt);
-}
-
-void ph_sl_velocity(fs_handle* h, float dt)
-{
-    const Launch L = h->L();
-    const Geom& g = h->g;
-    sl_faces(L, g, h->labels, UF(h), VF(h), dt, h->sl[0], h->sl[1], h->sl[2], h->sl_ok[0], h->sl[3], h->sl[4],
-             h->sl[5], h->sl_ok[1]);
-    const float* vu[1] = {h->sl[2]};
-    float* ou[1] = {UB(h)};
-    ordered_splat(L, g, g.dx, g.dy, h->ncell, h->sl[0], h->sl[1], h->sl_ok[0], 1, vu, ou, h->sw);
-    const float* vv[1] = {h->sl[5]};
-    float* ov[1] = {VB(h)};
-    ordered_splat(L, g, g.dx, g.dy, h->ncell, h->sl[3], h->sl[4], h->sl_ok[1], 1, vv, ov, h->sw);
-}
-
-void enqueue_phase(fs_handle* h, int ph, float dt)
-{
-    switch (ph) {
-        case FS_PH_CLASSIFY: ph_classify(h); break;
-        case FS_PH_P2G: ph_p2g(h); break;
-        case FS_PH_SAVE_PREV: ph_save_prev(h); break;
-        case FS_PH_GRAVITY: ph_gravity(h, dt); break;
-        case FS_PH_DIRICHLET: ph_dirichlet(h); break;
-        case FS_PH_EXTEND: ph_extend(h); break;
-        case FS_PH_PRESSURE: ph_pressure(h, dt); break;
-        case FS_PH_SAVE_DIFF: ph_save_diff(h); break;
-        case FS_PH_G2P_PICFLIP: ph_g2p(h, G2P_PICFLIP, ADV_NONE, dt); break;
-        case FS_PH_G2P_PIC: ph_g2p(h, G2P_PIC, ADV_NONE, dt); break;
-        case FS_PH_G2P_FLIP: ph_g2p(h, G2P_FLIP, ADV_NONE, dt); break;
-        case FS_PH_ADVECT_SAFE: ph_g2p(h, G2P_NONE, ADV_SAFE, dt); break;
-        case FS_PH_ADVECT: ph_g2p(h, G2P_NONE, ADV_PLAIN, dt); break;
-        case FS_PH_SL_VELOCITY: ph_sl_velocity(h, dt); break;
-        case FS_PH_SL_PARTICLES: ph_g2p(h, G2P_NONE, ADV_RK3, dt); break;
-        case FS_PH_SWAP: h->front ^= 1; break;
-        default: break;
-    }
-}
-
-// FluidSolver::step* (src/FluidSolver.cpp:99-251) as one queued sequence; the
-// grid-to-particle transfer and the particle advection share one kernel.
-void enqueue_step(fs_handle* h, int method, float dt)
-{
-    mark(h, FS_T_CLASSIFY);
-    ph_classify(h);
-    mark(h, FS_T_P2G);
-    if (method == FS_STEP_SEMI_LAGRANGIAN) {
-        mark(h, FS_T_FORCES);
-        ph_sl_velocity(h, dt);
-        ph_gravity(h, dt);
-        ph_dirichlet(h);
-    } else {
-        ph_p2g(h);
-        if (method != FS_STEP_PIC) ph_save_prev(h);
-        mark(h, FS_T_FORCES);
-        ph_gravity(h, dt);
-        ph_dirichlet(h);
-        ph_extend(h);
-    }
-    mark(h, FS_T_ASSEMBLY);
-    ph_pressure(h, dt);
-    ph_dirichlet(h);
-    if (method == FS_STEP_FLIP || method == FS_STEP_PICFLIP) ph_save_diff(h);
-    mark(h, FS_T_G2P);
-    switch (method) {
-        case FS_STEP_SEMI_LAGRANGIAN: ph_g2p(h, G2P_NONE, ADV_RK3, dt); break;
-        case FS_STEP_PIC: ph_g2p(h, G2P_PIC, ADV_PLAIN, dt); break;
-        case FS_STEP_FLIP: ph_g2p(h, G2P_FLIP, ADV_PLAIN, dt); break;
-        default: ph_g2p(h, G2P_PICFLIP, ADV_SAFE, dt); break;
-    }
-    mark(h, FS_NUM_TIMED);
+    StepState st = state(h);
+    enqueue_step(h->L(), st, method, dt);
 }
 
 int check_launch(fs_handle* h, const char* what)
@@ -606,7 +539,7 @@ int fs_create(const fs_config* cfg, fs_handle** out)
         A(cudaMemsetAsync(h->cg.result, 0, sizeof(CgResult), h->stream));
         A(cudaMemsetAsync(h->cg.partials, 0, sizeof(double) * 8 * (size_t)max_chunks, h->stream));
         A(cudaMemsetAsync(h->cg.barrier, 0, sizeof(unsigned), h->stream));
-        labels_clear(h->L(), h->g, h->labels);  // MacGrid ctor -> clearCellTypeBuffer (src/MacGrid.cpp:24)
+        labels_clear(h->L(), domain(h), h->labels);  // MacGrid ctor -> clearCellTypeBuffer (src/MacGrid.cpp:24)
         A(cudaGetLastError());
         A(cudaStreamSynchronize(h->stream));
     }
@@ -818,7 +751,7 @@ int fs_get_pressure(fs_handle* h, float* out)
 {
     if (!h) return FS_ERR_INVALID_ARGUMENT;
     cudaSetDevice(h->device);
-    pressure_to_grid(h->L(), h->g, h->fidx, h->d_nfluid, h->cg.x, h->grid_tmp);
+    pressure_to_grid(h->L(), domain(h), h->fidx, h->d_nfluid, h->cg.x, h->grid_tmp);
     const int rc = check_launch(h, "pressure");
     if (rc) return rc;
     return copy_out(h, out, h->grid_tmp, (size_t)h->ncell);
@@ -833,10 +766,9 @@ int fs_phase(fs_handle* h, int ph, float dt)
         cudaError_t e = ensure_sl_scratch(h);
         if (e != cudaSuccess) return cuda_fail(h, e, "semi-Lagrangian scratch");
     }
-    const bool t = h->timing;
-    h->timing = false;
-    enqueue_phase(h, ph, dt);
-    h->timing = t;
+    StepState st = state(h);
+    st.mark = nullptr;
+    enqueue_phase(h->L(), st, ph, dt);
     return check_launch(h, "phase");
 }
 
@@ -853,7 +785,7 @@ int fs_step(fs_handle* h, int method, float dt)
     }
     h->timed_valid = h->timing;
     if (!h->graphs || h->timing) {  // per-phase events are recorded by direct launches
-        enqueue_step(h, method, dt);
+        run_step(h, method, dt);
         return check_launch(h, "step");
     }
     const uint32_t db = float_bits(dt);
@@ -879,7 +811,7 @@ int fs_step(fs_handle* h, int method, float dt)
     cudaGraph_t graph = nullptr;
     cudaError_t e = cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) return cuda_fail(h, e, "begin capture");
-    enqueue_step(h, method, dt);
+    run_step(h, method, dt);
     cudaError_t e_launch = cudaGetLastError();
     e = cudaStreamEndCapture(h->stream, &graph);
     ge.front_out = h->front;
@@ -893,7 +825,7 @@ int fs_step(fs_handle* h, int method, float dt)
         h->graphs = false;
         h->front = ge.front_in;
         h->vfront = ge.vfront_in;
-        enqueue_step(h, method, dt);
+        run_step(h, method, dt);
         return check_launch(h, "step");
     }
     e = cudaGraphInstantiate(&ge.exec, graph, 0);
@@ -903,7 +835,7 @@ int fs_step(fs_handle* h, int method, float dt)
         h->graphs = false;
         h->front = ge.front_in;
         h->vfront = ge.vfront_in;
-        enqueue_step(h, method, dt);
+        run_step(h, method, dt);
         return check_launch(h, "step");
     }
     h->graph_cache.push_back(ge);

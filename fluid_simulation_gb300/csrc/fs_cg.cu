@@ -145,6 +145,41 @@ __device__ __forceinline__ bool cta_barrier(const CgArgs& a, bool grid, unsigned
     return !grid || sm.flag != 0;
 }
 
+// The CTAs that share one solve: every CTA of the cooperative grid (or the
+// first CTA alone, for small systems) ...
+struct GridSync
+{
+    bool grid;
+    unsigned target;
+    __device__ int rank() const { return grid ? (int)blockIdx.x : 0; }
+    __device__ int size() const { return grid ? (int)gridDim.x : 1; }
+    __device__ bool barrier(const CgArgs& a, Smem& sm) { return cta_barrier(a, grid, target, sm); }
+};
+
+// ... or the CTAs of one thread-block cluster, which the hardware schedules
+// together; its barrier releases and acquires at cluster scope, which covers
+// the global-memory partials and published z, p that the CTAs exchange.
+struct ClusterSync
+{
+    __device__ int rank() const
+    {
+        unsigned r;
+        asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+        return (int)r;
+    }
+    __device__ int size() const
+    {
+        unsigned n;
+        asm volatile("mov.u32 %0, %%cluster_nctarank;" : "=r"(n));
+        return (int)n;
+    }
+    __device__ bool barrier(const CgArgs&, Smem&)
+    {
+        asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+        return true;
+    }
+};
+
 // Level-1 (warp) tree of NV values for chunk slot `slot`; lane 0 keeps it.
 template <typename R, int NV>
 __device__ __forceinline__ void level1(const R (&v)[NV], int slot, Smem& sm)
@@ -258,18 +293,17 @@ __device__ __forceinline__ Resident resident(unsigned char* dyn, int K)
 
 // One CG solve.  K > 0: the CTA's cells (at most K chunks) live in shared
 // memory; K == 0: the state streams from global memory.
-template <int K, typename R>
-__device__ void cg_body(const CgArgs& a, Smem& sm, unsigned char* dyn, int nf, int nchunks, bool grid)
+template <int K, typename R, class Sync>
+__device__ __forceinline__ void cg_body(const CgArgs& a, Smem& sm, unsigned char* dyn, int nf, int nchunks, Sync& sync)
 {
     const int tid = threadIdx.x;
-    const int ncta = grid ? (int)gridDim.x : 1;
-    const int cta = grid ? (int)blockIdx.x : 0;
+    const int ncta = sync.size();
+    const int cta = sync.rank();
     const int c0 = (int)(((int64_t)cta * nchunks) / ncta);
     const int c1 = (int)(((int64_t)(cta + 1) * nchunks) / ncta);
     const int kb = c1 - c0;                // chunks owned
     const int e0 = c0 * CHUNK;             // owned element range [e0, e1)
     const int e1 = min(c1 * CHUNK, nf);
-    unsigned target = 0;
     const Resident RS = resident(dyn, K > 0 ? K : 1);
     const float* dtab = sm.dtab;
     const float* itab = sm.itab;
@@ -306,7 +340,7 @@ __device__ void cg_body(const CgArgs& a, Smem& sm, unsigned char* dyn, int nf, i
         }
         level2<R, 2>(a, 0, c0 + base, nslot, sm);
     }
-    if (!cta_barrier(a, grid, target, sm)) return;
+    if (!sync.barrier(a, sm)) return;
     R red2[2];
     reduce_all<R, 2>(a, 0, nchunks, sm, red2);
     const R bb = red2[0];
@@ -370,7 +404,7 @@ __device__ void cg_body(const CgArgs& a, Smem& sm, unsigned char* dyn, int nf, i
             }
             level2<R, 1>(a, 1, c0 + base, nslot, sm);
         }
-        if (!cta_barrier(a, grid, target, sm)) return;
+        if (!sync.barrier(a, sm)) return;
         R red1[1];
         reduce_all<R, 1>(a, 1, nchunks, sm, red1);
         const float alpha = Ar<R>::ratio(rz, red1[0]);
@@ -419,7 +453,7 @@ __device__ void cg_body(const CgArgs& a, Smem& sm, unsigned char* dyn, int nf, i
             }
             level2<R, 2>(a, 0, c0 + base, nslot, sm);
         }
-        if (!cta_barrier(a, grid, target, sm)) return;
+        if (!sync.barrier(a, sm)) return;
         reduce_all<R, 2>(a, 0, nchunks, sm, red2);
         rr = red2[0];
         iters = it;
@@ -471,13 +505,67 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(CgArgs a)
     if (!grid && blockIdx.x != 0) return;
     const int per_cta = grid ? (nchunks + gridDim.x - 1) / gridDim.x : nchunks;
     const bool resident = per_cta <= KREG;
+    GridSync sync{grid, 0u};
     if (a.fp64) {
-        if (resident) cg_body<KREG, double>(a, sm, dyn, nf, nchunks, grid);
-        else cg_body<0, double>(a, sm, dyn, nf, nchunks, grid);
+        if (resident) cg_body<KREG, double>(a, sm, dyn, nf, nchunks, sync);
+        else cg_body<0, double>(a, sm, dyn, nf, nchunks, sync);
     } else {
-        if (resident) cg_body<KREG, float>(a, sm, dyn, nf, nchunks, grid);
-        else cg_body<0, float>(a, sm, dyn, nf, nchunks, grid);
+        if (resident) cg_body<KREG, float>(a, sm, dyn, nf, nchunks, sync);
+        else cg_body<0, float>(a, sm, dyn, nf, nchunks, sync);
     }
+}
+
+// A batch of independent systems: one thread-block cluster per system (the
+// simulation order[cluster]); K chunks per CTA in shared memory.  The
+// reduction tree, and so every result, is that of k_cg.
+template <int K>
+__global__ void __launch_bounds__(CG_THREADS, 1) k_cg_cluster(CgBatchArgs ba)
+{
+    __shared__ Smem sm;
+    extern __shared__ __align__(16) unsigned char dyn[];
+    unsigned cluster;
+    asm volatile("mov.u32 %0, %%clusterid.x;" : "=r"(cluster));
+    const int sim = ba.order[cluster];
+    const CgSystem& sy = ba.systems[sim];
+    CgArgs a;
+    a.nfluid = ba.nfluid + sim;
+    a.b = ba.b + sy.co;
+    a.down = ba.down + sy.co;
+    a.up = ba.up + sy.co;
+    a.flags = ba.flags + sy.co;
+    a.off = sy.off;  // the diagonal tables go straight to shared memory below
+    a.tol = sy.tol;
+    a.maxit = sy.maxit;
+    a.fp64 = ba.fp64;
+    a.x = ba.x + sy.co;
+    a.r = ba.r + sy.co;
+    a.z = ba.z + sy.co;
+    a.p = ba.p + sy.co;
+    a.q = ba.q + sy.co;
+    a.partials = ba.partials + sy.part_off;
+    a.max_chunks = sy.max_chunks;
+    a.barrier = nullptr;
+    a.status = ba.status;
+    a.result = ba.result + sim;
+    if (threadIdx.x < 5) {
+        sm.dtab[threadIdx.x] = sy.dtab[threadIdx.x];
+        sm.itab[threadIdx.x] = sy.itab[threadIdx.x];
+    }
+    __syncthreads();
+    ClusterSync sync;
+    const int nf = *a.nfluid;
+    const int nchunks = (nf + CHUNK - 1) / CHUNK;
+    // Every CTA of the cluster takes the same branch: the system is shared.
+    if (nchunks == 0) {
+        if (sync.rank() == 0 && threadIdx.x == 0) *a.result = CgResult{0, 0, 0.0, 0.0};
+        return;
+    }
+    if (nchunks > a.max_chunks || nchunks > K * sync.size()) {
+        if (sync.rank() == 0 && threadIdx.x == 0) atomicOr(a.status, ST_TOO_LARGE);
+        return;
+    }
+    if (a.fp64) cg_body<K, double>(a, sm, dyn, nf, nchunks, sync);
+    else cg_body<K, float>(a, sm, dyn, nf, nchunks, sync);
 }
 
 }  // namespace
@@ -527,6 +615,71 @@ void cg_solve(const Launch& L, CgWork& w, const int32_t* nfluid, const float* b,
     void* args[] = {&a};
     cudaLaunchCooperativeKernel((const void*)k_cg, dim3(w.grid), dim3(CG_THREADS), args, RESIDENT_BYTES, L.stream);
     L.count();
+}
+
+namespace {
+
+template <int K>
+int prepare_cluster_kernel(int cluster)
+{
+    const size_t bytes = (size_t)K * CHUNK * 25;
+    if (cudaFuncSetAttribute(k_cg_cluster<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) != cudaSuccess)
+        return -1;
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = cluster;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.gridDim = dim3(cluster);
+    cfg.blockDim = dim3(CG_THREADS);
+    cfg.dynamicSmemBytes = bytes;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    int n = 0;
+    if (cudaOccupancyMaxActiveClusters(&n, k_cg_cluster<K>, &cfg) != cudaSuccess) return -1;
+    return n;
+}
+
+template <int K>
+cudaError_t launch_cluster(const Launch& L, const CgBatchArgs& ba, int nsys, int cluster)
+{
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = cluster;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.gridDim = dim3((unsigned)(nsys * cluster));
+    cfg.blockDim = dim3(CG_THREADS);
+    cfg.dynamicSmemBytes = (size_t)K * CHUNK * 25;
+    cfg.stream = L.stream;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    const cudaError_t e = cudaLaunchKernelEx(&cfg, k_cg_cluster<K>, ba);
+    L.count();
+    return e;
+}
+
+}  // namespace
+
+int cg_cluster_capacity(int chunks_per_cta, int cluster)
+{
+    switch (chunks_per_cta) {
+        case 4: return prepare_cluster_kernel<4>(cluster);
+        case 8: return prepare_cluster_kernel<8>(cluster);
+        default: return -1;
+    }
+}
+
+cudaError_t cg_solve_clusters(const Launch& L, const CgBatchArgs& ba, int nsys, int chunks_per_cta, int cluster)
+{
+    if (nsys <= 0) return cudaSuccess;
+    switch (chunks_per_cta) {
+        case 4: return launch_cluster<4>(L, ba, nsys, cluster);
+        case 8: return launch_cluster<8>(L, ba, nsys, cluster);
+        default: return cudaErrorInvalidValue;
+    }
 }
 
 }  // namespace fs

@@ -23,6 +23,49 @@ struct Launch
     }
 };
 
+// ---- launch domains (fs_domain.cuh) ---------------------------------------
+constexpr int DOMAIN_TPB = 256;
+
+// One simulation's slice of the flattened arrays (offsets 0 for a lone simulation).
+struct Seg
+{
+    Geom g;
+    int64_t co;   // first cell in the flattened cell arrays (a multiple of DOMAIN_TPB)
+    int64_t po;   // first particle in the flattened particle arrays (a multiple of DOMAIN_TPB)
+    int64_t np;   // particles
+    float pic;    // FluidDomain::picRatio
+    float rho;    // FluidDomain::density
+    float gx, gy; // gravitational acceleration
+    int sim;      // index of the simulation (0 for a lone one)
+    int cb0;      // first cell block of the simulation (batch only)
+    int ncb;      // its cell blocks (batch only)
+};
+
+// The simulations a kernel runs over: `one` when segs == nullptr, else every
+// simulation of a batch through its block tables (blk[b] = {simulation, first
+// local item of block b}, DOMAIN_TPB items per block).
+struct Domain
+{
+    Seg one{};
+    const Seg* segs = nullptr;
+    const int2* cblk = nullptr;
+    unsigned ncblk = 0;
+    const int2* pblk = nullptr;
+    unsigned npblk = 0;
+    int nsim = 1;
+    int64_t cells = 0;  // flattened cells
+    int64_t parts = 0;  // flattened particles
+
+    static Domain single(const Seg& s)
+    {
+        Domain d;
+        d.one = s;
+        d.cells = (int64_t)s.g.nx * s.g.ny;
+        d.parts = s.np;
+        return d;
+    }
+};
+
 // ---- scan (fs_scan.cu) ----------------------------------------------------
 // Exclusive prefix sum of n int32 values into out[0..n]; out[n] = total.
 // tmp must hold scan_tmp_ints(n) ints.
@@ -32,6 +75,11 @@ void scan_exclusive_i32(const Launch& L, const int32_t* in, int32_t* out, int64_
 // cells in j-major order or -1; cell_of[k] = c; *nfluid = count.
 void fluid_index(const Launch& L, const uint8_t* labels, int64_t n, int32_t* fidx, int32_t* cell_of,
                  int32_t* nfluid, int32_t* tmp);
+// The same per simulation of a batch: local fluid indices, cell_of[co + k] =
+// local cell, nfluid[sim].  tmp must hold 2 * (d.ncblk + 1) + scan_tmp_ints(d.ncblk + 1) ints.
+size_t fluid_index_batch_tmp_ints(const Domain& d);
+void fluid_index_batch(const Launch& L, const Domain& d, const uint8_t* labels, int32_t* fidx, int32_t* cell_of,
+                       int32_t* nfluid, int32_t* tmp);
 
 // ---- stable radix sort + ordered splat (fs_splat.cu) ---------------------
 struct SplatWork
@@ -46,41 +94,45 @@ struct SplatWork
     int64_t cap_items;
 };
 size_t splat_hist_ints(int64_t n_items);
-// Accumulates, for each node of a size nx*ny grid, sum over items k in
-// increasing k of the bilinear splat (Grid::addToValueInterpolated,
-// include/Grid.h:152-184) of value[c][k] at (x[k], y[k]) for channel c, exactly
-// as a sequential loop over k would (float adds in item order, corner order
-// 00, 10, 01, 11).  Items with valid[k] == 0 (or valid == nullptr: all valid)
-// contribute nothing.  out[c] are overwritten (start from +0).
-void ordered_splat(const Launch& L, const Geom& g, float gdx, float gdy, int64_t n_items, const float* x,
+// Accumulates, for each node of every simulation of d, sum over that
+// simulation's items k in increasing k of the bilinear splat
+// (Grid::addToValueInterpolated, include/Grid.h:152-184) of value[c][k] at
+// (x[k], y[k]) for channel c, exactly as a sequential loop over k would (float
+// adds in item order, corner order 00, 10, 01, 11).  Items are the particles
+// (items_are_cells false) or the cells of d, in the flattened layout; items
+// with valid[k] == 0 (or valid == nullptr: all valid) contribute nothing.
+// pool_deltas selects the solver pool's deltas (pdx, pdy) instead of (dx, dy).
+// out[c] are overwritten (start from +0).
+void ordered_splat(const Launch& L, const Domain& d, bool items_are_cells, bool pool_deltas, const float* x,
                    const float* y, const uint8_t* valid, int channels, const float* const* values,
                    float* const* out, SplatWork& w);
 
 // ---- grid kernels (fs_grid.cu) -------------------------------------------
-void labels_clear(const Launch& L, const Geom& g, uint8_t* lab);
-void labels_from_particles(const Launch& L, const Geom& g, const float* px, const float* py, int64_t n,
-                           uint8_t* lab);
-void labels_finalize(const Launch& L, const Geom& g, uint8_t* lab, const uint8_t* solid);
-void count_particles(const Launch& L, const Geom& g, const float* px, const float* py, int64_t n,
-                     int32_t* counts32, unsigned* warn);
-void p2g_finish(const Launch& L, const Geom& g, const float* sum_u, const float* w_u, const float* sum_v,
+// Cell arrays are flattened (simulation s at d's cell offset co); particle
+// arrays likewise at po.  Per-simulation scalars come from the Seg.
+void labels_clear(const Launch& L, const Domain& d, uint8_t* lab);
+void labels_from_particles(const Launch& L, const Domain& d, const float* px, const float* py, uint8_t* lab);
+void labels_finalize(const Launch& L, const Domain& d, uint8_t* lab, const uint8_t* solid);
+void count_particles(const Launch& L, const Domain& d, const float* px, const float* py, int32_t* counts32,
+                     unsigned* warn);
+void p2g_finish(const Launch& L, const Domain& d, const float* sum_u, const float* w_u, const float* sum_v,
                 const float* w_v, float* ub, float* vb);
-void grid_copy2(const Launch& L, const Geom& g, const float* a0, const float* a1, float* b0, float* b1);
-void grid_diff(const Launch& L, const Geom& g, const float* uf, const float* vf, const float* up,
+void grid_copy2(const Launch& L, const Domain& d, const float* a0, const float* a1, float* b0, float* b1);
+void grid_diff(const Launch& L, const Domain& d, const float* uf, const float* vf, const float* up,
                const float* vp, float* ud, float* vd);
-void gravity(const Launch& L, const Geom& g, const uint8_t* lab, float* uf, float* vf, float ax_dt,
-             float ay_dt);
-void dirichlet(const Launch& L, const Geom& g, const uint8_t* lab, float* uf, float* vf);
-void extend_init(const Launch& L, const Geom& g, const uint8_t* lab, float* uf, float* vf, float* ub, float* vb,
+void gravity(const Launch& L, const Domain& d, const uint8_t* lab, float* uf, float* vf, float dt);
+void dirichlet(const Launch& L, const Domain& d, const uint8_t* lab, float* uf, float* vf);
+void extend_init(const Launch& L, const Domain& d, const uint8_t* lab, float* uf, float* vf, float* ub, float* vb,
                  uint8_t* mxf, uint8_t* mxb, uint8_t* myf, uint8_t* myb);
-void extend_sweep(const Launch& L, const Geom& g, const uint8_t* lab, float* ub, float* vb, const uint8_t* mxf,
+void extend_sweep(const Launch& L, const Domain& d, const uint8_t* lab, float* ub, float* vb, const uint8_t* mxf,
                   uint8_t* mxb, const uint8_t* myf, uint8_t* myb);
-void assemble(const Launch& L, const Geom& g, const uint8_t* lab, const int32_t* fidx, const int32_t* cell_of,
+// nfluid[sim]; fluid-index vectors of simulation s start at its cell offset co.
+void assemble(const Launch& L, const Domain& d, const uint8_t* lab, const int32_t* fidx, const int32_t* cell_of,
               const int32_t* nfluid, const float* uf, const float* vf, float* b, int32_t* down, int32_t* up,
               uint8_t* flags, const int32_t* counts32, uint8_t* counts8);
-void project(const Launch& L, const Geom& g, const int32_t* fidx, const int32_t* nfluid, const float* x,
-             float* uf, float* vf, float* ub, float* vb, float dt_over_rho);
-void pressure_to_grid(const Launch& L, const Geom& g, const int32_t* fidx, const int32_t* nfluid,
+void project(const Launch& L, const Domain& d, const int32_t* fidx, const int32_t* nfluid, const float* x,
+             float* uf, float* vf, float* ub, float* vb, float dt);
+void pressure_to_grid(const Launch& L, const Domain& d, const int32_t* fidx, const int32_t* nfluid,
                       const float* x, float* out);
 
 // ---- particle kernels (fs_particles.cu) ----------------------------------
@@ -98,12 +150,11 @@ enum AdvectMode
     ADV_PLAIN = 2,
     ADV_RK3 = 3
 };
-void g2p_advect(const Launch& L, const Geom& g, int g2p_mode, int adv_mode, float* px, float* py, float* pvx,
-                float* pvy, int64_t n, const float* uf, const float* vf, const float* ud, const float* vd,
-                const uint8_t* lab, float pic_ratio, float dt);
-void p2g_positions(const Launch& L, const Geom& g, const float* px, const float* py, int64_t n, float* yu,
-                   float* xv);
-void sl_faces(const Launch& L, const Geom& g, const uint8_t* lab, const float* uf, const float* vf, float dt,
+void g2p_advect(const Launch& L, const Domain& d, int g2p_mode, int adv_mode, float* px, float* py, float* pvx,
+                float* pvy, const float* uf, const float* vf, const float* ud, const float* vd, const uint8_t* lab,
+                float dt);
+void p2g_positions(const Launch& L, const Domain& d, const float* px, const float* py, float* yu, float* xv);
+void sl_faces(const Launch& L, const Domain& d, const uint8_t* lab, const float* uf, const float* vf, float dt,
               float* ux, float* uy, float* uval, uint8_t* uok, float* vx, float* vy, float* vval, uint8_t* vok);
 void aos_to_soa(const Launch& L, const float* xyuv, int64_t n, float* px, float* py, float* pvx, float* pvy);
 void soa_to_aos(const Launch& L, const float* px, const float* py, const float* pvx, const float* pvy, int64_t n,
@@ -131,5 +182,40 @@ int cg_prepare(CgWork& w, int device);  // picks the cooperative grid size
 void cg_solve(const Launch& L, CgWork& w, const int32_t* nfluid, const float* b, const float* diag_tab,
               const int32_t* down, const int32_t* up, const uint8_t* flags, float off, double tol, int maxit,
               int fp64, unsigned* status);
+
+// One system of a batch of independent pressure solves (a simulation of a batch).
+struct CgSystem
+{
+    int64_t co;        // its fluid-index vectors start at this offset (the simulation's cell offset)
+    int64_t part_off;  // its chunk partials start here (doubles)
+    int max_chunks;    // chunk capacity of its partial buffers
+    float dtab[5];     // diagonal by non-solid count
+    float itab[5];     // 1 / diagonal, or 1 where the diagonal is 0
+    float off;         // off-diagonal coefficient
+    double tol;
+    int maxit;
+};
+struct CgBatchArgs
+{
+    const CgSystem* systems;  // [simulation]
+    const int32_t* order;     // simulation of each cluster of the launch
+    const int32_t* nfluid;    // [simulation]
+    const float* b;
+    const int32_t* down;
+    const int32_t* up;
+    const uint8_t* flags;
+    float *x, *r, *z, *p, *q;
+    double* partials;
+    unsigned* status;
+    CgResult* result;  // [simulation]
+    int fp64;
+};
+// Co-resident clusters of `cluster` CTAs with chunks_per_cta (4 or 8)
+// chunks of shared-memory state each (also sets the kernel's shared-memory
+// attribute); < 1 if that shape cannot run.
+int cg_cluster_capacity(int chunks_per_cta, int cluster);
+// Solves systems order[0..nsys) of ba, one cluster each; each must have at
+// most chunks_per_cta * cluster chunks of 1024 fluid cells.
+cudaError_t cg_solve_clusters(const Launch& L, const CgBatchArgs& ba, int nsys, int chunks_per_cta, int cluster);
 
 }  // namespace fs

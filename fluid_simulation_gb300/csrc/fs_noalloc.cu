@@ -164,10 +164,13 @@ extern "C" FS_API int fs_pressure_solve_noalloc(int size_x, int size_y, float le
     cudaMemsetAsync(counts32, 0, sizeof(int32_t) * (size_t)ncell, L.stream);
     cudaMemsetAsync(status, 0, sizeof(unsigned), L.stream);
     fluid_index(L, labels, ncell, fidx, cell_of, nfluid, scan_tmp);
-    assemble(L, g, labels, fidx, cell_of, nfluid, u, v, b, down, up, flags, counts32, counts8);
+    Seg sg{};
+    sg.g = g;
+    const Domain d = Domain::single(sg);
+    assemble(L, d, labels, fidx, cell_of, nfluid, u, v, b, down, up, flags, counts32, counts8);
     cg_solve(L, w, nfluid, b, diag_tab, down, up, flags, off, cg_tolerance, cg_max_iterations,
              cg_precision == FS_CG_DOUBLE ? 1 : 0, status);
-    pressure_to_grid(L, g, fidx, nfluid, w.x, pressure);
+    pressure_to_grid(L, d, fidx, nfluid, w.x, pressure);
     e = cudaGetLastError();
     if (e != cudaSuccess) return fail(FS_ERR_CUDA, std::string("launch: ") + cudaGetErrorString(e));
     if (cg_iterations || cg_residual) {

@@ -1,7 +1,7 @@
 // Per-particle kernels: grid-to-particle transfers, particle advection, the
 // semi-Lagrangian back-trace of faces, and layout conversion.  Particles are
 // stored as four SoA float arrays (x, y, vx, vy) in the caller's order.
-#include "fs_internal.h"
+#include "fs_domain.cuh"
 
 namespace fs {
 namespace {
@@ -12,105 +12,124 @@ constexpr int TPB = 256;
 // followed by MarkerParticleSet::advectAndEnsureOutsideObstacles
 // (src/MarkerParticleSet.cpp:48-62), ::advect (:40-46) or
 // FluidSolver::advectParticlesWithGrid (src/FluidSolver.cpp:774-791).
-__global__ void k_g2p_advect(Geom g, int g2p, int adv, float* __restrict__ px, float* __restrict__ py,
-                             float* __restrict__ pvx, float* __restrict__ pvy, int64_t n,
-                             const float* __restrict__ uf, const float* __restrict__ vf,
-                             const float* __restrict__ ud, const float* __restrict__ vd,
-                             const uint8_t* __restrict__ lab, float r, float dt)
+struct G2PAdvect
 {
-    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n) return;
-    float x = px[k], y = py[k], vx = pvx[k], vy = pvy[k];
-    if (g2p == G2P_PICFLIP) {
-        const float pic_x = vel_x_interp(uf, g, x, y);
-        const float pic_y = vel_y_interp(vf, g, x, y);
-        const float flip_x = fadd(vx, vel_x_interp(ud, g, x, y));
-        const float flip_y = fadd(vy, vel_y_interp(vd, g, x, y));
-        const float omr = fsub(1.0f, r);
-        vx = fadd(fmul(pic_x, r), fmul(flip_x, omr));
-        vy = fadd(fmul(pic_y, r), fmul(flip_y, omr));
-    } else if (g2p == G2P_PIC) {
-        vx = vel_x_interp(uf, g, x, y);
-        vy = vel_y_interp(vf, g, x, y);
-    } else if (g2p == G2P_FLIP) {
-        const float a = vel_x_interp(ud, g, x, y);
-        const float b = vel_y_interp(vd, g, x, y);
-        vx = fadd(vx, a);
-        vy = fadd(vy, b);
-    }
-    if (adv == ADV_SAFE || adv == ADV_PLAIN) {
-        x = fadd(x, fmul(vx, dt));
-        y = fadd(y, fmul(vy, dt));
-        if (adv == ADV_SAFE) {
-            const int ci = trunc_i(fdiv(x, g.dx));
-            const int cj = trunc_i(fdiv(y, g.dy));
-            if (cell_type(lab, g, ci, cj) == SOLID) {
-                const float mdt = -dt;
-                x = fadd(x, fmul(vx, mdt));
-                y = fadd(y, fmul(vy, mdt));
-            }
+    int g2p, adv;
+    float *px, *py, *pvx, *pvy;
+    const float *uf, *vf, *ud, *vd;
+    const uint8_t* lab;
+    float dt;
+    __device__ void operator()(const Seg& s, int64_t kl) const
+    {
+        const Geom& g = s.g;
+        const int64_t k = s.po + kl;
+        const float* U = uf + s.co;
+        const float* V = vf + s.co;
+        const float r = s.pic;
+        float x = px[k], y = py[k], vx = pvx[k], vy = pvy[k];
+        if (g2p == G2P_PICFLIP) {
+            const float pic_x = vel_x_interp(U, g, x, y);
+            const float pic_y = vel_y_interp(V, g, x, y);
+            const float flip_x = fadd(vx, vel_x_interp(ud + s.co, g, x, y));
+            const float flip_y = fadd(vy, vel_y_interp(vd + s.co, g, x, y));
+            const float omr = fsub(1.0f, r);
+            vx = fadd(fmul(pic_x, r), fmul(flip_x, omr));
+            vy = fadd(fmul(pic_y, r), fmul(flip_y, omr));
+        } else if (g2p == G2P_PIC) {
+            vx = vel_x_interp(U, g, x, y);
+            vy = vel_y_interp(V, g, x, y);
+        } else if (g2p == G2P_FLIP) {
+            const float a = vel_x_interp(ud + s.co, g, x, y);
+            const float b = vel_y_interp(vd + s.co, g, x, y);
+            vx = fadd(vx, a);
+            vy = fadd(vy, b);
         }
-    } else if (adv == ADV_RK3) {
-        float ox, oy;
-        advected_position(uf, vf, g, x, y, dt, &ox, &oy);
-        x = ox;
-        y = oy;
+        if (adv == ADV_SAFE || adv == ADV_PLAIN) {
+            x = fadd(x, fmul(vx, dt));
+            y = fadd(y, fmul(vy, dt));
+            if (adv == ADV_SAFE) {
+                const int ci = trunc_i(fdiv(x, g.dx));
+                const int cj = trunc_i(fdiv(y, g.dy));
+                if (cell_type(lab + s.co, g, ci, cj) == SOLID) {
+                    const float mdt = -dt;
+                    x = fadd(x, fmul(vx, mdt));
+                    y = fadd(y, fmul(vy, mdt));
+                }
+            }
+        } else if (adv == ADV_RK3) {
+            float ox, oy;
+            advected_position(U, V, g, x, y, dt, &ox, &oy);
+            x = ox;
+            y = oy;
+        }
+        px[k] = x;
+        py[k] = y;
+        pvx[k] = vx;
+        pvy[k] = vy;
     }
-    px[k] = x;
-    py[k] = y;
-    pvx[k] = vx;
-    pvy[k] = vy;
-}
+};
 
 // Splat positions of transferVelocityToGridSpread (src/FluidSolver.cpp:889-896):
 // u at (px, py - 0.5 dy), v at (px - 0.5 dx, py).
-__global__ void k_p2g_positions(Geom g, const float* __restrict__ px, const float* __restrict__ py, int64_t n,
-                                float* __restrict__ yu, float* __restrict__ xv)
+struct P2GPositions
 {
-    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n) return;
-    yu[k] = fsub(py[k], fmul(g.dy, 0.5f));
-    xv[k] = fsub(px[k], fmul(g.dx, 0.5f));
-}
+    const float *px, *py;
+    float *yu, *xv;
+    __device__ void operator()(const Seg& s, int64_t kl) const
+    {
+        const int64_t k = s.po + kl;
+        yu[k] = fsub(py[k], fmul(s.g.dy, 0.5f));
+        xv[k] = fsub(px[k], fmul(s.g.dx, 0.5f));
+    }
+};
 
 // advectVelocitySemiLagrangian's per-face work (src/FluidSolver.cpp:725-769):
 // for faces with a liquid neighbour, the RK3 back-traced splat position and
 // the velocity sampled at the face.
-__global__ void k_sl_faces(Geom g, const uint8_t* __restrict__ lab, const float* __restrict__ uf,
-                           const float* __restrict__ vf, float dt, float* __restrict__ ux, float* __restrict__ uy,
-                           float* __restrict__ uval, uint8_t* __restrict__ uok, float* __restrict__ vx,
-                           float* __restrict__ vy, float* __restrict__ vval, uint8_t* __restrict__ vok)
+struct SLFaces
 {
-    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= (int64_t)g.nx * g.ny) return;
-    const int i = (int)(c % g.nx), j = (int)(c / g.nx);
-    const bool liq = lab[c] == LIQUID;
-    const float mdt = -dt;
-    if (liq || cell_type(lab, g, i - 1, j) == LIQUID) {
-        const float x = fmul((float)i, g.dx);
-        const float y = fmul(fadd((float)j, 0.5f), g.dy);
-        float xp, yp;
-        advected_position(uf, vf, g, x, y, mdt, &xp, &yp);
-        uval[c] = vel_x_interp(uf, g, x, y);
-        ux[c] = xp;
-        uy[c] = fsub(yp, fmul(g.dy, 0.5f));
-        uok[c] = 1;
-    } else {
-        uok[c] = 0;
+    const uint8_t* lab;
+    const float *uf, *vf;
+    float dt;
+    float *ux, *uy, *uval;
+    uint8_t* uok;
+    float *vx, *vy, *vval;
+    uint8_t* vok;
+    __device__ void operator()(const Seg& s, int64_t cl, int i, int j) const
+    {
+        const Geom& g = s.g;
+        const uint8_t* L = lab + s.co;
+        const float* U = uf + s.co;
+        const float* V = vf + s.co;
+        const int64_t c = s.co + cl;
+        const bool liq = L[cl] == LIQUID;
+        const float mdt = -dt;
+        if (liq || cell_type(L, g, i - 1, j) == LIQUID) {
+            const float x = fmul((float)i, g.dx);
+            const float y = fmul(fadd((float)j, 0.5f), g.dy);
+            float xp, yp;
+            advected_position(U, V, g, x, y, mdt, &xp, &yp);
+            uval[c] = vel_x_interp(U, g, x, y);
+            ux[c] = xp;
+            uy[c] = fsub(yp, fmul(g.dy, 0.5f));
+            uok[c] = 1;
+        } else {
+            uok[c] = 0;
+        }
+        if (liq || cell_type(L, g, i, j - 1) == LIQUID) {
+            const float x = fmul(fadd((float)i, 0.5f), g.dx);
+            const float y = fmul((float)j, g.dy);
+            float xp, yp;
+            advected_position(U, V, g, x, y, mdt, &xp, &yp);
+            vval[c] = vel_y_interp(V, g, x, y);
+            vx[c] = fsub(xp, fmul(g.dx, 0.5f));
+            vy[c] = yp;
+            vok[c] = 1;
+        } else {
+            vok[c] = 0;
+        }
     }
-    if (liq || cell_type(lab, g, i, j - 1) == LIQUID) {
-        const float x = fmul(fadd((float)i, 0.5f), g.dx);
-        const float y = fmul((float)j, g.dy);
-        float xp, yp;
-        advected_position(uf, vf, g, x, y, mdt, &xp, &yp);
-        vval[c] = vel_y_interp(vf, g, x, y);
-        vx[c] = fsub(xp, fmul(g.dx, 0.5f));
-        vy[c] = yp;
-        vok[c] = 1;
-    } else {
-        vok[c] = 0;
-    }
-}
+};
 
 __global__ void k_aos_to_soa(const float4* __restrict__ in, int64_t n, float* __restrict__ px,
                              float* __restrict__ py, float* __restrict__ pvx, float* __restrict__ pvy)
@@ -137,29 +156,22 @@ unsigned blocks_for(int64_t n) { return (unsigned)((n + TPB - 1) / TPB); }
 
 }  // namespace
 
-void g2p_advect(const Launch& L, const Geom& g, int g2p_mode, int adv_mode, float* px, float* py, float* pvx,
-                float* pvy, int64_t n, const float* uf, const float* vf, const float* ud, const float* vd,
-                const uint8_t* lab, float pic_ratio, float dt)
+void g2p_advect(const Launch& L, const Domain& d, int g2p_mode, int adv_mode, float* px, float* py, float* pvx,
+                float* pvy, const float* uf, const float* vf, const float* ud, const float* vd, const uint8_t* lab,
+                float dt)
 {
-    if (n <= 0) return;
-    k_g2p_advect<<<blocks_for(n), TPB, 0, L.stream>>>(g, g2p_mode, adv_mode, px, py, pvx, pvy, n, uf, vf, ud, vd, lab,
-                                                      pic_ratio, dt);
-    L.count();
+    each_particle(L, d, G2PAdvect{g2p_mode, adv_mode, px, py, pvx, pvy, uf, vf, ud, vd, lab, dt});
 }
 
-void p2g_positions(const Launch& L, const Geom& g, const float* px, const float* py, int64_t n, float* yu, float* xv)
+void p2g_positions(const Launch& L, const Domain& d, const float* px, const float* py, float* yu, float* xv)
 {
-    if (n <= 0) return;
-    k_p2g_positions<<<blocks_for(n), TPB, 0, L.stream>>>(g, px, py, n, yu, xv);
-    L.count();
+    each_particle(L, d, P2GPositions{px, py, yu, xv});
 }
 
-void sl_faces(const Launch& L, const Geom& g, const uint8_t* lab, const float* uf, const float* vf, float dt, float* ux,
+void sl_faces(const Launch& L, const Domain& d, const uint8_t* lab, const float* uf, const float* vf, float dt, float* ux,
               float* uy, float* uval, uint8_t* uok, float* vx, float* vy, float* vval, uint8_t* vok)
 {
-    k_sl_faces<<<blocks_for((int64_t)g.nx * g.ny), TPB, 0, L.stream>>>(g, lab, uf, vf, dt, ux, uy, uval, uok, vx, vy,
-                                                                        vval, vok);
-    L.count();
+    each_cell(L, d, SLFaces{lab, uf, vf, dt, ux, uy, uval, uok, vx, vy, vval, vok});
 }
 
 void aos_to_soa(const Launch& L, const float* xyuv, int64_t n, float* px, float* py, float* pvx, float* pvy)

@@ -8,7 +8,6 @@ namespace {
 constexpr int SCAN_THREADS = 1024;
 constexpr int SCAN_ITEMS = 4;
 constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
-constexpr int64_t SCAN_MAX_TILES = SCAN_TILE;  // tile sums are scanned by one block
 
 __device__ __forceinline__ int warp_inclusive(int v)
 {
@@ -81,25 +80,30 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_reduce(Load ld, int64_t n
     if (threadIdx.x == 0) tile_sums[blockIdx.x] = total;
 }
 
-// One block: exclusive scan of nt tile sums in place; grand total to *total.
+// One block: exclusive scan of nt tile sums in place, SCAN_TILE sums per
+// round with a running carry; grand total to *total.
 __global__ void __launch_bounds__(SCAN_THREADS) k_scan_tiles(int32_t* tile_sums, int nt, int32_t* total)
 {
-    const int base = threadIdx.x * SCAN_ITEMS;
-    int v[SCAN_ITEMS];
-    int s = 0;
+    int carry = 0;
+    for (int round = 0; round < nt; round += SCAN_TILE) {
+        const int base = round + threadIdx.x * SCAN_ITEMS;
+        int v[SCAN_ITEMS];
+        int s = 0;
 #pragma unroll
-    for (int k = 0; k < SCAN_ITEMS; ++k) {
-        v[k] = base + k < nt ? tile_sums[base + k] : 0;
-        s += v[k];
-    }
-    int tot;
-    int run = block_exclusive(s, &tot);
+        for (int k = 0; k < SCAN_ITEMS; ++k) {
+            v[k] = base + k < nt ? tile_sums[base + k] : 0;
+            s += v[k];
+        }
+        int tot;
+        int run = block_exclusive(s, &tot) + carry;
 #pragma unroll
-    for (int k = 0; k < SCAN_ITEMS; ++k) {
-        if (base + k < nt) tile_sums[base + k] = run;
-        run += v[k];
+        for (int k = 0; k < SCAN_ITEMS; ++k) {
+            if (base + k < nt) tile_sums[base + k] = run;
+            run += v[k];
+        }
+        carry += tot;
     }
-    if (threadIdx.x == 0 && total) *total = tot;
+    if (threadIdx.x == 0 && total) *total = carry;
 }
 
 template <class Load, class Store>
@@ -136,13 +140,49 @@ void scan_generic(const Launch& L, Load ld, Store st, int64_t n, int32_t* tmp, i
     L.count(3);
 }
 
+// Batched fluid indexing, pass 1: LIQUID cells of each cell block.
+__global__ void __launch_bounds__(DOMAIN_TPB) k_block_liquid(const Seg* __restrict__ segs, const int2* __restrict__ blk,
+                                                             const uint8_t* __restrict__ lab, int32_t* __restrict__ cnt)
+{
+    const int2 m = blk[blockIdx.x];
+    const Seg& s = segs[m.x];
+    const int64_t c = (int64_t)m.y + threadIdx.x;
+    const int v = (c < (int64_t)s.g.nx * s.g.ny && lab[s.co + c] == LIQUID) ? 1 : 0;
+    const int t = __syncthreads_count(v);
+    if (threadIdx.x == 0) cnt[blockIdx.x] = t;
+}
+
+// Pass 3: local fluid index = (global offset of the block) - (global offset of
+// the simulation's first block) + rank within the block.
+__global__ void __launch_bounds__(DOMAIN_TPB) k_block_fluid_index(const Seg* __restrict__ segs,
+                                                                  const int2* __restrict__ blk,
+                                                                  const uint8_t* __restrict__ lab,
+                                                                  const int32_t* __restrict__ off,
+                                                                  int32_t* __restrict__ fidx,
+                                                                  int32_t* __restrict__ cell_of,
+                                                                  int32_t* __restrict__ nfluid)
+{
+    const int2 m = blk[blockIdx.x];
+    const Seg& s = segs[m.x];
+    const int64_t c = (int64_t)m.y + threadIdx.x;
+    const bool in = c < (int64_t)s.g.nx * s.g.ny;
+    const int v = (in && lab[s.co + c] == LIQUID) ? 1 : 0;
+    int total;
+    const int excl = block_exclusive(v, &total);
+    const int base = off[blockIdx.x] - off[s.cb0];
+    if (in) {
+        fidx[s.co + c] = v ? base + excl : -1;
+        if (v) cell_of[s.co + base + excl] = (int32_t)c;
+    }
+    if (threadIdx.x == 0 && (int)blockIdx.x == s.cb0 + s.ncb - 1) nfluid[s.sim] = off[s.cb0 + s.ncb] - off[s.cb0];
+}
+
 }  // namespace
 
 size_t scan_tmp_ints(int64_t n) { return (size_t)((n + SCAN_TILE - 1) / SCAN_TILE) + 1; }
 
 void scan_exclusive_i32(const Launch& L, const int32_t* in, int32_t* out, int64_t n, int32_t* tmp)
 {
-    // Callers size their arrays to at most SCAN_TILE * SCAN_MAX_TILES items.
     scan_generic(L, LoadI32{in}, StoreI32{out}, n, tmp, out + n);
 }
 
@@ -150,6 +190,30 @@ void fluid_index(const Launch& L, const uint8_t* labels, int64_t n, int32_t* fid
                  int32_t* nfluid, int32_t* tmp)
 {
     scan_generic(L, LoadLiquid{labels}, StoreFluidIndex{fidx, cell_of}, n, tmp, nfluid);
+}
+
+}  // namespace fs
+
+namespace fs {
+
+size_t fluid_index_batch_tmp_ints(const Domain& d) { return 2 * ((size_t)d.ncblk + 1) + scan_tmp_ints((int64_t)d.ncblk + 1); }
+
+void fluid_index_batch(const Launch& L, const Domain& d, const uint8_t* labels, int32_t* fidx, int32_t* cell_of,
+                       int32_t* nfluid, int32_t* tmp)
+{
+    if (!d.segs) {
+        fluid_index(L, labels, d.cells, fidx, cell_of, nfluid, tmp);
+        return;
+    }
+    if (d.ncblk == 0) return;
+    int32_t* cnt = tmp;
+    int32_t* off = tmp + d.ncblk + 1;
+    int32_t* stmp = off + d.ncblk + 1;
+    k_block_liquid<<<d.ncblk, DOMAIN_TPB, 0, L.stream>>>(d.segs, d.cblk, labels, cnt);
+    L.count();
+    scan_exclusive_i32(L, cnt, off, d.ncblk, stmp);
+    k_block_fluid_index<<<d.ncblk, DOMAIN_TPB, 0, L.stream>>>(d.segs, d.cblk, labels, off, fidx, cell_of, nfluid);
+    L.count();
 }
 
 }  // namespace fs

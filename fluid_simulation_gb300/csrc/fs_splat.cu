@@ -9,7 +9,7 @@
 // base cells that can reach it, merging the four item lists by item index.
 // Each node thus adds exactly the same float terms in exactly the same order
 // as the reference's sequential loop, and the result is bit-identical.
-#include "fs_internal.h"
+#include "fs_domain.cuh"
 
 namespace fs {
 namespace {
@@ -26,17 +26,34 @@ __device__ __forceinline__ unsigned lanemask_lt()
     return m;
 }
 
-// Key of each item: base cell of its footprint, or n_cells for invalid items.
-__global__ void k_splat_keys(Geom g, float gdx, float gdy, int64_t n, const float* __restrict__ x,
-                             const float* __restrict__ y, const uint8_t* __restrict__ valid,
-                             uint32_t* __restrict__ keys, int32_t* __restrict__ vals, int32_t* __restrict__ bin_count)
+// Key of each item: the flattened index (co + local cell) of the base cell of
+// its footprint, or d.cells for invalid items and for the padding between
+// simulations.  Item k of the flattened range belongs to block k / DOMAIN_TPB.
+__global__ void __launch_bounds__(DOMAIN_TPB) k_splat_keys(Seg one, const Seg* __restrict__ segs,
+                                                           const int2* __restrict__ blk, bool cells, bool pool,
+                                                           int64_t n, uint32_t invalid, const float* __restrict__ x,
+                                                           const float* __restrict__ y,
+                                                           const uint8_t* __restrict__ valid,
+                                                           uint32_t* __restrict__ keys, int32_t* __restrict__ vals,
+                                                           int32_t* __restrict__ bin_count)
 {
-    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t k = (int64_t)blockIdx.x * DOMAIN_TPB + threadIdx.x;
     if (k >= n) return;
-    uint32_t key = (uint32_t)g.nx * (uint32_t)g.ny;
-    if (!valid || valid[k]) {
-        const Splat s = splat(g, gdx, gdy, x[k], y[k], 0.0f);
-        key = (uint32_t)s.i + (uint32_t)s.j * (uint32_t)g.nx;
+    Seg s;
+    int64_t local;
+    if (blk) {
+        const int2 m = blk[blockIdx.x];
+        s = segs[m.x];
+        local = (int64_t)m.y + threadIdx.x;
+    } else {
+        s = one;
+        local = k;
+    }
+    const int64_t count = cells ? (int64_t)s.g.nx * s.g.ny : s.np;
+    uint32_t key = invalid;
+    if (local < count && (!valid || valid[k])) {
+        const Splat sp = splat(s.g, pool ? s.g.pdx : s.g.dx, pool ? s.g.pdy : s.g.dy, x[k], y[k], 0.0f);
+        key = (uint32_t)(s.co + sp.i + (int64_t)sp.j * s.g.nx);
     }
     keys[k] = key;
     vals[k] = (int32_t)k;
@@ -111,63 +128,66 @@ __global__ void __launch_bounds__(RT) k_radix_scatter(const uint32_t* __restrict
     }
 }
 
-constexpr int MAX_CH = 2;
-
 // Each node (a, b) merges the item lists of base cells (a-1..a) x (b-1..b) by
 // item index and adds the corners of each item's footprint that land on it.
-__global__ void k_splat_gather(Geom g, float gdx, float gdy, const float* __restrict__ x,
-                               const float* __restrict__ y, int channels, const float* __restrict__ val0,
-                               const float* __restrict__ val1, const int32_t* __restrict__ bin_start,
-                               const int32_t* __restrict__ sorted, float* __restrict__ out0, float* __restrict__ out1)
+struct SplatGather
 {
-    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const int64_t ncell = (int64_t)g.nx * g.ny;
-    if (c >= ncell) return;
-    const int a = (int)(c % g.nx), b = (int)(c / g.nx);
-    int cur[4], end[4];
-    int nb = 0;
+    bool pool;
+    const float *x, *y;
+    int channels;
+    const float *val0, *val1;
+    const int32_t* bin_start;  // flattened cells + 2
+    const int32_t* sorted;
+    float *out0, *out1;
+    __device__ void operator()(const Seg& s, int64_t c, int a, int b) const
+    {
+        const Geom& g = s.g;
+        const float gdx = pool ? g.pdx : g.dx, gdy = pool ? g.pdy : g.dy;
+        int cur[4], end[4];
+        int nb = 0;
 #pragma unroll
-    for (int dj = -1; dj <= 0; ++dj)
+        for (int dj = -1; dj <= 0; ++dj)
 #pragma unroll
-        for (int di = -1; di <= 0; ++di) {
-            const int ii = a + di, jj = b + dj;
-            if (ii >= 0 && jj >= 0) {
-                const int64_t cell = (int64_t)ii + (int64_t)jj * g.nx;
-                cur[nb] = bin_start[cell];
-                end[nb] = bin_start[cell + 1];
-                ++nb;
+            for (int di = -1; di <= 0; ++di) {
+                const int ii = a + di, jj = b + dj;
+                if (ii >= 0 && jj >= 0) {
+                    const int64_t cell = s.co + (int64_t)ii + (int64_t)jj * g.nx;
+                    cur[nb] = bin_start[cell];
+                    end[nb] = bin_start[cell + 1];
+                    ++nb;
+                }
+            }
+        float acc0 = 0.0f, acc1 = 0.0f;
+        int head[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) head[q] = (q < nb && cur[q] < end[q]) ? sorted[cur[q]] : INT32_MAX;
+        for (;;) {
+            int best = INT32_MAX, bq = -1;
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+                if (head[q] < best) {
+                    best = head[q];
+                    bq = q;
+                }
+            if (bq < 0) break;
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+                if (q == bq) {
+                    ++cur[q];
+                    head[q] = cur[q] < end[q] ? sorted[cur[q]] : INT32_MAX;
+                }
+            const float xi = x[best], yi = y[best];
+            const Splat s0 = splat(g, gdx, gdy, xi, yi, val0 ? val0[best] : 1.0f);
+            acc0 = splat_accumulate(acc0, s0, a, b);
+            if (channels > 1) {
+                const Splat s1 = splat(g, gdx, gdy, xi, yi, val1 ? val1[best] : 1.0f);
+                acc1 = splat_accumulate(acc1, s1, a, b);
             }
         }
-    float acc0 = 0.0f, acc1 = 0.0f;
-    int head[4];
-#pragma unroll
-    for (int q = 0; q < 4; ++q) head[q] = (q < nb && cur[q] < end[q]) ? sorted[cur[q]] : INT32_MAX;
-    for (;;) {
-        int best = INT32_MAX, bq = -1;
-#pragma unroll
-        for (int q = 0; q < 4; ++q)
-            if (head[q] < best) {
-                best = head[q];
-                bq = q;
-            }
-        if (bq < 0) break;
-#pragma unroll
-        for (int q = 0; q < 4; ++q)
-            if (q == bq) {
-                ++cur[q];
-                head[q] = cur[q] < end[q] ? sorted[cur[q]] : INT32_MAX;
-            }
-        const float xi = x[best], yi = y[best];
-        const Splat s0 = splat(g, gdx, gdy, xi, yi, val0 ? val0[best] : 1.0f);
-        acc0 = splat_accumulate(acc0, s0, a, b);
-        if (channels > 1) {
-            const Splat s1 = splat(g, gdx, gdy, xi, yi, val1 ? val1[best] : 1.0f);
-            acc1 = splat_accumulate(acc1, s1, a, b);
-        }
+        out0[s.co + c] = acc0;
+        if (channels > 1) out1[s.co + c] = acc1;
     }
-    out0[c] = acc0;
-    if (channels > 1) out1[c] = acc1;
-}
+};
 
 int key_bits(uint32_t max_key)
 {
@@ -184,17 +204,20 @@ size_t splat_hist_ints(int64_t n_items)
     return (size_t)(256 * (ntiles > 0 ? ntiles : 1)) + 1;
 }
 
-void ordered_splat(const Launch& L, const Geom& g, float gdx, float gdy, int64_t n, const float* x, const float* y,
-                   const uint8_t* valid, int channels, const float* const* values, float* const* out, SplatWork& w)
+void ordered_splat(const Launch& L, const Domain& d, bool items_are_cells, bool pool_deltas, const float* x,
+                   const float* y, const uint8_t* valid, int channels, const float* const* values, float* const* out,
+                   SplatWork& w)
 {
-    const int64_t ncell = (int64_t)g.nx * g.ny;
-    const unsigned cb = (unsigned)((ncell + 255) / 256);
+    const int64_t ncell = d.cells;
+    const int64_t n = items_are_cells ? d.cells : d.parts;
     // bin counts over ncell + 1 bins (the last one collects invalid items)
     cudaMemsetAsync(w.hist_scan, 0, sizeof(int32_t) * (size_t)(ncell + 2), L.stream);
     int32_t* bin_count = w.hist_scan;
     if (n > 0) {
-        k_splat_keys<<<(unsigned)((n + 255) / 256), 256, 0, L.stream>>>(g, gdx, gdy, n, x, y, valid, w.keys_a, w.vals_a,
-                                                                        bin_count);
+        const int2* blk = d.segs ? (items_are_cells ? d.cblk : d.pblk) : nullptr;
+        k_splat_keys<<<domain_blocks(n), DOMAIN_TPB, 0, L.stream>>>(d.one, d.segs, blk, items_are_cells, pool_deltas,
+                                                                     n, (uint32_t)ncell, x, y, valid, w.keys_a,
+                                                                     w.vals_a, bin_count);
         L.count();
     }
     scan_exclusive_i32(L, bin_count, w.bin_start, ncell + 1, w.scan_tmp);
@@ -217,9 +240,9 @@ void ordered_splat(const Launch& L, const Geom& g, float gdx, float gdy, int64_t
             vout = tv;
         }
     }
-    k_splat_gather<<<cb, 256, 0, L.stream>>>(g, gdx, gdy, x, y, channels, values[0], channels > 1 ? values[1] : nullptr,
-                                             w.bin_start, vin, out[0], channels > 1 ? out[1] : nullptr);
-    L.count();
+    each_cell(L, d,
+              SplatGather{pool_deltas, x, y, channels, values[0], channels > 1 ? values[1] : nullptr, w.bin_start, vin,
+                          out[0], channels > 1 ? out[1] : nullptr});
 }
 
 }  // namespace fs

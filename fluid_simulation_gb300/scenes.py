@@ -149,3 +149,39 @@ def projection_problem(n: int = 4096, seed: int = 0xC5, solid_fraction: float = 
     means = np.concatenate([[0.0], sums / counts])
     rhs = np.where(fluid, g - means[comp], 0.0)
     return labels, rhs
+
+
+def batch_scenes(n: int = 512, seed: int = 0xC3, min_side: int = 32, max_side: int = 256,
+                 max_discs: int = 3) -> list[Scene]:
+    """n independent square simulations with unit cells: side ~ U{min_side..max_side},
+    a random rectangular fluid block (4 jittered particles per non-solid cell),
+    0..max_discs random solid discs, FLIP ratio ~ U[0.9, 1.0] (pic_ratio = 1 -
+    ratio), rho = dt = 0.005, CG to relative residual 1e-5.  Every draw comes
+    from the SplitMix64 stream of (seed, simulation)."""
+    out = []
+    for s in range(n):
+        u = splitmix64((seed << 20) ^ (s * 0x9E37), 16)
+        f = (u >> np.uint64(11)).astype(np.float64) * (2.0 ** -53)
+        side = min_side + int(f[0] * (max_side - min_side + 1))
+        side = min(side, max_side)
+        # block [i0, i1) x [j0, j1) inside the solid border, at least 2 cells a side
+        w = max(2, int((0.2 + 0.5 * f[1]) * (side - 2)))
+        h = max(2, int((0.2 + 0.5 * f[2]) * (side - 2)))
+        i0 = 1 + int(f[3] * (side - 2 - w))
+        j0 = 1 + int(f[4] * (side - 2 - h))
+        ndisc = min(max_discs, int(f[5] * (max_discs + 1)))
+        solid = np.zeros((side, side), np.uint8)
+        for d in range(ndisc):
+            r = 2.0 + f[6 + 3 * d] * side / 10.0
+            cx = 1.0 + f[7 + 3 * d] * (side - 2)
+            cy = 1.0 + f[8 + 3 * d] * (side - 2)
+            solid |= disc_mask(side, side, cx, cy, r)
+        ratio = 0.9 + 0.1 * f[15]
+        pic = float(np.float32(1.0 - ratio))
+        parts = block_particles(side, side, float(side), float(side), i0, i0 + w, j0, j0 + h, 4,
+                                seed * 1000003 + s, solid if ndisc else None)
+        out.append(Scene(side, side, float(side), float(side), 0.005, pic, 0.005, parts,
+                         solid=solid if ndisc else None, cg_tolerance=1e-5, cg_max_iterations=20000,
+                         description="batch member %d: %dx%d, block %dx%d, %d discs" % (s, side, side, w, h, ndisc),
+                         meta={"block": [i0, i0 + w, j0, j0 + h], "discs": ndisc, "seed": seed}))
+    return out

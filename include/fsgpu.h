@@ -203,7 +203,7 @@ FS_API int fs_set_stream(fs_handle* h, void* stream);
 /* Number of this library's kernel launches queued so far on h. */
 FS_API int64_t fs_kernel_launches(fs_handle* h);
 
-/* Pressure projection alone (no particles; BASELINE configs[4]-style use): the
+/* Pressure projection alone (no particles): the
  * Poisson system of FluidSolver::pressureSolve (src/FluidSolver.cpp:363-425)
  * built from a label grid (FS_LIQUID = unknown, FS_AIR = pressure 0,
  * FS_SOLID = wall), with a double right-hand side per cell, solved by
@@ -238,6 +238,50 @@ FS_API int fs_poisson_solve(fs_poisson* p, int method, double tolerance, int max
 /* The solution on every cell (0 outside fluid), host array of doubles. */
 FS_API int fs_poisson_get_solution(fs_poisson* p, double* out);
 FS_API int64_t fs_poisson_kernel_launches(const fs_poisson* p);
+
+/* A batch of independent simulations stepped together (no counterpart in the
+ * reference, whose caller would loop over FluidSolver/FluidDomain pairs,
+ * src/FluidSolver.cpp:211-251, include/FluidDomain.h:40-64).  Simulation s is
+ * configured by cfgs[s] exactly like fs_create; sizes may differ.  Batch-wide
+ * settings come from cfgs[0]: device, extension_iterations, cg_precision.
+ * Each simulation's results are bit-identical to stepping it alone through a
+ * handle.  Limits: at most 65536 interior cells ((size_x-2) * (size_y-2)) per
+ * simulation and 16 Mi cells in total (FS_ERR_TOO_LARGE).
+ *
+ * Particles set with fs_batch_set_particles are laid out on the device at the
+ * next step or particle read.  fs_batch_step runs every simulation's
+ * FluidSolver::step* once, as one CUDA graph (captured on first use per
+ * method, dt and particle layout).  The pressure solves run one thread-block
+ * cluster per simulation; fs_batch_tune times whole steps for each cluster
+ * plan (1, 2, 4 or 8 chunks of 1024 fluid cells per CTA), keeps the fastest
+ * and leaves the state as it found it (ms_out: 4 floats or NULL). */
+typedef struct fs_batch fs_batch;
+
+FS_API int fs_batch_create(int n, const fs_config* cfgs, fs_batch** out);
+FS_API int fs_batch_destroy(fs_batch* b);
+/* NULL b: the message of the last failed fs_batch_create on this thread. */
+FS_API const char* fs_batch_last_error(const fs_batch* b);
+FS_API int fs_batch_size(const fs_batch* b);
+/* AoS {x, y, vx, vy} float quadruples, as fs_set_particles. */
+FS_API int fs_batch_set_particles(fs_batch* b, int sim, const float* xyuv, int64_t n);
+FS_API int fs_batch_num_particles(fs_batch* b, int sim, int64_t* n);
+FS_API int fs_batch_get_particles(fs_batch* b, int sim, float* xyuv, int64_t n);
+/* size_x * size_y uint8 of simulation sim (non-zero = solid), or NULL to clear. */
+FS_API int fs_batch_set_solid_mask(fs_batch* b, int sim, const uint8_t* mask);
+FS_API int fs_batch_get_grid(fs_batch* b, int sim, int which, float* out);
+FS_API int fs_batch_get_labels(fs_batch* b, int sim, uint8_t* out);
+FS_API int fs_batch_get_pressure(fs_batch* b, int sim, float* out);
+FS_API int fs_batch_step(fs_batch* b, int method, float dt);
+FS_API int fs_batch_synchronize(fs_batch* b);
+/* CG iterations, residual, fluid cells and warnings of simulation sim's last
+ * pressure solve (ms fields are 0). */
+FS_API int fs_batch_get_stats(fs_batch* b, int sim, fs_step_stats* out);
+FS_API int fs_batch_tune(fs_batch* b, int method, float dt, int steps, float* ms_out);
+FS_API int fs_batch_set_tuning(fs_batch* b, int chunks_per_cta);
+FS_API int fs_batch_get_tuning(const fs_batch* b);
+FS_API int fs_batch_set_graphs(fs_batch* b, int enable);
+FS_API void* fs_batch_get_stream(fs_batch* b);
+FS_API int64_t fs_batch_kernel_launches(fs_batch* b);
 
 /* Allocation-free pressure solve.  No counterpart in the reference: this is
  * FluidSolver::pressureSolve's fluid indexing, assembly and conjugate gradient

@@ -208,3 +208,28 @@ def test_empty_domain_and_no_fluid():
         o.step(po.STEP_PICFLIP, sc.dt)
     assert_same(g.state(), o.state(), where="empty")
     assert g.stats()["n_fluid"] == 0
+
+
+def test_p2g_on_4096_grid_reaches_the_last_cells():
+    """4096 x 4096 cells make 4096^2 + 1 splat bins, more tiles than one block
+    of the tile-sum scan covers in one round; particles next to the last
+    cell must still land in the right bins."""
+    n = 4096
+    rng = np.random.default_rng(3)
+    k = 4000
+    corner = np.stack([n - 2 + rng.random(k) * 1.9, n - 2 + rng.random(k) * 1.9,
+                       rng.standard_normal(k), rng.standard_normal(k)], axis=1).astype(np.float32)
+    spread = np.stack([1 + rng.random(k) * (n - 2), 1 + rng.random(k) * (n - 2),
+                       rng.standard_normal(k), rng.standard_normal(k)], axis=1).astype(np.float32)
+    parts = np.concatenate([corner, spread])
+    g = fsg.FluidSim(n, n, float(n), float(n), 1.0, 0.02)
+    o = po.OracleSim("restatement", n, n, float(n), float(n), 1.0, 0.02)
+    g.set_particles(parts)
+    o.set_particles(parts)
+    for ph in (fsg.PH_CLASSIFY, fsg.PH_P2G):
+        g.phase(ph, 0.005)
+        o.phase(ph, 0.005)
+    for w in (fsg.U_FRONT, fsg.V_FRONT):
+        a, b = g.grid(w), o.grid(w)
+        assert np.array_equal(a.view(np.uint32), b.view(np.uint32)), w
+        assert np.count_nonzero(a[n - 3:, n - 3:]) > 0

@@ -124,6 +124,9 @@ def test_gpu_methods_error_against_fp64_direct_solve():
         st = ps.solve(method, tol, 50000, inner_tol=1e-3)
         x = demean(ps.solution()[fluid])
         errs[name] = np.linalg.norm(x - xd) / np.linalg.norm(xd)
-        assert st["residual"] < (2e-5 if method == 0 else 1e-10), (name, st)
+        # the FP32 method stops on the float CG's recursive residual (1e-5); the
+        # reported residual is the true FP64 one, a few times larger
+        assert st["residual"] < (1e-4 if method == 0 else 1e-10), (name, st)
+    print("relative error vs FP64 direct solve:", errs)
     assert errs["fp64"] < 1e-8 and errs["mixed"] < 1e-8, errs
     assert errs["fp32"] < 1e-2, errs
