@@ -16,6 +16,12 @@ times the reference's CPU implementation of the path (the reference's own
 sources when built here, else the C restatement of them) on the same
 workload.  Under torchrun (N > 1) every rank runs an independent replica
 (nothing on the data path is exchanged); rank 0 prints.
+
+At N = 1 the line also carries `forms`: the batched form (512 independent
+simulations of sides 32..256 stepped as one graph-replayed batch step) and the
+mixed-precision form (the 4096^2 pressure projection to relative residual
+1e-10 by FP64 iterative refinement around float CG, against an FP64-only CG).
+--no-forms skips them; --only-form measures one of them alone.
 """
 from __future__ import annotations
 
@@ -48,6 +54,11 @@ def parse():
     ap.add_argument("--size", type=int, default=1024)
     ap.add_argument("--cpu-budget", type=float, default=150.0, help="seconds of CPU work for CPU timings")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample (profiling runs)")
+    ap.add_argument("--no-forms", action="store_true", help="skip the batched and mixed-precision forms")
+    ap.add_argument("--batch", type=int, default=512, help="members of the batched form")
+    ap.add_argument("--projection-size", type=int, default=4096, help="grid side of the mixed-precision form")
+    ap.add_argument("--only-form", choices=["batched", "mixed_precision"], default=None,
+                    help="measure one form alone (profiling runs) and print its JSON object")
     return ap.parse_args()
 
 
@@ -230,6 +241,79 @@ def peaks():
     return 6800.0, "fallback"
 
 
+def measure_batched(args, local_rank, plain_value, flush):
+    """The batched form: args.batch independent simulations (sides U{32..256},
+    random blocks and discs, FLIP ratio U[0.9, 1.0], CG 1e-5) advanced by one
+    graph-replayed fs_batch_step per step, after the autotuner picked the CG
+    cluster plan.  Same timing discipline as the main line."""
+    import torch
+
+    import fluid_simulation_gb300 as fsg
+    from fluid_simulation_gb300 import scenes
+
+    sc = scenes.batch_scenes(args.batch)
+    cells = sum(s.cells for s in sc)
+    b = fsg.FluidBatch.from_scenes(sc, device=local_rank)
+    b.step(fsg.STEP_PICFLIP, 0.005)
+    tuned = b.tune(fsg.STEP_PICFLIP, 0.005, steps=2)
+    for _ in range(args.warmup):
+        b.step(fsg.STEP_PICFLIP, 0.005)
+    b.synchronize()
+    stream = torch.cuda.ExternalStream(b.stream(), device=local_rank)
+    ms, fi, itmax = [], 0, 0
+    l0 = b.kernel_launches()
+    for _ in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+        b.step(fsg.STEP_PICFLIP, 0.005)
+        e1.record(stream)
+        b.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    for s in range(len(sc)):
+        st = b.stats(s)
+        fi += st["n_fluid"] * st["cg_iterations"]
+        itmax = max(itmax, st["cg_iterations"])
+    t = sum(ms) / 1000.0
+    value = cells * args.steps / t
+    return {"workload": "%d simulations, sides U{32..256} (seed 0xC3), %d cells, %d particles, "
+                        "stepPICFLIP, CG 1e-5" % (len(sc), cells, sum(len(s.particles) for s in sc)),
+            "value": value, "unit": UNIT, "ms_per_step": 1000.0 * t / args.steps, "vs_plain": value / plain_value,
+            "cg_plan_chunks_per_cta": tuned["chunks_per_cta"], "tuner_ms_per_step": tuned["ms_per_step"],
+            "cg_iterations_max_last_step": itmax, "sum_F_I_last_step": fi,
+            "gpu_launches": int(b.kernel_launches() - l0)}
+
+
+def measure_projection(args, local_rank):
+    """The mixed-precision form: the pressure projection alone on an n x n
+    domain (solid border, 5% random solids, N(0,1) right-hand side with each
+    component's mean removed) to relative residual 1e-10, by FP64 iterative
+    refinement around float-vector CG (float or double dot products), and by
+    an FP64-only CG; device time of each solve."""
+    import fluid_simulation_gb300 as fsg
+    from fluid_simulation_gb300 import scenes
+
+    n = args.projection_size
+    labels, rhs = scenes.projection_problem(n)
+    ps = fsg.PoissonSolver(n, n, float(n), float(n), device=local_rank)
+    ps.set_problem(labels, rhs)
+    out = {"workload": "%dx%d projection, 5%% solids, N(0,1) rhs, relative residual 1e-10" % (n, n),
+           "fluid_cells": int((labels == 0).sum())}
+    for name, method, inner in (("mixed_f32_dots", fsg.POISSON_MIXED, fsg.CG_FLOAT),
+                                ("mixed_f64_dots", fsg.POISSON_MIXED, fsg.CG_DOUBLE),
+                                ("fp64", fsg.POISSON_FP64, fsg.CG_FLOAT)):
+        st = ps.solve(method, 1e-10, 200000, inner_tol=1e-3, inner_precision=inner)
+        out[name] = {"ms": st["ms"], "residual": st["residual"], "outer_iterations": st["outer_iterations"],
+                     "inner_iterations": st["inner_iterations"],
+                     "cell_solves_per_s": n * n / (st["ms"] / 1000.0)}
+    out["speedup_mixed_vs_fp64"] = out["fp64"]["ms"] / out["mixed_f32_dots"]["ms"]
+    out["speedup_mixed_f64_dots_vs_fp64"] = out["fp64"]["ms"] / out["mixed_f64_dots"]["ms"]
+    ps.close()
+    return out
+
+
 def run_gpu(args, rank, world, local_rank):
     import torch
 
@@ -243,6 +327,15 @@ def run_gpu(args, rank, world, local_rank):
 
         dist.barrier()
     torch.cuda.set_device(local_rank)
+    if args.only_form:
+        if rank == 0:
+            flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda:%d" % local_rank)
+            if args.only_form == "batched":
+                out = measure_batched(args, local_rank, float("nan"), flush)
+            else:
+                out = measure_projection(args, local_rank)
+            print(json.dumps({"form": args.only_form, **out}), flush=True)
+        return
     sc = workload(args.size)
     sim = fsg.FluidSim.from_scene(sc, device=local_rank)
     stream = torch.cuda.ExternalStream(sim.stream(), device=local_rank)
@@ -321,6 +414,10 @@ def run_gpu(args, rank, world, local_rank):
 
     if rank != 0:
         return
+    forms = None
+    if world == 1 and not args.no_forms:
+        forms = {"batched": measure_batched(args, local_rank, value, flush),
+                 "mixed_precision": measure_projection(args, local_rank)}
     # roofline of the dominant kernel (the CG)
     peak, peak_kind = peaks()
     cg_s = sum(cg_ms) / 1000.0
@@ -338,7 +435,7 @@ def run_gpu(args, rank, world, local_rank):
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1000.0 * t_dev / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32 (CG dot products f64)",
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded SplitMix64 dam break)",
         "config": config_of(sc, {"parallelism": "replicas" if world > 1 else "single GPU",
                                  "l2": "256 MiB written before every timed step; the step's CUDA events exclude it",
@@ -360,6 +457,8 @@ def run_gpu(args, rank, world, local_rank):
                                    "the timed region (%.1f s), single thread" % sum(ctimes)},
         "clocks": clocks,
     }
+    if forms:
+        line["forms"] = forms
     print(json.dumps(line), flush=True)
 
 

@@ -119,6 +119,7 @@ struct fs_batch
     CgResult* results = nullptr;
     int32_t* d_order = nullptr;
     std::vector<ClassPlan> plan;
+    std::vector<int> plan_chunks;  // chunks each simulation's cluster is sized for
     int plan_target = 8;
 
     int front = 0, vfront = 0;
@@ -158,14 +159,16 @@ int max_chunks(const Seg& s) { return (int)std::max<int64_t>(1, (interior(s) + 1
 
 // Cluster shape of each simulation for a target of `target` chunks per CTA:
 // the smallest power-of-two cluster (<= 8) that keeps the chunks per CTA at or
-// under the target; the shared-memory footprint is 4 chunks (two CTAs per SM)
-// or 8 (one CTA per SM).
+// under the target, for the chunk count the simulation is planned for
+// (plan_chunks); the shared-memory footprint is 4 chunks (two CTAs per SM) or
+// 8 (one CTA per SM).  A simulation that later outgrows its cluster still
+// solves correctly, from global memory.
 int make_plan(fs_batch* b, int target)
 {
     std::vector<std::vector<int>> groups(8);
     auto key = [](int K, int C) { return (K == 8 ? 4 : 0) + (C == 1 ? 0 : C == 2 ? 1 : C == 4 ? 2 : 3); };
     for (int s = 0; s < b->n; ++s) {
-        const int ch = max_chunks(b->seg[s]);
+        const int ch = b->plan_chunks[s];
         int C = 1;
         while (C < 8 && (ch + C - 1) / C > target) C *= 2;
         const int per = (ch + C - 1) / C;
@@ -177,8 +180,7 @@ int make_plan(fs_batch* b, int target)
     for (int g = 0; g < 8; ++g) {
         if (groups[g].empty()) continue;
         std::vector<int>& v = groups[g];
-        std::stable_sort(v.begin(), v.end(),
-                         [&](int a, int c) { return max_chunks(b->seg[a]) > max_chunks(b->seg[c]); });
+        std::stable_sort(v.begin(), v.end(), [&](int a, int c) { return b->plan_chunks[a] > b->plan_chunks[c]; });
         ClassPlan cp;
         cp.K = g >= 4 ? 8 : 4;
         cp.C = 1 << (g & 3);
@@ -199,6 +201,21 @@ int make_plan(fs_batch* b, int target)
     b->plan = plan;
     b->plan_target = target;
     clear_graphs(b);
+    return FS_OK;
+}
+
+// Plans clusters for the current fluid cells of every simulation plus a 25%
+// margin (never more than its interior), as the tuner does.
+int refresh_plan_chunks(fs_batch* b)
+{
+    std::vector<int32_t> nf(b->n);
+    cudaError_t e = cudaMemcpyAsync(nf.data(), b->nfluid, sizeof(int32_t) * b->n, cudaMemcpyDeviceToHost, b->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+    if (e != cudaSuccess) return cuda_fail(b, e, "fluid counts");
+    for (int s = 0; s < b->n; ++s) {
+        const int64_t want = ((int64_t)nf[s] * 5 / 4 + 1023) / 1024;
+        b->plan_chunks[s] = (int)std::max<int64_t>(1, std::min<int64_t>(want, max_chunks(b->seg[s])));
+    }
     return FS_OK;
 }
 
@@ -755,6 +772,8 @@ int fs_batch_create(int n, const fs_config* cfgs, fs_batch** out)
         free_all(b);
         return code;
     }
+    b->plan_chunks.resize(n);
+    for (int s = 0; s < n; ++s) b->plan_chunks[s] = max_chunks(b->seg[s]);
     const int rc = make_plan(b, 8);
     if (rc != FS_OK) {
         g_batch_error = b->err;
@@ -932,6 +951,8 @@ int fs_batch_tune(fs_batch* b, int method, float dt, int steps, float* ms_out)
         const cudaError_t e = ensure_sl_scratch(b);
         if (e != cudaSuccess) return cuda_fail(b, e, "semi-Lagrangian scratch");
     }
+    rc = refresh_plan_chunks(b);
+    if (rc) return rc;
     // Save the state, time `steps` steps per candidate from that state, restore.
     const std::vector<Region> regs = persistent(b);
     size_t total = 0;

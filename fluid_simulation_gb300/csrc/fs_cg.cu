@@ -516,7 +516,7 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(CgArgs a)
 }
 
 // A batch of independent systems: one thread-block cluster per system (the
-// simulation order[cluster]); K chunks per CTA in shared memory.  The
+// simulation order[cluster]); up to K chunks per CTA in shared memory.  The
 // reduction tree, and so every result, is that of k_cg.
 template <int K>
 __global__ void __launch_bounds__(CG_THREADS, 1) k_cg_cluster(CgBatchArgs ba)
@@ -560,12 +560,20 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg_cluster(CgBatchArgs ba)
         if (sync.rank() == 0 && threadIdx.x == 0) *a.result = CgResult{0, 0, 0.0, 0.0};
         return;
     }
-    if (nchunks > a.max_chunks || nchunks > K * sync.size()) {
+    if (nchunks > a.max_chunks) {
         if (sync.rank() == 0 && threadIdx.x == 0) atomicOr(a.status, ST_TOO_LARGE);
         return;
     }
-    if (a.fp64) cg_body<K, double>(a, sm, dyn, nf, nchunks, sync);
-    else cg_body<K, float>(a, sm, dyn, nf, nchunks, sync);
+    // A system that outgrew the cluster's shared memory streams its state
+    // from global memory instead (same arithmetic, same results).
+    const bool resident = nchunks <= K * sync.size();
+    if (a.fp64) {
+        if (resident) cg_body<K, double>(a, sm, dyn, nf, nchunks, sync);
+        else cg_body<0, double>(a, sm, dyn, nf, nchunks, sync);
+    } else {
+        if (resident) cg_body<K, float>(a, sm, dyn, nf, nchunks, sync);
+        else cg_body<0, float>(a, sm, dyn, nf, nchunks, sync);
+    }
 }
 
 }  // namespace

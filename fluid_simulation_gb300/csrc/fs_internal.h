@@ -214,8 +214,9 @@ struct CgBatchArgs
 // chunks of shared-memory state each (also sets the kernel's shared-memory
 // attribute); < 1 if that shape cannot run.
 int cg_cluster_capacity(int chunks_per_cta, int cluster);
-// Solves systems order[0..nsys) of ba, one cluster each; each must have at
-// most chunks_per_cta * cluster chunks of 1024 fluid cells.
+// Solves systems order[0..nsys) of ba, one cluster each; a system of more than
+// chunks_per_cta * cluster chunks of 1024 fluid cells streams its state from
+// global memory instead of holding it in shared memory.
 cudaError_t cg_solve_clusters(const Launch& L, const CgBatchArgs& ba, int nsys, int chunks_per_cta, int cluster);
 
 }  // namespace fs

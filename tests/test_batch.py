@@ -89,6 +89,8 @@ def test_batch_matches_oracle_per_simulation(method):
             it, res, nf = o.cg_stats()
             st = b.stats(s)
             assert (st["cg_iterations"], st["n_fluid"]) == (it, nf), (k, s)
+    # the comparison is not vacuous: the fields moved
+    assert np.abs(os_[-1].state()["v_front"]).max() > 0 and np.abs(b.state(len(sc) - 1)["particles"][:, 3]).max() > 0
 
 
 @pytest.mark.gpu
@@ -160,3 +162,30 @@ def test_batch_validate_quirk_and_empty_members():
         e_.step(po.STEP_PICFLIP, 0.005)
         assert_same(b.state(0), o.state(), "step %d sim 0" % k)
         assert_same(b.state(1), e_.state(), "step %d empty sim" % k)
+
+
+@pytest.mark.gpu
+def test_batch_member_outgrowing_its_cluster_plan_stays_exact():
+    """The tuner sizes each member's cluster for its current fluid cells; a
+    member whose fluid then grows past that size solves from global memory,
+    with the same results."""
+    fsbuild.build()
+    sc = scenes.batch_scenes(n=3, seed=51, min_side=120, max_side=200)
+    s0 = sc[0]
+    small = scenes.block_particles(s0.size_x, s0.size_y, s0.length_x, s0.length_y, 1, 9, 1, 9, 4, 77, s0.solid)
+    b = fsg.FluidBatch.from_scenes(sc)
+    b.set_particles(0, small)
+    os_ = [oracle_for(s) for s in sc]
+    os_[0].set_particles(small)
+    b.step(fsg.STEP_PICFLIP, 0.005)
+    for o in os_:
+        o.step(po.STEP_PICFLIP, 0.005)
+    b.tune(fsg.STEP_PICFLIP, 0.005, steps=1)
+    b.set_particles(0, s0.particles)
+    os_[0].set_particles(s0.particles)
+    for k in range(3):
+        b.step(fsg.STEP_PICFLIP, 0.005)
+        for s, o in enumerate(os_):
+            o.step(po.STEP_PICFLIP, 0.005)
+            assert_same(b.state(s), o.state(), "grown step %d sim %d" % (k, s))
+    assert b.stats(0)["n_fluid"] > 4 * 1024 * 5 // 4
