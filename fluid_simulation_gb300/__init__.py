@@ -29,6 +29,8 @@ STEP_SEMI_LAGRANGIAN, STEP_PIC, STEP_FLIP, STEP_PICFLIP = range(4)
  PH_SWAP) = range(16)
 CG_FLOAT, CG_DOUBLE = 0, 1
 POISSON_FP32, POISSON_FP64, POISSON_MIXED = 0, 1, 2
+INTEGRATOR_EULER, INTEGRATOR_RK2, INTEGRATOR_RK3 = 0, 1, 2
+SMOKE_FP32, SMOKE_FP64 = 0, 1
 TIMED_PHASES = ("classify", "p2g", "forces", "assembly", "cg", "project", "g2p")
 
 
@@ -49,6 +51,13 @@ class fs_config(C.Structure):
 class fs_poisson_stats(C.Structure):
     _fields_ = [("outer_iterations", C.c_int), ("inner_iterations", C.c_int), ("residual", C.c_double),
                 ("ms", C.c_float)]
+
+
+class fs_smoke_config(C.Structure):
+    _fields_ = [("size_x", C.c_int), ("size_y", C.c_int), ("length_x", C.c_float), ("length_y", C.c_float),
+                ("dt", C.c_float), ("integrator", C.c_int), ("precision", C.c_int), ("projection_method", C.c_int),
+                ("cg_tolerance", C.c_double), ("cg_max_iterations", C.c_int), ("inner_tolerance", C.c_double),
+                ("checkpoint_every", C.c_int), ("device", C.c_int), ("reserved", C.c_int * 8)]
 
 
 class fs_step_stats(C.Structure):
@@ -117,6 +126,17 @@ SIGNATURES = {
     "fs_batch_set_graphs": (_i, [_vp, _i]),
     "fs_batch_get_stream": (_vp, [_vp]),
     "fs_batch_kernel_launches": (_i64, [_vp]),
+    "fs_smoke_config_init": (None, [C.POINTER(fs_smoke_config), _i, _i]),
+    "fs_smoke_create": (_i, [C.POINTER(fs_smoke_config), C.POINTER(_vp)]),
+    "fs_smoke_destroy": (_i, [_vp]),
+    "fs_smoke_last_error": (C.c_char_p, [_vp]),
+    "fs_smoke_set_solid_mask": (_i, [_vp, _vp]),
+    "fs_smoke_set_state": (_i, [_vp, _vp, _vp, _vp]),
+    "fs_smoke_set_target": (_i, [_vp, _vp]),
+    "fs_smoke_forward": (_i, [_vp, _i, C.POINTER(_d)]),
+    "fs_smoke_get_state": (_i, [_vp, _vp, _vp, _vp]),
+    "fs_smoke_backward": (_i, [_vp, _vp, _vp, _vp]),
+    "fs_smoke_kernel_launches": (_i64, [_vp]),
     "fs_pressure_solve_noalloc": (_i, [_i, _i, _f, _f, _vp, _vp, _vp, _d, _i, _i, _vp, C.POINTER(_i),
                                        C.POINTER(_d), _vp]),
 }
@@ -451,6 +471,79 @@ class FluidBatch:
         s["pressure"] = self.pressure(sim)
         s["particles"] = self.particles(sim)
         return s
+
+
+class Smoke:
+    """Differentiable smoke on the GPU (fs_smoke_*): forward steps, the loss
+    ||density - target|| and its gradient with respect to the initial state."""
+
+    def __init__(self, size_x: int, size_y: int, dt: float = 0.01, integrator: int = INTEGRATOR_RK2,
+                 precision: int = SMOKE_FP32, projection_method: int = POISSON_MIXED, cg_tolerance: float = 1e-10,
+                 checkpoint_every: int = 8, device: int = 0, cg_max_iterations: int = 100000,
+                 inner_tolerance: float = 1e-3):
+        self.lib = load_library()
+        cfg = fs_smoke_config()
+        self.lib.fs_smoke_config_init(C.byref(cfg), size_x, size_y)
+        cfg.dt, cfg.integrator, cfg.precision = dt, integrator, precision
+        cfg.projection_method, cfg.cg_tolerance, cfg.checkpoint_every = projection_method, cg_tolerance, checkpoint_every
+        cfg.device, cfg.cg_max_iterations, cfg.inner_tolerance = device, cg_max_iterations, inner_tolerance
+        h = C.c_void_p()
+        rc = self.lib.fs_smoke_create(C.byref(cfg), C.byref(h))
+        if rc != FS_OK:
+            raise FsError(rc, self.lib.fs_smoke_last_error(None).decode())
+        self.h = h
+        self.shape = (size_y, size_x)
+
+    def _check(self, rc: int) -> None:
+        if rc != FS_OK:
+            raise FsError(rc, self.lib.fs_smoke_last_error(self.h).decode())
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            self.lib.fs_smoke_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _arr(self, a) -> np.ndarray:
+        return np.ascontiguousarray(a, dtype=np.float64).reshape(self.shape)
+
+    def set_solid_mask(self, mask: np.ndarray | None) -> None:
+        if mask is None:
+            self._check(self.lib.fs_smoke_set_solid_mask(self.h, None))
+        else:
+            m = np.ascontiguousarray(mask, dtype=np.uint8).reshape(self.shape)
+            self._check(self.lib.fs_smoke_set_solid_mask(self.h, _ptr(m)))
+
+    def set_state(self, u, v, density) -> None:
+        u, v, d = self._arr(u), self._arr(v), self._arr(density)
+        self._check(self.lib.fs_smoke_set_state(self.h, _ptr(u), _ptr(v), _ptr(d)))
+
+    def set_target(self, target) -> None:
+        t = self._arr(target)
+        self._check(self.lib.fs_smoke_set_target(self.h, _ptr(t)))
+
+    def forward(self, steps: int) -> float:
+        loss = C.c_double()
+        self._check(self.lib.fs_smoke_forward(self.h, steps, C.byref(loss)))
+        return loss.value
+
+    def state(self) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
+        out = [np.empty(self.shape, np.float64) for _ in range(3)]
+        self._check(self.lib.fs_smoke_get_state(self.h, *[_ptr(a) for a in out]))
+        return tuple(out)
+
+    def backward(self) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
+        out = [np.empty(self.shape, np.float64) for _ in range(3)]
+        self._check(self.lib.fs_smoke_backward(self.h, *[_ptr(a) for a in out]))
+        return tuple(out)
+
+    def kernel_launches(self) -> int:
+        return self.lib.fs_smoke_kernel_launches(self.h)
 
 
 class PoissonSolver:

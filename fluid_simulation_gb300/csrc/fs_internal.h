@@ -219,4 +219,14 @@ int cg_cluster_capacity(int chunks_per_cta, int cluster);
 // global memory instead of holding it in shared memory.
 cudaError_t cg_solve_clusters(const Launch& L, const CgBatchArgs& ba, int nsys, int chunks_per_cta, int cluster);
 
+// ---- the Poisson solver of fs_poisson.cu, from device pointers --------------
+// Labels (device, FS_* cell types) define the system; d_rhs and d_x hold one
+// double per cell (the solution is 0 outside fluid).  Work runs on the
+// solver's own stream; the call returns after the solve.
+cudaStream_t poisson_stream(const fs_poisson* p);
+int poisson_set_labels_device(fs_poisson* p, const uint8_t* d_labels);
+int poisson_solve_device(fs_poisson* p, const double* d_rhs, double* d_x, int method, double tol, int max_iterations,
+                         double inner_tolerance, int inner_precision, fs_poisson_stats* stats);
+int64_t poisson_launches(const fs_poisson* p);
+
 }  // namespace fs

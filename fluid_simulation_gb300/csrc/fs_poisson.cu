@@ -43,6 +43,14 @@ __global__ void k_poisson_rows(Geom g, const uint8_t* __restrict__ lab, const in
     b[t] = rhs[c];
 }
 
+// b[t] = rhs[cell of fluid cell t] (right-hand side given per cell on the device)
+__global__ void k_gather_rhs(const int32_t* __restrict__ cell_of, const int32_t* __restrict__ nfluid,
+                             const double* __restrict__ rhs, double* __restrict__ b)
+{
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < *nfluid) b[t] = rhs[cell_of[t]];
+}
+
 // ---- double vectors ----------------------------------------------------
 
 struct Mat64
@@ -470,6 +478,100 @@ double read_scalar(fs_poisson* p, int slot)
     return v;
 }
 
+// The three methods on the assembled system (right-hand side in p->b), the
+// solution in p->x (fluid-index order).
+int solve_impl(fs_poisson* p, int method, double tol, int max_iterations, double inner_tolerance,
+               int inner_precision, fs_poisson_stats* stats)
+{
+    const Launch L{p->stream, &p->launches, 0};
+    const unsigned nb = blocks(p->ncell);
+    fs_poisson_stats st{};
+    cudaMemsetAsync(p->status, 0, 4, p->stream);
+    cudaEventRecord(p->ev[0], p->stream);
+    const int fp64dots = inner_precision == FS_CG_DOUBLE ? 1 : 0;
+    if (method == FS_POISSON_FP32) {
+        k_to_f32<<<nb, 256, 0, p->stream>>>(p->nfluid, p->b, p->b32);
+        cg_solve(L, p->cg, p->nfluid, p->b32, p->diag32, p->down, p->up, p->flags, p->off32, tol, max_iterations,
+                 fp64dots, p->status);
+        k_add_f32<<<nb, 256, 0, p->stream>>>(p->nfluid, p->cg.x, p->x, 1);
+        p->launches += 2;
+        CgResult r{};
+        cudaMemcpyAsync(&r, p->cg.result, sizeof(r), cudaMemcpyDeviceToHost, p->stream);
+        cudaStreamSynchronize(p->stream);
+        st.inner_iterations = r.iterations;
+        st.outer_iterations = 1;
+    } else if (method == FS_POISSON_FP64) {
+        Cg64Args a{};
+        a.nfluid = p->nfluid;
+        a.b = p->b;
+        a.m = p->m;
+        a.tol = tol;
+        a.maxit = max_iterations;
+        a.x = p->x;
+        a.r = p->cr;
+        a.z = p->cz;
+        a.p = p->cp;
+        a.q = p->cq;
+        a.partials = p->cpart;
+        a.max_chunks = (int)((p->ncell + T - 1) / T);
+        a.barrier = p->barrier64;
+        a.status = p->status;
+        a.result = p->result64;
+        cudaMemsetAsync(p->barrier64, 0, 4, p->stream);
+        void* args[] = {&a};
+        cudaLaunchCooperativeKernel((const void*)k_cg64, dim3(p->grid64), dim3(T), args, 0, p->stream);
+        p->launches += 1;
+        CgResult r{};
+        cudaMemcpyAsync(&r, p->result64, sizeof(r), cudaMemcpyDeviceToHost, p->stream);
+        cudaStreamSynchronize(p->stream);
+        st.inner_iterations = r.iterations;
+        st.outer_iterations = 1;
+    } else {
+        // FP64 iterative refinement around float-vector CG corrections.
+        cudaMemsetAsync(p->x, 0, 8 * (size_t)p->ncell, p->stream);
+        k_copy64<<<nb, 256, 0, p->stream>>>(p->nfluid, p->b, p->r);
+        p->launches += 1;
+        dot64(p, p->b, p->b, 0);
+        const double bb = read_scalar(p, 0);
+        const double thr = tol * tol * bb;
+        double rr = bb;
+        for (int outer = 0; outer < 64; ++outer) {
+            if (!(rr >= thr) || bb == 0.0) break;
+            k_to_f32<<<nb, 256, 0, p->stream>>>(p->nfluid, p->r, p->b32);
+            cg_solve(L, p->cg, p->nfluid, p->b32, p->diag32, p->down, p->up, p->flags, p->off32, inner_tolerance,
+                     max_iterations, fp64dots, p->status);
+            k_add_f32<<<nb, 256, 0, p->stream>>>(p->nfluid, p->cg.x, p->x, 0);
+            k_residual64<<<nb, 256, 0, p->stream>>>(p->m, p->nfluid, p->b, p->x, p->r);
+            p->launches += 3;
+            dot64(p, p->r, p->r, 1);
+            CgResult r{};
+            cudaMemcpyAsync(&r, p->cg.result, sizeof(r), cudaMemcpyDeviceToHost, p->stream);
+            const double rr_new = read_scalar(p, 1);
+            st.inner_iterations += r.iterations;
+            st.outer_iterations = outer + 1;
+            if (r.iterations == 0) break;  // no progress possible
+            rr = rr_new;
+        }
+    }
+    // final FP64 residual of the solution, whatever the method
+    k_residual64<<<nb, 256, 0, p->stream>>>(p->m, p->nfluid, p->b, p->x, p->r);
+    p->launches += 1;
+    dot64(p, p->r, p->r, 1);
+    dot64(p, p->b, p->b, 0);
+    cudaEventRecord(p->ev[1], p->stream);
+    unsigned status = 0;
+    cudaMemcpyAsync(&status, p->status, 4, cudaMemcpyDeviceToHost, p->stream);
+    const double rr = read_scalar(p, 1), bb = read_scalar(p, 0);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_check(e, "fs_poisson_solve");
+    if (status & ST_TIMEOUT) return fail(FS_ERR_TIMEOUT, "a device-side wait of a CG kernel timed out");
+    if (status & ST_TOO_LARGE) return fail(FS_ERR_TOO_LARGE, "too many fluid cells");
+    st.residual = bb > 0 ? std::sqrt(rr / bb) : 0.0;
+    cudaEventElapsedTime(&st.ms, p->ev[0], p->ev[1]);
+    if (stats) *stats = st;
+    return FS_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -586,93 +688,7 @@ FS_API int fs_poisson_solve(fs_poisson* p, int method, double tol, int max_itera
         (method != FS_POISSON_FP32 && method != FS_POISSON_FP64 && method != FS_POISSON_MIXED))
         return fail(FS_ERR_INVALID_ARGUMENT, "invalid Poisson solve");
     cudaSetDevice(p->device);
-    const Launch L{p->stream, &p->launches, 0};
-    const unsigned nb = blocks(p->ncell);
-    fs_poisson_stats st{};
-    cudaMemsetAsync(p->status, 0, 4, p->stream);
-    cudaEventRecord(p->ev[0], p->stream);
-    const int fp64dots = inner_precision == FS_CG_DOUBLE ? 1 : 0;
-    if (method == FS_POISSON_FP32) {
-        k_to_f32<<<nb, 256, 0, p->stream>>>(p->nfluid, p->b, p->b32);
-        cg_solve(L, p->cg, p->nfluid, p->b32, p->diag32, p->down, p->up, p->flags, p->off32, tol, max_iterations,
-                 fp64dots, p->status);
-        k_add_f32<<<nb, 256, 0, p->stream>>>(p->nfluid, p->cg.x, p->x, 1);
-        p->launches += 2;
-        CgResult r{};
-        cudaMemcpyAsync(&r, p->cg.result, sizeof(r), cudaMemcpyDeviceToHost, p->stream);
-        cudaStreamSynchronize(p->stream);
-        st.inner_iterations = r.iterations;
-        st.outer_iterations = 1;
-    } else if (method == FS_POISSON_FP64) {
-        Cg64Args a{};
-        a.nfluid = p->nfluid;
-        a.b = p->b;
-        a.m = p->m;
-        a.tol = tol;
-        a.maxit = max_iterations;
-        a.x = p->x;
-        a.r = p->cr;
-        a.z = p->cz;
-        a.p = p->cp;
-        a.q = p->cq;
-        a.partials = p->cpart;
-        a.max_chunks = (int)((p->ncell + T - 1) / T);
-        a.barrier = p->barrier64;
-        a.status = p->status;
-        a.result = p->result64;
-        cudaMemsetAsync(p->barrier64, 0, 4, p->stream);
-        void* args[] = {&a};
-        cudaLaunchCooperativeKernel((const void*)k_cg64, dim3(p->grid64), dim3(T), args, 0, p->stream);
-        p->launches += 1;
-        CgResult r{};
-        cudaMemcpyAsync(&r, p->result64, sizeof(r), cudaMemcpyDeviceToHost, p->stream);
-        cudaStreamSynchronize(p->stream);
-        st.inner_iterations = r.iterations;
-        st.outer_iterations = 1;
-    } else {
-        // FP64 iterative refinement around float-vector CG corrections.
-        cudaMemsetAsync(p->x, 0, 8 * (size_t)p->ncell, p->stream);
-        k_copy64<<<nb, 256, 0, p->stream>>>(p->nfluid, p->b, p->r);
-        p->launches += 1;
-        dot64(p, p->b, p->b, 0);
-        const double bb = read_scalar(p, 0);
-        const double thr = tol * tol * bb;
-        double rr = bb;
-        for (int outer = 0; outer < 64; ++outer) {
-            if (!(rr >= thr) || bb == 0.0) break;
-            k_to_f32<<<nb, 256, 0, p->stream>>>(p->nfluid, p->r, p->b32);
-            cg_solve(L, p->cg, p->nfluid, p->b32, p->diag32, p->down, p->up, p->flags, p->off32, inner_tolerance,
-                     max_iterations, fp64dots, p->status);
-            k_add_f32<<<nb, 256, 0, p->stream>>>(p->nfluid, p->cg.x, p->x, 0);
-            k_residual64<<<nb, 256, 0, p->stream>>>(p->m, p->nfluid, p->b, p->x, p->r);
-            p->launches += 3;
-            dot64(p, p->r, p->r, 1);
-            CgResult r{};
-            cudaMemcpyAsync(&r, p->cg.result, sizeof(r), cudaMemcpyDeviceToHost, p->stream);
-            const double rr_new = read_scalar(p, 1);
-            st.inner_iterations += r.iterations;
-            st.outer_iterations = outer + 1;
-            if (r.iterations == 0) break;  // no progress possible
-            rr = rr_new;
-        }
-    }
-    // final FP64 residual of the solution, whatever the method
-    k_residual64<<<nb, 256, 0, p->stream>>>(p->m, p->nfluid, p->b, p->x, p->r);
-    p->launches += 1;
-    dot64(p, p->r, p->r, 1);
-    dot64(p, p->b, p->b, 0);
-    cudaEventRecord(p->ev[1], p->stream);
-    unsigned status = 0;
-    cudaMemcpyAsync(&status, p->status, 4, cudaMemcpyDeviceToHost, p->stream);
-    const double rr = read_scalar(p, 1), bb = read_scalar(p, 0);
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return cuda_check(e, "fs_poisson_solve");
-    if (status & ST_TIMEOUT) return fail(FS_ERR_TIMEOUT, "a device-side wait of a CG kernel timed out");
-    if (status & ST_TOO_LARGE) return fail(FS_ERR_TOO_LARGE, "too many fluid cells");
-    st.residual = bb > 0 ? std::sqrt(rr / bb) : 0.0;
-    cudaEventElapsedTime(&st.ms, p->ev[0], p->ev[1]);
-    if (stats) *stats = st;
-    return FS_OK;
+    return solve_impl(p, method, tol, max_iterations, inner_tolerance, inner_precision, stats);
 }
 
 FS_API int fs_poisson_get_solution(fs_poisson* p, double* out)
@@ -689,3 +705,43 @@ FS_API int fs_poisson_get_solution(fs_poisson* p, double* out)
 FS_API int64_t fs_poisson_kernel_launches(const fs_poisson* p) { return p ? p->launches : 0; }
 
 }  // extern "C"
+
+// ---- device-side use by the other solvers of this library ------------------
+
+namespace fs {
+
+cudaStream_t poisson_stream(const fs_poisson* p) { return p->stream; }
+
+int poisson_set_labels_device(fs_poisson* p, const uint8_t* d_labels)
+{
+    const size_t N = (size_t)p->ncell;
+    cudaMemcpyAsync(p->labels, d_labels, N, cudaMemcpyDeviceToDevice, p->stream);
+    cudaMemsetAsync(p->rhs, 0, 8 * N, p->stream);
+    const Launch L{p->stream, &p->launches, 0};
+    fluid_index(L, p->labels, p->ncell, p->fidx, p->cell_of, p->nfluid, p->scan_tmp);
+    k_poisson_rows<<<blocks(p->ncell), 256, 0, p->stream>>>(p->g, p->labels, p->fidx, p->cell_of, p->nfluid, p->rhs,
+                                                            p->b, p->down, p->up, p->flags);
+    p->launches += 1;
+    p->m.down = p->down;
+    p->m.up = p->up;
+    p->m.flags = p->flags;
+    p->ready = true;
+    return cuda_check(cudaStreamSynchronize(p->stream), "Poisson labels");
+}
+
+int poisson_solve_device(fs_poisson* p, const double* d_rhs, double* d_x, int method, double tol, int max_iterations,
+                         double inner_tolerance, int inner_precision, fs_poisson_stats* stats)
+{
+    if (!p->ready) return fail(FS_ERR_INVALID_ARGUMENT, "Poisson labels not set");
+    k_gather_rhs<<<blocks(p->ncell), 256, 0, p->stream>>>(p->cell_of, p->nfluid, d_rhs, p->b);
+    p->launches += 1;
+    const int rc = solve_impl(p, method, tol, max_iterations, inner_tolerance, inner_precision, stats);
+    if (rc) return rc;
+    k_scatter64<<<blocks(p->ncell), 256, 0, p->stream>>>(p->g, p->fidx, p->nfluid, p->x, d_x);
+    p->launches += 1;
+    return cuda_check(cudaGetLastError(), "Poisson solve");
+}
+
+int64_t poisson_launches(const fs_poisson* p) { return p->launches; }
+
+}  // namespace fs

@@ -185,3 +185,40 @@ def batch_scenes(n: int = 512, seed: int = 0xC3, min_side: int = 32, max_side: i
                          description="batch member %d: %dx%d, block %dx%d, %d discs" % (s, side, side, w, h, ndisc),
                          meta={"block": [i0, i0 + w, j0, j0 + h], "discs": ndisc, "seed": seed}))
     return out
+
+
+def normal01(seed: int, n: int) -> np.ndarray:
+    """n N(0, 1) doubles by Box-Muller on two SplitMix64 streams."""
+    u1 = uniform01(seed, n).astype(np.float64)
+    u2 = uniform01(seed ^ 0xA5A5A5A5, n).astype(np.float64)
+    return np.sqrt(-2.0 * np.log(1.0 - u1)) * np.cos(2.0 * np.pi * u2)
+
+
+def smoke_problem(n: int = 256, seed: int = 0xC4, sigma: float = 20.0, shift: tuple[float, float] = (16.0, 8.0),
+                  kmax: int = 8):
+    """Differentiable-smoke initial state on an n x n unit-cell grid: a Gaussian
+    density blob (sigma cells) at the centre, a target blob shifted by `shift`
+    cells, and a velocity of random Fourier modes 1 <= |k| <= kmax (seeded
+    N(0, 1) cosine and sine coefficients per component) normalised to RMS 1
+    and rounded to float32.  Returns (u, v, density, target) as float64
+    arrays of shape (n, n), u(i, j) at (i, j + 1/2), v(i, j) at (i + 1/2, j)."""
+    jj, ii = np.meshgrid(np.arange(n, dtype=np.float64), np.arange(n, dtype=np.float64), indexing="ij")
+    c = n / 2.0
+    d0 = np.exp(-((ii + 0.5 - c) ** 2 + (jj + 0.5 - c) ** 2) / (2 * sigma * sigma))
+    tx, ty = c + shift[0], c + shift[1]
+    target = np.exp(-((ii + 0.5 - tx) ** 2 + (jj + 0.5 - ty) ** 2) / (2 * sigma * sigma))
+    modes = [(kx, ky) for kx in range(-kmax, kmax + 1) for ky in range(0, kmax + 1)
+             if 1 <= kx * kx + ky * ky <= kmax * kmax and (ky > 0 or kx > 0)]
+    coef = normal01(seed, 4 * len(modes)).reshape(len(modes), 4)
+    L = float(n)
+    u = np.zeros((n, n))
+    v = np.zeros((n, n))
+    for (kx, ky), (a, b, cc, d) in zip(modes, coef):
+        ph_u = 2 * np.pi * (kx * ii + ky * (jj + 0.5)) / L
+        ph_v = 2 * np.pi * (kx * (ii + 0.5) + ky * jj) / L
+        u += a * np.cos(ph_u) + b * np.sin(ph_u)
+        v += cc * np.cos(ph_v) + d * np.sin(ph_v)
+    rms = np.sqrt((np.mean(u * u) + np.mean(v * v)) / 2.0)
+    u = (u / rms).astype(np.float32).astype(np.float64)
+    v = (v / rms).astype(np.float32).astype(np.float64)
+    return u, v, d0.astype(np.float32).astype(np.float64), target.astype(np.float32).astype(np.float64)

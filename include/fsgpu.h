@@ -283,6 +283,61 @@ FS_API int fs_batch_set_graphs(fs_batch* b, int enable);
 FS_API void* fs_batch_get_stream(fs_batch* b);
 FS_API int64_t fs_batch_kernel_launches(fs_batch* b);
 
+/* Differentiable smoke (no counterpart in the reference, whose
+ * semi-Lagrangian step scatters, src/FluidSolver.cpp:709-772): a passive
+ * density and the velocity advected by gathering semi-Lagrangian steps
+ * (bilinear sampling as Grid::valueInterpolated, include/Grid.h:117-144;
+ * back-trace by explicit Euler, the midpoint rule or RK3 as
+ * include/OdeSolver.h:102-113), faces touching a solid cell closed, then the
+ * pressure projection (FluidSolver::pressureSolve's matrix, solved by
+ * projection_method to cg_tolerance).  The grid has a solid border.
+ * fs_smoke_forward runs `steps` steps from the state of fs_smoke_set_state
+ * and returns L = ||density - target||_2; fs_smoke_backward returns dL/d(the
+ * initial u, v, density) from a hand-written adjoint, recomputing the states
+ * between checkpoints stored every checkpoint_every steps.  Fields are float
+ * or double on the device (precision); adjoints accumulate in double.  Host
+ * arrays are size_x * size_y doubles, row-major: u(i, j) on the face at
+ * (i h, (j + 1/2) h), v(i, j) at ((i + 1/2) h, j h), density at cell centres. */
+#define FS_INTEGRATOR_EULER 0
+#define FS_INTEGRATOR_RK2 1
+#define FS_INTEGRATOR_RK3 2
+#define FS_SMOKE_FP32 0
+#define FS_SMOKE_FP64 1
+
+typedef struct fs_smoke fs_smoke;
+typedef struct fs_smoke_config
+{
+    int size_x, size_y;
+    float length_x, length_y;  /* square cells: length_x / size_x == length_y / size_y */
+    float dt;
+    int integrator;            /* FS_INTEGRATOR_* */
+    int precision;             /* FS_SMOKE_FP32 / FS_SMOKE_FP64 */
+    int projection_method;     /* FS_POISSON_* */
+    double cg_tolerance;       /* relative residual of each projection */
+    int cg_max_iterations;
+    double inner_tolerance;    /* FS_POISSON_MIXED: tolerance of each float correction */
+    int checkpoint_every;      /* steps between stored states */
+    int device;
+    int reserved[8];
+} fs_smoke_config;
+
+/* Defaults: unit cells, dt 0.01, RK2, FP32 fields, mixed-precision projection
+ * to 1e-10, checkpoints every 8 steps. */
+FS_API void fs_smoke_config_init(fs_smoke_config* c, int size_x, int size_y);
+FS_API int fs_smoke_create(const fs_smoke_config* cfg, fs_smoke** out);
+FS_API int fs_smoke_destroy(fs_smoke* s);
+/* NULL s: the message of the last failed fs_smoke_create on this thread. */
+FS_API const char* fs_smoke_last_error(const fs_smoke* s);
+/* size_x * size_y uint8 (non-zero = solid) added to the solid border, or NULL. */
+FS_API int fs_smoke_set_solid_mask(fs_smoke* s, const uint8_t* mask);
+FS_API int fs_smoke_set_state(fs_smoke* s, const double* u, const double* v, const double* density);
+FS_API int fs_smoke_set_target(fs_smoke* s, const double* target);
+FS_API int fs_smoke_forward(fs_smoke* s, int steps, double* loss);
+/* The state after the last fs_smoke_forward. */
+FS_API int fs_smoke_get_state(fs_smoke* s, double* u, double* v, double* density);
+FS_API int fs_smoke_backward(fs_smoke* s, double* grad_u, double* grad_v, double* grad_density);
+FS_API int64_t fs_smoke_kernel_launches(const fs_smoke* s);
+
 /* Allocation-free pressure solve.  No counterpart in the reference: this is
  * FluidSolver::pressureSolve's fluid indexing, assembly and conjugate gradient
  * for callers that cannot allocate device memory -- an application that owns
