@@ -93,6 +93,12 @@ SIGNATURES = {
     "fs_get_pressure": (_i, [_vp, _vp]),
     "fs_step": (_i, [_vp, _i, _f]),
     "fs_phase": (_i, [_vp, _i, _f]),
+    "fs_add_fluid_source": (_i, [_vp, _f, _f, _f, _f, _f, _f, _f, _f, _f, _i]),
+    "fs_update": (_i, [_vp, _f]),
+    "fs_clear_fluid_sources": (_i, [_vp]),
+    "fs_num_fluid_sources": (_i, [_vp, C.POINTER(_i)]),
+    "fs_set_fluid_source_state": (_i, [_vp, _i, _f, _i]),
+    "fs_reset_particles": (_i, [_vp]),
     "fs_synchronize": (_i, [_vp]),
     "fs_get_stats": (_i, [_vp, C.POINTER(fs_step_stats)]),
     "fs_set_timing": (_i, [_vp, _i]),
@@ -305,6 +311,21 @@ class FluidSim:
         out = np.empty((self.ny, self.nx), np.float32)
         self._check(self.lib.fs_get_pressure(self.h, _ptr(out)))
         return out
+
+    # fluid sources (FluidDomain::addFluidSource / update / clearFluidSources)
+    def add_fluid_source(self, x_min, x_max, y_min, y_max, delta_x, delta_y, x_velocity, y_velocity, time_step,
+                         max_spawns) -> None:
+        self._check(self.lib.fs_add_fluid_source(self.h, x_min, x_max, y_min, y_max, delta_x, delta_y, x_velocity,
+                                                 y_velocity, time_step, int(max_spawns)))
+
+    def update(self, dt: float) -> None:
+        self._check(self.lib.fs_update(self.h, dt))
+
+    def clear_fluid_sources(self) -> None:
+        self._check(self.lib.fs_clear_fluid_sources(self.h))
+
+    def reset_particles(self) -> None:
+        self._check(self.lib.fs_reset_particles(self.h))
 
     # stepping
     def step(self, method: int, dt: float) -> None:

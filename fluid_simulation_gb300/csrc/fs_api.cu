@@ -42,6 +42,18 @@ uint32_t float_bits(float f)
     return b;
 }
 
+// FluidSource (src/FluidDomain.cpp:3-52): the timing state on the host, the
+// spawn lattice's coordinates -- the reference's float-accumulated loop
+// variables, expanded once -- on the device.
+struct DevSource
+{
+    float vx, vy, time_step, time_since_last;
+    int max_spawns, n_spawns;
+    int nx, ny;
+    float* d_xs;
+    float* d_ys;
+};
+
 }  // namespace
 
 struct fs_handle
@@ -104,6 +116,7 @@ struct fs_handle
     cudaEvent_t ev[FS_NUM_TIMED + 1] = {};
     int64_t launches = 0;
     std::vector<GraphEntry> graph_cache;
+    std::vector<DevSource> sources;
     std::string err;
 
     Launch L() { return Launch{stream, &launches, 0}; }
@@ -334,6 +347,10 @@ void destroy_all(fs_handle* h)
                     h->cg.p, h->cg.q, h->cg.partials, h->cg.barrier, h->cg.result, h->cg_b, h->cg_down, h->cg_up,
                     h->cg_flags, h->d_nfluid, h->d_status, h->d_warn, h->scan_tmp};
     for (void* p : ptrs) cudaFree(p);
+    for (DevSource& src : h->sources) {
+        cudaFree(src.d_xs);
+        cudaFree(src.d_ys);
+    }
     for (auto& e : h->ev)
         if (e) cudaEventDestroy(e);
     if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
@@ -838,10 +855,125 @@ int fs_step(fs_handle* h, int method, float dt)
         run_step(h, method, dt);
         return check_launch(h, "step");
     }
+    if (h->graph_cache.size() >= 8) {  // particle counts that changed (fluid sources) leave unused graphs
+        cudaGraphExecDestroy(h->graph_cache.front().exec);
+        h->graph_cache.erase(h->graph_cache.begin());
+    }
     h->graph_cache.push_back(ge);
     e = cudaGraphLaunch(ge.exec, h->stream);
     if (e != cudaSuccess) return cuda_fail(h, e, "graph launch");
     h->launches += ge.kernels;
+    return FS_OK;
+}
+
+int fs_add_fluid_source(fs_handle* h, float x_min, float x_max, float y_min, float y_max, float delta_x,
+                        float delta_y, float x_velocity, float y_velocity, float time_step, int max_spawns)
+{
+    if (!h) return FS_ERR_INVALID_ARGUMENT;
+    // the spawn lattice of FluidSource::update (src/FluidDomain.cpp:37-48):
+    // increments delta / 2.5 rounded to float, loop variables accumulated in float
+    const float x_incr = (float)(delta_x / 2.5);
+    const float y_incr = (float)(delta_y / 2.5);
+    constexpr size_t kMaxLattice = (size_t)1 << 26;
+    std::vector<float> xs, ys;
+    for (float x = x_min; x < x_max; x += x_incr) {
+        xs.push_back(x);
+        if (xs.size() > kMaxLattice)  // the reference would not stop (an increment too small to advance x)
+            return fail(h, FS_ERR_INVALID_ARGUMENT, "fluid source lattice does not end in x");
+    }
+    for (float y = y_min; y < y_max; y += y_incr) {
+        ys.push_back(y);
+        if (ys.size() > kMaxLattice) return fail(h, FS_ERR_INVALID_ARGUMENT, "fluid source lattice does not end in y");
+    }
+    if (!xs.empty() && !ys.empty() && xs.size() * ys.size() > (size_t)INT32_MAX)
+        return fail(h, FS_ERR_TOO_LARGE, "fluid source spawns more than 2^31-1 particles");
+    cudaSetDevice(h->device);
+    DevSource src{};
+    src.vx = x_velocity;
+    src.vy = y_velocity;
+    src.time_step = time_step;
+    src.time_since_last = 0.0f;
+    src.max_spawns = max_spawns;
+    src.n_spawns = 0;
+    src.nx = (int)xs.size();
+    src.ny = (int)ys.size();
+    cudaError_t e = dalloc(&src.d_xs, xs.size());
+    if (e == cudaSuccess) e = dalloc(&src.d_ys, ys.size());
+    if (e == cudaSuccess && !xs.empty())
+        e = cudaMemcpyAsync(src.d_xs, xs.data(), 4 * xs.size(), cudaMemcpyHostToDevice, h->stream);
+    if (e == cudaSuccess && !ys.empty())
+        e = cudaMemcpyAsync(src.d_ys, ys.data(), 4 * ys.size(), cudaMemcpyHostToDevice, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) {
+        cudaFree(src.d_xs);
+        cudaFree(src.d_ys);
+        return cuda_fail(h, e, "fluid source");
+    }
+    h->sources.push_back(src);
+    return FS_OK;
+}
+
+int fs_update(fs_handle* h, float dt)
+{
+    if (!h) return FS_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(h->device);
+    for (DevSource& src : h->sources) {
+        // FluidSource::update (src/FluidDomain.cpp:29-52)
+        if (src.max_spawns != -1 && src.n_spawns >= src.max_spawns) continue;
+        if (src.time_since_last >= src.time_step) {
+            const int64_t k = (int64_t)src.nx * src.ny;
+            if (k > 0) {
+                const int64_t total = h->n_part + k;
+                if (total > (int64_t)INT32_MAX) return fail(h, FS_ERR_TOO_LARGE, "more than 2^31-1 particles");
+                const cudaError_t e = ensure_particle_capacity(h, total);
+                if (e != cudaSuccess) return cuda_fail(h, e, "particle storage");
+                spawn_lattice(h->L(), src.d_xs, src.nx, src.d_ys, src.ny, src.vx, src.vy, h->px + h->n_part,
+                              h->py + h->n_part, h->pvx + h->n_part, h->pvy + h->n_part);
+                h->n_part = total;
+                const int rc = check_launch(h, "fluid source");
+                if (rc) return rc;
+            }
+            src.time_since_last = 0;
+            src.n_spawns++;
+        }
+        src.time_since_last += dt;
+    }
+    return FS_OK;
+}
+
+int fs_clear_fluid_sources(fs_handle* h)
+{
+    if (!h) return FS_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(h->device);
+    cudaStreamSynchronize(h->stream);
+    for (DevSource& src : h->sources) {
+        cudaFree(src.d_xs);
+        cudaFree(src.d_ys);
+    }
+    h->sources.clear();
+    return FS_OK;
+}
+
+int fs_set_fluid_source_state(fs_handle* h, int index, float time_since_last, int n_spawns)
+{
+    if (!h || index < 0 || index >= (int)h->sources.size())
+        return h ? fail(h, FS_ERR_INVALID_ARGUMENT, "no such fluid source") : FS_ERR_INVALID_ARGUMENT;
+    h->sources[index].time_since_last = time_since_last;
+    h->sources[index].n_spawns = n_spawns;
+    return FS_OK;
+}
+
+int fs_num_fluid_sources(fs_handle* h, int* n)
+{
+    if (!h || !n) return FS_ERR_INVALID_ARGUMENT;
+    *n = (int)h->sources.size();
+    return FS_OK;
+}
+
+int fs_reset_particles(fs_handle* h)
+{
+    if (!h) return FS_ERR_INVALID_ARGUMENT;
+    h->n_part = 0;  // FluidDomain::resetParticleSet (src/FluidDomain.cpp:94-97)
     return FS_OK;
 }
 

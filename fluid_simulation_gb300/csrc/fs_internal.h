@@ -156,6 +156,9 @@ void g2p_advect(const Launch& L, const Domain& d, int g2p_mode, int adv_mode, fl
 void p2g_positions(const Launch& L, const Domain& d, const float* px, const float* py, float* yu, float* xv);
 void sl_faces(const Launch& L, const Domain& d, const uint8_t* lab, const float* uf, const float* vf, float dt,
               float* ux, float* uy, float* uval, uint8_t* uok, float* vx, float* vy, float* vval, uint8_t* vok);
+// Appends nx * ny particles (xs[i], ys[j], vx, vy), j outer, i inner.
+void spawn_lattice(const Launch& L, const float* xs, int nx, const float* ys, int ny, float vx, float vy, float* px,
+                   float* py, float* pvx, float* pvy);
 void aos_to_soa(const Launch& L, const float* xyuv, int64_t n, float* px, float* py, float* pvx, float* pvy);
 void soa_to_aos(const Launch& L, const float* px, const float* py, const float* pvx, const float* pvy, int64_t n,
                 float* xyuv);

@@ -131,6 +131,20 @@ struct SLFaces
     }
 };
 
+// MarkerParticle(x, y, vx, vy) for y over ys (outer) and x over xs (inner),
+// the loop order of FluidSource::update (src/FluidDomain.cpp:39-47).
+__global__ void k_spawn_lattice(const float* __restrict__ xs, int nx, const float* __restrict__ ys, int64_t n,
+                                float vx, float vy, float* __restrict__ px, float* __restrict__ py,
+                                float* __restrict__ pvx, float* __restrict__ pvy)
+{
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    px[t] = xs[t % nx];
+    py[t] = ys[t / nx];
+    pvx[t] = vx;
+    pvy[t] = vy;
+}
+
 __global__ void k_aos_to_soa(const float4* __restrict__ in, int64_t n, float* __restrict__ px,
                              float* __restrict__ py, float* __restrict__ pvx, float* __restrict__ pvy)
 {
@@ -172,6 +186,15 @@ void sl_faces(const Launch& L, const Domain& d, const uint8_t* lab, const float*
               float* uy, float* uval, uint8_t* uok, float* vx, float* vy, float* vval, uint8_t* vok)
 {
     each_cell(L, d, SLFaces{lab, uf, vf, dt, ux, uy, uval, uok, vx, vy, vval, vok});
+}
+
+void spawn_lattice(const Launch& L, const float* xs, int nx, const float* ys, int ny, float vx, float vy, float* px,
+                   float* py, float* pvx, float* pvy)
+{
+    const int64_t n = (int64_t)nx * ny;
+    if (n <= 0) return;
+    k_spawn_lattice<<<blocks_for(n), TPB, 0, L.stream>>>(xs, nx, ys, n, vx, vy, px, py, pvx, pvy);
+    L.count();
 }
 
 void aos_to_soa(const Launch& L, const float* xyuv, int64_t n, float* px, float* py, float* pvx, float* pvy)

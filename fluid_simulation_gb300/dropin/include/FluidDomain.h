@@ -27,6 +27,7 @@ private:
     BBox<MyFloat> _area;
     MyFloat _x_velocity, _y_velocity, _delta_x, _delta_y, _time_step, _time_since_last;
     int _max_spawns, _n_spawns;
+    friend class FluidDomain;  // not in the reference: hands the source to the device
 };
 
 class FluidDomain : public GridInterface

@@ -70,6 +70,8 @@ public:
     void attach(fs_handle* h);
     void push();
     void invalidate();
+    // n particles now on the device (sources appended there); the mirror follows lazily
+    void deviceAppended(std::size_t n);
 
 private:
     void pull() const;

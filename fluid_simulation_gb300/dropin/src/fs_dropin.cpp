@@ -210,6 +210,14 @@ void MarkerParticleSet::invalidate()
     if (_h) _stale = true;
 }
 
+// The next host access downloads all n: the device holds every particle.
+void MarkerParticleSet::deviceAppended(std::size_t n)
+{
+    _particles.resize(n);
+    _synced = n;
+    _stale = true;
+}
+
 // Appends without downloading: the device keeps its newer copy of the
 // particles before this one, and only the appended ones are uploaded.
 void MarkerParticleSet::addParticle(MarkerParticle p) { _particles.push_back(p); }
@@ -358,15 +366,35 @@ FluidDomain::FluidDomain(int size_x, int size_y, MyFloat length_x, MyFloat lengt
 
 FluidDomain::~FluidDomain() { fs_destroy(_h); }
 
-void FluidDomain::addFluidSource(FluidSource fluid_source) { _fluid_sources.push_back(fluid_source); }
-
-// src/FluidDomain.cpp:80-87.
-void FluidDomain::update(MyFloat dt)
+// src/FluidDomain.cpp:75-78; the source (with its timing state) lives on the
+// device, which spawns its particles there.
+void FluidDomain::addFluidSource(FluidSource s)
 {
-    for (size_t i = 0; i < _fluid_sources.size(); ++i) _fluid_sources[i].update(_particle_set, dt);
+    const BBox<MyFloat>& a = s._area;
+    check(_h, fs_add_fluid_source(_h, a.x_min, a.x_max, a.y_min, a.y_max, s._delta_x, s._delta_y, s._x_velocity,
+                                  s._y_velocity, s._time_step, s._max_spawns));
+    int n = 0;
+    check(_h, fs_num_fluid_sources(_h, &n));
+    check(_h, fs_set_fluid_source_state(_h, n - 1, s._time_since_last, s._n_spawns));
+    _fluid_sources.push_back(s);
 }
 
-void FluidDomain::clearFluidSources() { _fluid_sources.clear(); }
+// src/FluidDomain.cpp:80-87: every source's FluidSource::update, on the device.
+void FluidDomain::update(MyFloat dt)
+{
+    _particle_set.push();  // host additions first, as they came first
+    int64_t before = 0, after = 0;
+    check(_h, fs_num_particles(_h, &before));
+    check(_h, fs_update(_h, dt));
+    check(_h, fs_num_particles(_h, &after));
+    if (after != before) _particle_set.deviceAppended(static_cast<std::size_t>(after));
+}
+
+void FluidDomain::clearFluidSources()
+{
+    check(_h, fs_clear_fluid_sources(_h));
+    _fluid_sources.clear();
+}
 void FluidDomain::resetParticleSet() { _particle_set.clear(); }
 
 // src/FluidDomain.cpp:99-102.

@@ -203,6 +203,25 @@ FS_API int fs_set_stream(fs_handle* h, void* stream);
 /* Number of this library's kernel launches queued so far on h. */
 FS_API int64_t fs_kernel_launches(fs_handle* h);
 
+/* Fluid sources on the device: FluidDomain::addFluidSource / update /
+ * clearFluidSources / resetParticleSet (src/FluidDomain.cpp:3-52,75-97).  A
+ * source spawns, every time_step of accumulated dt and at most max_spawns
+ * times (-1: unlimited), a lattice of spacing delta / 2.5 over
+ * [x_min, x_max) x [y_min, y_max) with velocity (x_velocity, y_velocity),
+ * appended in the reference's loop order (y outer, x inner, float-accumulated
+ * coordinates).  The lattice is written by a kernel into device memory: no
+ * particle crosses the host.  A lattice whose increment cannot advance its
+ * coordinate (the reference would loop forever) is FS_ERR_INVALID_ARGUMENT. */
+FS_API int fs_add_fluid_source(fs_handle* h, float x_min, float x_max, float y_min, float y_max, float delta_x,
+                               float delta_y, float x_velocity, float y_velocity, float time_step, int max_spawns);
+FS_API int fs_update(fs_handle* h, float dt);
+FS_API int fs_clear_fluid_sources(fs_handle* h);
+FS_API int fs_num_fluid_sources(fs_handle* h, int* n);
+/* The timing state of source `index` (in order of addition), for a FluidSource
+ * copy that was already updated: its time since the last spawn and spawns so far. */
+FS_API int fs_set_fluid_source_state(fs_handle* h, int index, float time_since_last, int n_spawns);
+FS_API int fs_reset_particles(fs_handle* h);
+
 /* Pressure projection alone (no particles): the
  * Poisson system of FluidSolver::pressureSolve (src/FluidSolver.cpp:363-425)
  * built from a label grid (FS_LIQUID = unknown, FS_AIR = pressure 0,

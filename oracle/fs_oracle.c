@@ -1063,6 +1063,9 @@ void fso_update(fso_sim* s, float dt)
     }
 }
 
+/* FluidDomain::clearFluidSources (FluidDomain.cpp:89-92). */
+void fso_clear_sources(fso_sim* s) { s->n_src = 0; }
+
 
 /* ---- pressure projection alone (the GPU's fs_poisson_*) ------------------- */
 

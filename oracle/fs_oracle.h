@@ -116,6 +116,8 @@ void fso_add_source(fso_sim* s, float x_min, float x_max, float y_min, float y_m
                     float delta_y, float x_velocity, float y_velocity, float time_step,
                     int max_spawns);
 void fso_update(fso_sim* s, float dt);
+/* FluidDomain::clearFluidSources (FluidDomain.cpp:89-92). */
+void fso_clear_sources(fso_sim* s);
 
 /* Pressure projection alone (the GPU's fs_poisson_*), restatement only:
  * method 0 float CG (dots per inner_precision), 1 double CG, 2 double

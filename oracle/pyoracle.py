@@ -67,6 +67,7 @@ def _lib(kind: str) -> C.CDLL:
         "fso_phase": (i, [vp, i, f]),
         "fso_add_source": (None, [vp, f, f, f, f, f, f, f, f, f, i]),
         "fso_update": (None, [vp, f]),
+        "fso_clear_sources": (None, [vp]),
         "fso_kind": (C.c_char_p, []),
         "fso_poisson_solve": (i, [i, i, f, f, vp, vp, i, d, i, d, i, vp, C.POINTER(i), C.POINTER(i),
                                   C.POINTER(d)]),
@@ -213,6 +214,9 @@ class OracleSim:
 
     def update(self, dt: float) -> None:
         self.lib.fso_update(self.h, dt)
+
+    def clear_sources(self) -> None:
+        self.lib.fso_clear_sources(self.h)
 
     def state(self) -> dict[str, np.ndarray]:
         """Every observable array, for comparisons."""

@@ -367,4 +367,6 @@ void fso_add_source(fso_sim* s, float x_min, float x_max, float y_min, float y_m
 
 void fso_update(fso_sim* s, float dt) { s->domain.update(dt); }
 
+void fso_clear_sources(fso_sim* s) { s->domain.clearFluidSources(); }
+
 }  // extern "C"

@@ -84,9 +84,10 @@ def test_picflip_200_steps_bit_exact_with_graphs(precision):
             assert st["cg_residual"] == pytest.approx(err, rel=1e-12, abs=0)
 
 
-@pytest.mark.parametrize("case", sorted(c for c in mg.CASES if c != "picflip_source64"))
+@pytest.mark.parametrize("case", sorted(mg.CASES))
 def test_against_reference_fixtures(case, golden_dir):
-    """The GPU against the states recorded from the reference's own code."""
+    """The GPU against the states recorded from the reference's own code
+    (the fluid-source case spawns its particles on the device)."""
     ref = np.load(os.path.join(golden_dir, case + ".npz"))
     method, steps, scene, opt = mg.CASES[case]
     sc = scenes.dam_break_small()
@@ -94,8 +95,13 @@ def test_against_reference_fixtures(case, golden_dir):
                      cg_tolerance=sc.cg_tolerance, cg_max_iterations=sc.cg_max_iterations)
     if "disc" in opt:
         g.set_solid_mask(scenes.disc_mask(sc.size_x, sc.size_y, *opt["disc"]))
-    g.set_particles(sc.particles)
+    if scene == "source":
+        g.add_fluid_source(2.0, 10.0, 40.0, 50.0, 1.0, 1.0, 3.0, 0.0, 0.05, 5)
+    else:
+        g.set_particles(sc.particles)
     for k in range(1, max(steps) + 1):
+        if scene == "source":
+            g.update(sc.dt)
         g.step(method, sc.dt)
         if k in steps:
             st = g.state()
@@ -233,3 +239,37 @@ def test_p2g_on_4096_grid_reaches_the_last_cells():
         a, b = g.grid(w), o.grid(w)
         assert np.array_equal(a.view(np.uint32), b.view(np.uint32)), w
         assert np.count_nonzero(a[n - 3:, n - 3:]) > 0
+
+
+def test_fluid_sources_on_device_match_oracle():
+    """Two sources (one unlimited, one limited, odd spacings whose float
+    accumulation matters) on top of existing particles, with a clear and a
+    particle reset midway."""
+    sc = scenes.dam_break_small()
+    g, o = pair(sc, cg_maxit=400)
+    args = [(3.3, 11.1, 44.0, 52.5, 0.7, 1.3, 2.5, -1.0, 0.02, -1), (40.0, 47.0, 20.0, 30.0, 1.1, 0.9, 0.0, 0.0, 0.05, 3)]
+    for a in args:
+        g.add_fluid_source(*a)
+        o.add_source(*a)
+    for k in range(40):
+        if k == 25:
+            g.clear_fluid_sources()
+            o.clear_sources()
+            g.add_fluid_source(*args[0])
+            o.add_source(*args[0])
+        if k == 30:
+            g.reset_particles()
+            o.set_particles(np.zeros((0, 4), np.float32))
+        g.update(sc.dt)
+        o.update(sc.dt)
+        g.step(fsg.STEP_PICFLIP, sc.dt)
+        o.step(po.STEP_PICFLIP, sc.dt)
+        assert g.num_particles() == len(o.particles()), k
+        assert_same(g.state(), o.state(), where="source step %d" % k)
+
+
+def test_fluid_source_lattice_that_cannot_advance_is_rejected():
+    g = fsg.FluidSim(16, 16, 16.0, 16.0, 1.0, 0.0)
+    with pytest.raises(fsg.FsError) as e:
+        g.add_fluid_source(1.0e8, 1.0e8 + 64.0, 1.0, 2.0, 1.0, 1.0, 0.0, 0.0, 0.0, 1)
+    assert e.value.code == 1

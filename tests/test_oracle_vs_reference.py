@@ -101,3 +101,24 @@ def test_non_square_cells_rejected_like_reference():
     for kind in ("restatement", "reference"):
         s = po.OracleSim(kind, 32, 16, 32.0, 32.0, 0.005, 0.05)
         assert s.step(po.STEP_PICFLIP, 0.005) == -1
+
+
+def test_clear_sources_matches_reference():
+    """FluidDomain::clearFluidSources between spawns: restatement == reference."""
+    sims = []
+    for kind in ("restatement", "reference"):
+        sc = scenes.dam_break_small()
+        s = po.OracleSim(kind, sc.size_x, sc.size_y, sc.length_x, sc.length_y, sc.density, sc.pic_ratio)
+        s.set_cg(sc.cg_tolerance, 400)
+        s.add_source(3.3, 11.1, 44.0, 52.5, 0.7, 1.3, 2.5, -1.0, 0.02, -1)
+        sims.append(s)
+    for k in range(12):
+        for s in sims:
+            if k == 6:
+                s.clear_sources()
+                s.add_source(40.0, 47.0, 20.0, 30.0, 1.1, 0.9, 0.0, 0.0, 0.05, 3)
+            s.update(0.005)
+            assert s.step(po.STEP_PICFLIP, 0.005) == 0
+        a, b = sims[0].state(), sims[1].state()
+        for key in a:
+            assert np.array_equal(a[key].view(np.uint8), b[key].view(np.uint8)), (k, key)
