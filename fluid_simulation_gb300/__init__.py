@@ -99,6 +99,10 @@ SIGNATURES = {
     "fs_num_fluid_sources": (_i, [_vp, C.POINTER(_i)]),
     "fs_set_fluid_source_state": (_i, [_vp, _i, _f, _i]),
     "fs_reset_particles": (_i, [_vp]),
+    "fs_snapshot": (_i, [_vp, C.POINTER(_vp)]),
+    "fs_restore": (_i, [_vp, _vp]),
+    "fs_snapshot_destroy": (_i, [_vp]),
+    "fs_debug_set_cg_barrier_fault": (_i, [_vp, _i, _d]),
     "fs_synchronize": (_i, [_vp]),
     "fs_get_stats": (_i, [_vp, C.POINTER(fs_step_stats)]),
     "fs_set_timing": (_i, [_vp, _i]),
@@ -327,6 +331,15 @@ class FluidSim:
     def reset_particles(self) -> None:
         self._check(self.lib.fs_reset_particles(self.h))
 
+    # snapshots
+    def snapshot(self) -> "Snapshot":
+        p = C.c_void_p()
+        self._check(self.lib.fs_snapshot(self.h, C.byref(p)))
+        return Snapshot(self.lib, p)
+
+    def restore(self, snap: "Snapshot") -> None:
+        self._check(self.lib.fs_restore(self.h, snap.p))
+
     # stepping
     def step(self, method: int, dt: float) -> None:
         self._check(self.lib.fs_step(self.h, method, dt))
@@ -361,6 +374,24 @@ class FluidSim:
         s["pressure"] = self.pressure()
         s["particles"] = self.particles()
         return s
+
+
+class Snapshot:
+    """A device copy of a FluidSim's state (fs_snapshot); freed with the object."""
+
+    def __init__(self, lib: C.CDLL, p: C.c_void_p):
+        self.lib, self.p = lib, p
+
+    def close(self) -> None:
+        if getattr(self, "p", None):
+            self.lib.fs_snapshot_destroy(self.p)
+            self.p = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def scene_config(lib: C.CDLL, sc, device: int = 0) -> fs_config:

@@ -122,6 +122,19 @@ struct fs_handle
     Launch L() { return Launch{stream, &launches, 0}; }
 };
 
+// A device copy of a handle's simulation state (fs_snapshot / fs_restore).
+struct fs_saved_state
+{
+    const fs_handle* owner = nullptr;
+    int64_t ncell = 0, n_part = 0;
+    int front = 0, vfront = 0;
+    unsigned char* cells = nullptr;  // cell arrays, one after another
+    float* parts = nullptr;          // x, y, vx, vy
+    unsigned char* misc = nullptr;   // nfluid, CG result, warnings
+    std::vector<float> src_time;
+    std::vector<int> src_spawns;
+};
+
 namespace {
 
 int fail(fs_handle* h, int code, const std::string& msg)
@@ -974,6 +987,125 @@ int fs_reset_particles(fs_handle* h)
 {
     if (!h) return FS_ERR_INVALID_ARGUMENT;
     h->n_part = 0;  // FluidDomain::resetParticleSet (src/FluidDomain.cpp:94-97)
+    return FS_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+// The cell arrays a snapshot holds: {pointer, bytes per cell}.
+std::vector<std::pair<void*, size_t>> snapshot_cells(fs_handle* h)
+{
+    return {{h->u[0], 4}, {h->u[1], 4}, {h->v[0], 4},   {h->v[1], 4},   {h->u_prev, 4},  {h->v_prev, 4},
+            {h->u_diff, 4}, {h->v_diff, 4}, {h->labels, 1}, {h->vmx[0], 1}, {h->vmx[1], 1}, {h->vmy[0], 1},
+            {h->vmy[1], 1}, {h->fidx, 4},  {h->counts8, 1}, {h->cg.x, 4}};
+}
+
+cudaError_t copy_snapshot(fs_handle* h, fs_saved_state* sn, bool save)
+{
+    cudaError_t e = cudaSuccess;
+    size_t off = 0;
+    for (auto& a : snapshot_cells(h)) {
+        const size_t bytes = a.second * (size_t)h->ncell;
+        if (e == cudaSuccess)
+            e = save ? cudaMemcpyAsync(sn->cells + off, a.first, bytes, cudaMemcpyDeviceToDevice, h->stream)
+                     : cudaMemcpyAsync(a.first, sn->cells + off, bytes, cudaMemcpyDeviceToDevice, h->stream);
+        off += (bytes + 255) / 256 * 256;
+    }
+    float* P[4] = {h->px, h->py, h->pvx, h->pvy};
+    const size_t pb = 4 * (size_t)sn->n_part;
+    for (int k = 0; k < 4 && e == cudaSuccess && pb; ++k)
+        e = save ? cudaMemcpyAsync(sn->parts + k * sn->n_part, P[k], pb, cudaMemcpyDeviceToDevice, h->stream)
+                 : cudaMemcpyAsync(P[k], sn->parts + k * sn->n_part, pb, cudaMemcpyDeviceToDevice, h->stream);
+    struct M
+    {
+        void* p;
+        size_t bytes;
+    } misc[3] = {{h->d_nfluid, 4}, {h->cg.result, sizeof(CgResult)}, {h->d_warn, 4}};
+    off = 0;
+    for (const M& m : misc) {
+        if (e == cudaSuccess)
+            e = save ? cudaMemcpyAsync(sn->misc + off, m.p, m.bytes, cudaMemcpyDeviceToDevice, h->stream)
+                     : cudaMemcpyAsync(m.p, sn->misc + off, m.bytes, cudaMemcpyDeviceToDevice, h->stream);
+        off += 64;
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    return e;
+}
+
+}  // namespace
+
+extern "C" {
+
+int fs_snapshot(fs_handle* h, fs_saved_state** out)
+{
+    if (!h || !out) return h ? fail(h, FS_ERR_INVALID_ARGUMENT, "null snapshot") : FS_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    cudaSetDevice(h->device);
+    fs_saved_state* sn = new fs_saved_state();
+    sn->owner = h;
+    sn->ncell = h->ncell;
+    sn->n_part = h->n_part;
+    sn->front = h->front;
+    sn->vfront = h->vfront;
+    size_t cbytes = 0;
+    for (auto& a : snapshot_cells(h)) cbytes += (a.second * (size_t)h->ncell + 255) / 256 * 256;
+    cudaError_t e = cudaMalloc(&sn->cells, cbytes);
+    if (e == cudaSuccess) e = cudaMalloc(&sn->parts, 16 * (size_t)std::max<int64_t>(sn->n_part, 1));
+    if (e == cudaSuccess) e = cudaMalloc(&sn->misc, 3 * 64);
+    if (e == cudaSuccess) e = copy_snapshot(h, sn, true);
+    if (e != cudaSuccess) {
+        fs_snapshot_destroy(sn);
+        return cuda_fail(h, e, "snapshot");
+    }
+    for (const DevSource& src : h->sources) {
+        sn->src_time.push_back(src.time_since_last);
+        sn->src_spawns.push_back(src.n_spawns);
+    }
+    *out = sn;
+    return FS_OK;
+}
+
+int fs_restore(fs_handle* h, const fs_saved_state* sn)
+{
+    if (!h || !sn) return h ? fail(h, FS_ERR_INVALID_ARGUMENT, "null snapshot") : FS_ERR_INVALID_ARGUMENT;
+    if (sn->owner != h) return fail(h, FS_ERR_INVALID_ARGUMENT, "snapshot of another handle");
+    if (sn->src_time.size() != h->sources.size())
+        return fail(h, FS_ERR_INVALID_ARGUMENT, "fluid sources were added or cleared since the snapshot");
+    cudaSetDevice(h->device);
+    cudaError_t e = ensure_particle_capacity(h, sn->n_part);
+    if (e != cudaSuccess) return cuda_fail(h, e, "particle storage");
+    if (sn->n_part != h->n_part) clear_graphs(h);
+    h->n_part = sn->n_part;
+    h->front = sn->front;
+    h->vfront = sn->vfront;
+    e = copy_snapshot(h, const_cast<fs_saved_state*>(sn), false);
+    if (e != cudaSuccess) return cuda_fail(h, e, "restore");
+    for (size_t k = 0; k < h->sources.size(); ++k) {
+        h->sources[k].time_since_last = sn->src_time[k];
+        h->sources[k].n_spawns = sn->src_spawns[k];
+    }
+    return FS_OK;
+}
+
+int fs_snapshot_destroy(fs_saved_state* sn)
+{
+    if (!sn) return FS_OK;
+    cudaFree(sn->cells);
+    cudaFree(sn->parts);
+    cudaFree(sn->misc);
+    delete sn;
+    return FS_OK;
+}
+
+int fs_debug_set_cg_barrier_fault(fs_handle* h, int missing_arrivals, double wait_limit_seconds)
+{
+    if (!h || missing_arrivals < 0 || !(wait_limit_seconds > 0) || wait_limit_seconds > 10.0)
+        return h ? fail(h, FS_ERR_INVALID_ARGUMENT, "invalid barrier fault settings") : FS_ERR_INVALID_ARGUMENT;
+    h->cg.missing_arrivals = (unsigned)missing_arrivals;
+    h->cg.wait_ns = (uint64_t)(wait_limit_seconds * 1e9);
+    clear_graphs(h);  // both are arguments of the recorded CG launch
     return FS_OK;
 }
 

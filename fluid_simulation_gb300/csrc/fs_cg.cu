@@ -64,6 +64,8 @@ struct CgArgs
     unsigned* barrier;
     unsigned* status;
     CgResult* result;
+    unsigned missing;          // arrivals the grid barrier waits for beyond the grid (test hook; normally 0)
+    uint64_t wait_ns;          // bound of a barrier wait
 };
 
 struct Smem
@@ -120,7 +122,7 @@ __device__ __forceinline__ R warp_tree(R v)
 // the counter (bar.sync first makes the CTA's writes part of what it
 // releases) and spins with acquire loads; the closing bar.sync hands the
 // acquired view to the other threads, which read shared data with ld.cg.
-// Returns false if this CTA gave up waiting (after WAIT_LIMIT_NS); a CTA that
+// Returns false if this CTA gave up waiting (after a.wait_ns); a CTA that
 // gives up returns, so every other CTA also gives up at its next barrier.
 __device__ __forceinline__ bool cta_barrier(const CgArgs& a, bool grid, unsigned& target, Smem& sm)
 {
@@ -129,10 +131,11 @@ __device__ __forceinline__ bool cta_barrier(const CgArgs& a, bool grid, unsigned
         target += gridDim.x;
         red_release_add_u32(a.barrier, 1u);
         int ok = 1;
-        if (ld_acquire_u32(a.barrier) < target) {
+        const unsigned want = target + a.missing;
+        if (ld_acquire_u32(a.barrier) < want) {
             const uint64_t t0 = globaltimer_ns();
-            while (ld_acquire_u32(a.barrier) < target) {
-                if (globaltimer_ns() - t0 > WAIT_LIMIT_NS) {
+            while (ld_acquire_u32(a.barrier) < want) {
+                if (globaltimer_ns() - t0 > a.wait_ns) {
                     atomicOr(a.status, ST_TIMEOUT);
                     ok = 0;
                     break;
@@ -547,6 +550,8 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg_cluster(CgBatchArgs ba)
     a.barrier = nullptr;
     a.status = ba.status;
     a.result = ba.result + sim;
+    a.missing = 0;
+    a.wait_ns = WAIT_LIMIT_NS;
     if (threadIdx.x < 5) {
         sm.dtab[threadIdx.x] = sy.dtab[threadIdx.x];
         sm.itab[threadIdx.x] = sy.itab[threadIdx.x];
@@ -619,6 +624,8 @@ void cg_solve(const Launch& L, CgWork& w, const int32_t* nfluid, const float* b,
     a.barrier = w.barrier;
     a.status = status;
     a.result = w.result;
+    a.missing = w.missing_arrivals;
+    a.wait_ns = w.wait_ns;
     cudaMemsetAsync(w.barrier, 0, sizeof(unsigned), L.stream);
     void* args[] = {&a};
     cudaLaunchCooperativeKernel((const void*)k_cg, dim3(w.grid), dim3(CG_THREADS), args, RESIDENT_BYTES, L.stream);

@@ -179,6 +179,8 @@ struct CgWork
     CgResult* result;
     int64_t max_cells;
     int grid;           // co-resident CTAs of the cooperative launch
+    unsigned missing_arrivals = 0;       // test hook: barrier waits for CTAs that do not exist
+    uint64_t wait_ns = 2000000000ull;    // bound of every device-side wait
 };
 int cg_prepare(CgWork& w, int device);  // picks the cooperative grid size
 // fp64: 0 = float dot products (the reference's precision), 1 = double.

@@ -200,6 +200,15 @@ FS_API int fs_set_graphs(fs_handle* h, int enable);
 /* The handle's CUDA stream (cudaStream_t) and a way to replace it. */
 FS_API void* fs_get_stream(fs_handle* h);
 FS_API int fs_set_stream(fs_handle* h, void* stream);
+/* Test hook of the failure path: the next solves' grid barriers wait for
+ * missing_arrivals CTAs that do not exist, each wait bounded by
+ * wait_limit_seconds (0 < limit <= 10; normally 2).  Every CTA then gives up,
+ * the solve ends early, and fs_synchronize / fs_get_stats return
+ * FS_ERR_TIMEOUT; the handle stays usable.  (0, 2.0) is normal operation.
+ * Solves of at most 16 chunks of 1024 fluid cells run in one CTA and have no
+ * grid barrier. */
+FS_API int fs_debug_set_cg_barrier_fault(fs_handle* h, int missing_arrivals, double wait_limit_seconds);
+
 /* Number of this library's kernel launches queued so far on h. */
 FS_API int64_t fs_kernel_launches(fs_handle* h);
 
@@ -221,6 +230,17 @@ FS_API int fs_num_fluid_sources(fs_handle* h, int* n);
  * copy that was already updated: its time since the last spawn and spawns so far. */
 FS_API int fs_set_fluid_source_state(fs_handle* h, int index, float time_since_last, int n_spawns);
 FS_API int fs_reset_particles(fs_handle* h);
+
+/* Snapshots: a device copy of a handle's simulation state -- the eight
+ * velocity grids, labels, extension masks, fluid indices, particle counts,
+ * pressure, particles, the last CG result and warnings, buffer parities and
+ * the fluid sources' timing state (settings are not part of it).  fs_restore
+ * puts it back into the same handle; it fails if sources were added or
+ * cleared in between.  A snapshot holds device memory until destroyed. */
+typedef struct fs_saved_state fs_saved_state;
+FS_API int fs_snapshot(fs_handle* h, fs_saved_state** out);
+FS_API int fs_restore(fs_handle* h, const fs_saved_state* snap);
+FS_API int fs_snapshot_destroy(fs_saved_state* snap);
 
 /* Pressure projection alone (no particles): the
  * Poisson system of FluidSolver::pressureSolve (src/FluidSolver.cpp:363-425)

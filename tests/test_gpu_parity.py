@@ -273,3 +273,53 @@ def test_fluid_source_lattice_that_cannot_advance_is_rejected():
     with pytest.raises(fsg.FsError) as e:
         g.add_fluid_source(1.0e8, 1.0e8 + 64.0, 1.0, 2.0, 1.0, 1.0, 0.0, 0.0, 0.0, 1)
     assert e.value.code == 1
+
+
+def test_snapshot_and_restore_replay_bit_exact():
+    sc = scenes.dam_break_small()
+    g, o = pair(sc, cg_maxit=400)
+    g.add_fluid_source(2.0, 10.0, 40.0, 50.0, 1.0, 1.0, 3.0, 0.0, 0.02, 4)
+    for _ in range(5):
+        g.update(sc.dt)
+        g.step(fsg.STEP_PICFLIP, sc.dt)
+    snap = g.snapshot()
+    for _ in range(7):
+        g.update(sc.dt)
+        g.step(fsg.STEP_PICFLIP, sc.dt)
+    first = g.state()
+    g.restore(snap)
+    for _ in range(7):
+        g.update(sc.dt)
+        g.step(fsg.STEP_PICFLIP, sc.dt)
+    assert_same(g.state(), first, where="replay from snapshot")
+    other = fsg.FluidSim(sc.size_x, sc.size_y, sc.length_x, sc.length_y, sc.density, sc.pic_ratio)
+    with pytest.raises(fsg.FsError):
+        other.restore(snap)
+    g.clear_fluid_sources()
+    with pytest.raises(fsg.FsError):
+        g.restore(snap)
+
+
+def test_cg_barrier_timeout_is_reported_and_the_handle_recovers():
+    """Failure detection without a GPU fault: the CG's grid barrier is made to
+    wait for CTAs that do not exist (a bounded 50 ms wait); every CTA gives
+    up, the host reads FS_ERR_TIMEOUT, and the handle keeps working: restored
+    from a snapshot it continues bit-exact with the oracle."""
+    sc = scenes.dam_break_large(256)
+    g, o = pair(sc, cg_maxit=5000)
+    for _ in range(2):
+        g.step(fsg.STEP_PICFLIP, sc.dt)
+        o.step(po.STEP_PICFLIP, sc.dt)
+    assert g.stats()["n_fluid"] > 16 * 1024  # the solve runs grid-wide
+    snap = g.snapshot()
+    assert g.lib.fs_debug_set_cg_barrier_fault(g.h, 1, 0.05) == 0
+    g.step(fsg.STEP_PICFLIP, sc.dt)
+    with pytest.raises(fsg.FsError) as e:
+        g.synchronize()
+    assert e.value.code == 4
+    assert g.lib.fs_debug_set_cg_barrier_fault(g.h, 0, 2.0) == 0
+    g.restore(snap)
+    for k in range(2):
+        g.step(fsg.STEP_PICFLIP, sc.dt)
+        o.step(po.STEP_PICFLIP, sc.dt)
+        assert_same(g.state(), o.state(), where="after recovery, step %d" % k)
