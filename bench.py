@@ -57,6 +57,8 @@ def parse():
     ap.add_argument("--no-forms", action="store_true", help="skip the batched and mixed-precision forms")
     ap.add_argument("--batch", type=int, default=512, help="members of the batched form")
     ap.add_argument("--projection-size", type=int, default=4096, help="grid side of the mixed-precision form")
+    ap.add_argument("--batch-plan", type=int, choices=[1, 2, 4, 8], default=None,
+                    help="batched form: CG chunks per CTA instead of the autotuner's choice")
     ap.add_argument("--only-form", choices=["batched", "mixed_precision"], default=None,
                     help="measure one form alone (profiling runs) and print its JSON object")
     return ap.parse_args()
@@ -255,7 +257,11 @@ def measure_batched(args, local_rank, plain_value, flush):
     cells = sum(s.cells for s in sc)
     b = fsg.FluidBatch.from_scenes(sc, device=local_rank)
     b.step(fsg.STEP_PICFLIP, 0.005)
-    tuned = b.tune(fsg.STEP_PICFLIP, 0.005, steps=2)
+    if args.batch_plan:
+        b.set_tuning(args.batch_plan)
+        tuned = {"chunks_per_cta": args.batch_plan, "ms_per_step": None}
+    else:
+        tuned = b.tune(fsg.STEP_PICFLIP, 0.005, steps=2)
     for _ in range(args.warmup):
         b.step(fsg.STEP_PICFLIP, 0.005)
     b.synchronize()
