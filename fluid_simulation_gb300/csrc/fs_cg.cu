@@ -260,6 +260,33 @@ __device__ __forceinline__ void reduce_all(const CgArgs& a, int buf, int nchunks
     __syncthreads();
 }
 
+// Levels 2+ when one CTA owns all of at most 32 chunks: one warp reduces each
+// chunk's 32 level-1 results and then the chunk partials, the same tree as
+// level2 + reduce_all (a lone chunk's partial is the result as it stands),
+// without the round trip of the partials through global memory.
+template <typename R, int NV>
+__device__ __forceinline__ void local_reduce(int nchunks, Smem& sm, R (&out)[NV])
+{
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (warp == 0) {
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            R mine = R(0);
+            for (int s = 0; s < nchunks; ++s) {
+                R t = warp_tree<R>(Ar<R>::red(sm, s, lane, k));
+                t = __shfl_sync(0xffffffffu, t, 0);
+                if (lane == s) mine = t;
+            }
+            const R res = nchunks == 1 ? mine : warp_tree<R>(lane < nchunks ? mine : R(0));
+            if (lane == 0) Ar<R>::lvlB(sm, 0, k) = res;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < NV; ++k) out[k] = Ar<R>::lvlB(sm, 0, k);
+}
+
 // p_new of a cell outside this CTA's range, from its published z and p_old.
 __device__ __forceinline__ float remote_p(const CgArgs& a, int n, bool first, float beta)
 {
@@ -307,6 +334,10 @@ __device__ __forceinline__ void cg_body(const CgArgs& a, Smem& sm, unsigned char
     const int kb = c1 - c0;                // chunks owned
     const int e0 = c0 * CHUNK;             // owned element range [e0, e1)
     const int e1 = min(c1 * CHUNK, nf);
+    // One CTA owning every chunk keeps the reductions in shared memory and,
+    // with its state resident, publishes nothing for other CTAs.
+    const bool local = ncta == 1 && nchunks <= 32;
+    const bool publish = !(local && K > 0);
     const Resident RS = resident(dyn, K > 0 ? K : 1);
     const float* dtab = sm.dtab;
     const float* itab = sm.itab;
@@ -322,7 +353,7 @@ __device__ __forceinline__ void cg_body(const CgArgs& a, Smem& sm, unsigned char
                 const float r = a.b[e];
                 const uint8_t fl = a.flags[e];
                 const float z = fmul(itab[fl >> 2], r);
-                __stcg(&a.z[e], z);
+                if (publish) __stcg(&a.z[e], z);
                 v[0] = Ar<R>::prod(r, r);
                 v[1] = Ar<R>::prod(r, z);
                 if (K > 0) {
@@ -341,11 +372,15 @@ __device__ __forceinline__ void cg_body(const CgArgs& a, Smem& sm, unsigned char
             }
             level1<R, 2>(v, sl, sm);
         }
-        level2<R, 2>(a, 0, c0 + base, nslot, sm);
+        if (!local) level2<R, 2>(a, 0, c0 + base, nslot, sm);
     }
-    if (!sync.barrier(a, sm)) return;
     R red2[2];
-    reduce_all<R, 2>(a, 0, nchunks, sm, red2);
+    if (local) {
+        local_reduce<R, 2>(nchunks, sm, red2);
+    } else {
+        if (!sync.barrier(a, sm)) return;
+        reduce_all<R, 2>(a, 0, nchunks, sm, red2);
+    }
     const R bb = red2[0];
     R rz = red2[1];
     R rr = bb;
@@ -405,11 +440,15 @@ __device__ __forceinline__ void cg_body(const CgArgs& a, Smem& sm, unsigned char
                 }
                 level1<R, 1>(v, sl, sm);
             }
-            level2<R, 1>(a, 1, c0 + base, nslot, sm);
+            if (!local) level2<R, 1>(a, 1, c0 + base, nslot, sm);
         }
-        if (!sync.barrier(a, sm)) return;
         R red1[1];
-        reduce_all<R, 1>(a, 1, nchunks, sm, red1);
+        if (local) {
+            local_reduce<R, 1>(nchunks, sm, red1);
+        } else {
+            if (!sync.barrier(a, sm)) return;
+            reduce_all<R, 1>(a, 1, nchunks, sm, red1);
+        }
         const float alpha = Ar<R>::ratio(rz, red1[0]);
 
         // ---- phase B: x += alpha p, r -= alpha q, z = M^-1 r; publish z, p; partial r.r, r.z
@@ -447,17 +486,23 @@ __device__ __forceinline__ void cg_body(const CgArgs& a, Smem& sm, unsigned char
                         __stcg(&a.x[e], x);
                         __stcg(&a.r[e], r);
                     }
-                    __stcg(&a.z[e], z);
-                    __stcg(&a.p[e], pn);
+                    if (publish) {
+                        __stcg(&a.z[e], z);
+                        __stcg(&a.p[e], pn);
+                    }
                     v[0] = Ar<R>::prod(r, r);
                     v[1] = Ar<R>::prod(r, z);
                 }
                 level1<R, 2>(v, sl, sm);
             }
-            level2<R, 2>(a, 0, c0 + base, nslot, sm);
+            if (!local) level2<R, 2>(a, 0, c0 + base, nslot, sm);
         }
-        if (!sync.barrier(a, sm)) return;
-        reduce_all<R, 2>(a, 0, nchunks, sm, red2);
+        if (local) {
+            local_reduce<R, 2>(nchunks, sm, red2);
+        } else {
+            if (!sync.barrier(a, sm)) return;
+            reduce_all<R, 2>(a, 0, nchunks, sm, red2);
+        }
         rr = red2[0];
         iters = it;
         if (rr < thr) break;
