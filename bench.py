@@ -217,6 +217,20 @@ def run_reference(args, rank):
     print(json.dumps(line), flush=True)
 
 
+def max_over_ranks(value: float, device: str) -> float:
+    """The largest of every rank's value (the job's time is its slowest
+    replica's); `device` holds the exchanged tensor ("cuda:k" under NCCL,
+    "cpu" under gloo).  One rank: the value itself."""
+    import torch
+    import torch.distributed as dist
+
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(value)
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 # ---------------------------------------------------------------- GPU arm
 def read_traffic():
     """DRAM bytes per CG launch from the committed ncu summary, if any."""
@@ -382,13 +396,7 @@ def run_gpu(args, rank, world, local_rank):
             iters.append(st["cg_iterations"])
     launches = sim.kernel_launches() - launches0
     torch.cuda.synchronize()
-    t_dev = sum(step_ms) / 1000.0
-    if world > 1:
-        import torch.distributed as dist
-
-        t = torch.tensor([t_dev], dtype=torch.float64, device="cuda:%d" % local_rank)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_dev = float(t.item())
+    t_dev = max_over_ranks(sum(step_ms) / 1000.0, "cuda:%d" % local_rank)
     value = sc.cells * args.steps * world / t_dev
 
     # end to end through the C ABI with host (pinned) particle buffers
@@ -409,13 +417,7 @@ def run_gpu(args, rank, world, local_rank):
         sim.lib.fs_get_particles(sim.h, host_out.ctypes.data, n)
         host_in, host_out = host_out, host_in
     sim.synchronize()
-    t_e2e = time.perf_counter() - t0
-    if world > 1:
-        import torch.distributed as dist
-
-        t = torch.tensor([t_e2e], dtype=torch.float64, device="cuda:%d" % local_rank)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_e2e = float(t.item())
+    t_e2e = max_over_ranks(time.perf_counter() - t0, "cuda:%d" % local_rank)
     e2e_value = sc.cells * e2e_steps * world / t_e2e
 
     if rank != 0:
