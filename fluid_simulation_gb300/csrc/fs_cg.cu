@@ -126,13 +126,14 @@ __device__ __forceinline__ R warp_tree(R v)
 // gives up returns, so every other CTA also gives up at its next barrier.
 __device__ __forceinline__ bool cta_barrier(const CgArgs& a, bool grid, unsigned& target, Smem& sm)
 {
-    __syncthreads();
+    // (callers come straight from level2, whose closing bar.sync orders the CTA's writes)
     if (grid && threadIdx.x == 0) {
         target += gridDim.x;
-        red_release_add_u32(a.barrier, 1u);
+        unsigned old;
+        asm volatile("atom.add.acq_rel.gpu.global.u32 %0, [%1], 1;" : "=r"(old) : "l"(a.barrier) : "memory");
         int ok = 1;
         const unsigned want = target + a.missing;
-        if (ld_acquire_u32(a.barrier) < want) {
+        if (old + 1u < want && ld_acquire_u32(a.barrier) < want) {
             const uint64_t t0 = globaltimer_ns();
             while (ld_acquire_u32(a.barrier) < want) {
                 if (globaltimer_ns() - t0 > a.wait_ns) {
@@ -257,7 +258,7 @@ __device__ __forceinline__ void reduce_all(const CgArgs& a, int buf, int nchunks
     }
 #pragma unroll
     for (int k = 0; k < NV; ++k) out[k] = inA ? Ar<R>::lvlA(sm, 0, k) : Ar<R>::lvlB(sm, 0, k);
-    __syncthreads();
+    if (inA) __syncthreads();  // lvlA shares storage with the next phase's level-1 results
 }
 
 // Levels 2+ when one CTA owns all of at most 32 chunks: one warp reduces each
