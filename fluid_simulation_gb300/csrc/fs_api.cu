@@ -89,7 +89,6 @@ struct fs_handle
     int64_t n_part = 0, cap_part = 0;
 
     SplatWork sw{};
-    int64_t sw_items = 0;
 
     // pressure solve
     CgWork cg{};
@@ -165,32 +164,10 @@ void clear_graphs(fs_handle* h)
 
 cudaError_t ensure_splat_capacity(fs_handle* h, int64_t items)
 {
-    if (items <= h->sw_items) return cudaSuccess;
-    SplatWork& w = h->sw;
-    cudaFree(w.keys_a);
-    cudaFree(w.keys_b);
-    cudaFree(w.vals_a);
-    cudaFree(w.vals_b);
-    cudaFree(w.hist);
-    cudaFree(w.hist_scan);
-    cudaFree(w.scan_tmp);
-    w.keys_a = w.keys_b = nullptr;
-    w.vals_a = w.vals_b = w.hist = w.hist_scan = w.scan_tmp = nullptr;
-    h->sw_items = 0;
-    const size_t hist = splat_hist_ints(items);
-    const size_t hscan = std::max(hist, (size_t)h->ncell + 2);
-    cudaError_t e;
-    if ((e = dalloc(&w.keys_a, (size_t)items)) != cudaSuccess) return e;
-    if ((e = dalloc(&w.keys_b, (size_t)items)) != cudaSuccess) return e;
-    if ((e = dalloc(&w.vals_a, (size_t)items)) != cudaSuccess) return e;
-    if ((e = dalloc(&w.vals_b, (size_t)items)) != cudaSuccess) return e;
-    if ((e = dalloc(&w.hist, hist)) != cudaSuccess) return e;
-    if ((e = dalloc(&w.hist_scan, hscan)) != cudaSuccess) return e;
-    if ((e = dalloc(&w.scan_tmp, scan_tmp_ints((int64_t)hscan))) != cudaSuccess) return e;
-    w.cap_items = items;
-    h->sw_items = items;
+    if (items <= h->sw.cap_items) return cudaSuccess;
+    const cudaError_t e = splat_alloc(h->sw, items, h->ncell);
     clear_graphs(h);
-    return cudaSuccess;
+    return e;
 }
 
 cudaError_t ensure_particle_capacity(fs_handle* h, int64_t n)
@@ -355,11 +332,11 @@ void destroy_all(fs_handle* h)
                     h->solid, h->vmx[0], h->vmx[1], h->vmy[0], h->vmy[1], h->fidx, h->cell_of, h->counts32,
                     h->counts8, h->acc[0], h->acc[1], h->acc[2], h->acc[3], h->grid_tmp, h->sl[0], h->sl[1],
                     h->sl[2], h->sl[3], h->sl[4], h->sl[5], h->sl_ok[0], h->sl_ok[1], h->px, h->py, h->pvx,
-                    h->pvy, h->yu, h->xv, h->staging, h->sw.keys_a, h->sw.keys_b, h->sw.vals_a, h->sw.vals_b,
-                    h->sw.hist, h->sw.hist_scan, h->sw.scan_tmp, h->sw.bin_start, h->cg.x, h->cg.r, h->cg.z,
+                    h->pvy, h->yu, h->xv, h->staging, h->cg.x, h->cg.r, h->cg.z,
                     h->cg.p, h->cg.q, h->cg.partials, h->cg.barrier, h->cg.result, h->cg_b, h->cg_down, h->cg_up,
                     h->cg_flags, h->d_nfluid, h->d_status, h->d_warn, h->scan_tmp};
     for (void* p : ptrs) cudaFree(p);
+    splat_free(h->sw);
     for (DevSource& src : h->sources) {
         cudaFree(src.d_xs);
         cudaFree(src.d_ys);
@@ -528,7 +505,6 @@ int fs_create(const fs_config* cfg, fs_handle** out)
     A(dalloc(&h->counts8, N));
     for (int k = 0; k < 4; ++k) A(dalloc(&h->acc[k], N));
     A(dalloc(&h->grid_tmp, N));
-    A(dalloc(&h->sw.bin_start, N + 2));
     A(dalloc(&h->cg.x, N));
     A(dalloc(&h->cg.r, N));
     A(dalloc(&h->cg.z, N));

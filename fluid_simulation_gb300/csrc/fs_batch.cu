@@ -107,7 +107,6 @@ struct fs_batch
     float* staging = nullptr;
     int64_t staging_cap = 0;
     SplatWork sw{};
-    int64_t sw_items = 0;
 
     int32_t* nfluid = nullptr;
     unsigned* status = nullptr;
@@ -221,27 +220,9 @@ int refresh_plan_chunks(fs_batch* b)
 
 cudaError_t ensure_splat_capacity(fs_batch* b, int64_t items)
 {
-    if (items <= b->sw_items) return cudaSuccess;
-    SplatWork& w = b->sw;
-    for (void* p : {(void*)w.keys_a, (void*)w.keys_b, (void*)w.vals_a, (void*)w.vals_b, (void*)w.hist,
-                    (void*)w.hist_scan, (void*)w.scan_tmp})
-        cudaFree(p);
-    w.keys_a = w.keys_b = nullptr;
-    w.vals_a = w.vals_b = w.hist = w.hist_scan = w.scan_tmp = nullptr;
-    b->sw_items = 0;
-    const size_t hist = splat_hist_ints(items);
-    const size_t hscan = std::max(hist, (size_t)b->cells + 2);
-    cudaError_t e;
-    if ((e = dalloc(&w.keys_a, (size_t)items)) != cudaSuccess) return e;
-    if ((e = dalloc(&w.keys_b, (size_t)items)) != cudaSuccess) return e;
-    if ((e = dalloc(&w.vals_a, (size_t)items)) != cudaSuccess) return e;
-    if ((e = dalloc(&w.vals_b, (size_t)items)) != cudaSuccess) return e;
-    if ((e = dalloc(&w.hist, hist)) != cudaSuccess) return e;
-    if ((e = dalloc(&w.hist_scan, hscan)) != cudaSuccess) return e;
-    if ((e = dalloc(&w.scan_tmp, scan_tmp_ints((int64_t)hscan))) != cudaSuccess) return e;
-    w.cap_items = items;
-    b->sw_items = items;
-    return cudaSuccess;
+    if (items <= b->sw.cap_items) return cudaSuccess;
+    clear_graphs(b);
+    return splat_alloc(b->sw, items, b->cells);
 }
 
 // Lays out the particles of every simulation after sets: new capacities and
@@ -572,10 +553,10 @@ void free_all(fs_batch* b)
                     b->cell_of, b->counts32, b->counts8, b->acc[0], b->acc[1], b->acc[2], b->acc[3], b->grid_tmp,
                     b->sl[0], b->sl[1], b->sl[2], b->sl[3], b->sl[4], b->sl[5], b->sl_ok[0], b->sl_ok[1], b->cg_b,
                     b->cg_down, b->cg_up, b->cg_flags, b->cx, b->cr, b->cz, b->cp, b->cq, b->px, b->py, b->pvx,
-                    b->pvy, b->yu, b->xv, b->staging, b->sw.keys_a, b->sw.keys_b, b->sw.vals_a, b->sw.vals_b,
-                    b->sw.hist, b->sw.hist_scan, b->sw.scan_tmp, b->sw.bin_start, b->nfluid, b->status, b->warn,
+                    b->pvy, b->yu, b->xv, b->staging, b->nfluid, b->status, b->warn,
                     b->index_tmp, b->d_sys, b->partials, b->results, b->d_order};
     for (void* p : ptrs) cudaFree(p);
+    splat_free(b->sw);
     for (cudaStream_t s : b->aux)
         if (s) cudaStreamDestroy(s);
     for (cudaEvent_t e : b->join)
@@ -732,7 +713,6 @@ int fs_batch_create(int n, const fs_config* cfgs, fs_batch** out)
     A(dalloc(&b->cg_down, C));
     A(dalloc(&b->cg_up, C));
     A(dalloc(&b->cg_flags, C));
-    A(dalloc(&b->sw.bin_start, C + 2));
     A(dalloc(&b->nfluid, (size_t)n));
     A(dalloc(&b->status, 1));
     A(dalloc(&b->warn, 1));

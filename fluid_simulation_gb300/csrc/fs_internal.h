@@ -84,16 +84,17 @@ void fluid_index_batch(const Launch& L, const Domain& d, const uint8_t* labels, 
 // ---- stable radix sort + ordered splat (fs_splat.cu) ---------------------
 struct SplatWork
 {
-    // Sort buffers sized for the largest item count.
-    uint32_t *keys_a, *keys_b;
-    int32_t *vals_a, *vals_b;
-    int32_t* hist;       // 256 * blocks(n) + 1
-    int32_t* hist_scan;  // same
-    int32_t* scan_tmp;
-    int32_t* bin_start;  // cells + 1
-    int64_t cap_items;
+    uint32_t* keys = nullptr;      // bin of each item
+    int32_t* sorted = nullptr;     // items grouped by bin, each bin in item order
+    int32_t* bin_count = nullptr;  // cells + 2
+    int32_t* bin_start = nullptr;  // cells + 2
+    int32_t* scan_tmp = nullptr;
+    int64_t cap_items = 0;
+    int64_t cells = 0;
 };
-size_t splat_hist_ints(int64_t n_items);
+// Buffers for up to `items` items over `cells` cells (frees what w held).
+cudaError_t splat_alloc(SplatWork& w, int64_t items, int64_t cells);
+void splat_free(SplatWork& w);
 // Accumulates, for each node of every simulation of d, sum over that
 // simulation's items k in increasing k of the bilinear splat
 // (Grid::addToValueInterpolated, include/Grid.h:152-184) of value[c][k] at

@@ -4,27 +4,17 @@
 // FluidSolver::advectVelocitySemiLagrangian (src/FluidSolver.cpp:721-771).
 //
 // Float sums depend on their order, so instead of float atomics the items are
-// stably sorted by the base cell of their splat footprint (LSD radix sort,
-// 8-bit digits) and every grid node gathers the items of the (up to) four
-// base cells that can reach it, merging the four item lists by item index.
-// Each node thus adds exactly the same float terms in exactly the same order
-// as the reference's sequential loop, and the result is bit-identical.
+// binned by the base cell of their splat footprint (a counting sort: bin
+// counts, their prefix sum, a scatter with per-bin atomic cursors, then each
+// bin sorted by item index, which makes the order the items' own) and every
+// grid node gathers the items of the (up to) four base cells that can reach
+// it, merging the four item lists by item index.  Each node thus adds exactly
+// the same float terms in exactly the same order as the reference's
+// sequential loop, and the result is bit-identical.
 #include "fs_domain.cuh"
 
 namespace fs {
 namespace {
-
-constexpr int RT = 256;            // radix threads per tile
-constexpr int RW = RT / 32;        // warps per tile
-constexpr int R_PER_WARP = 512;    // items per warp
-constexpr int RTILE = RW * R_PER_WARP;  // 4096 items per tile
-
-__device__ __forceinline__ unsigned lanemask_lt()
-{
-    unsigned m;
-    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
-    return m;
-}
 
 // Key of each item: the flattened index (co + local cell) of the base cell of
 // its footprint, or d.cells for invalid items and for the padding between
@@ -34,8 +24,7 @@ __global__ void __launch_bounds__(DOMAIN_TPB) k_splat_keys(Seg one, const Seg* _
                                                            int64_t n, uint32_t invalid, const float* __restrict__ x,
                                                            const float* __restrict__ y,
                                                            const uint8_t* __restrict__ valid,
-                                                           uint32_t* __restrict__ keys, int32_t* __restrict__ vals,
-                                                           int32_t* __restrict__ bin_count)
+                                                           uint32_t* __restrict__ keys, int32_t* __restrict__ bin_count)
 {
     const int64_t k = (int64_t)blockIdx.x * DOMAIN_TPB + threadIdx.x;
     if (k >= n) return;
@@ -56,75 +45,56 @@ __global__ void __launch_bounds__(DOMAIN_TPB) k_splat_keys(Seg one, const Seg* _
         key = (uint32_t)(s.co + sp.i + (int64_t)sp.j * s.g.nx);
     }
     keys[k] = key;
-    vals[k] = (int32_t)k;
     atomicAdd(&bin_count[key], 1);
 }
 
-// Per-tile digit histogram, stored digit-major: hist[d * ntiles + tile].
-__global__ void __launch_bounds__(RT) k_radix_hist(const uint32_t* __restrict__ keys, int64_t n, int shift,
-                                                  int ntiles, int32_t* __restrict__ hist)
+// Item k goes to position bin_start[key] + (its rank among the bin's items
+// in arrival order, counted down on the bin's count).
+__global__ void k_bin_scatter(int64_t n, uint32_t invalid, const uint32_t* __restrict__ keys,
+                              const int32_t* __restrict__ bin_start, int32_t* __restrict__ count,
+                              int32_t* __restrict__ sorted)
 {
-    __shared__ int h[256];
-    h[threadIdx.x] = 0;
-    __syncthreads();
-    const int64_t base = (int64_t)blockIdx.x * RTILE;
-    for (int k = threadIdx.x; k < RTILE; k += RT) {
-        const int64_t i = base + k;
-        if (i < n) atomicAdd(&h[(keys[i] >> shift) & 255u], 1);
-    }
-    __syncthreads();
-    hist[(int64_t)threadIdx.x * ntiles + blockIdx.x] = h[threadIdx.x];
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const uint32_t key = keys[k];
+    if (key == invalid) return;  // the bin of invalid items is never gathered
+    const int pos = bin_start[key] + atomicSub(&count[key], 1) - 1;
+    sorted[pos] = (int32_t)k;
 }
 
-// Stable scatter: each warp owns 512 consecutive items of the tile and walks
-// them 32 at a time; ranks among equal digits come from __match_any_sync.
-__global__ void __launch_bounds__(RT) k_radix_scatter(const uint32_t* __restrict__ kin, const int32_t* __restrict__ vin,
-                                                     uint32_t* __restrict__ kout, int32_t* __restrict__ vout, int64_t n,
-                                                     int shift, int ntiles, const int32_t* __restrict__ hist_off)
+// Each bin's items in increasing item index (insertion sort; bins hold a few
+// items).
+__global__ void k_bin_sort(int64_t nbins, const int32_t* __restrict__ bin_start, int32_t* __restrict__ sorted)
 {
-    __shared__ int cnt[RW][256];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    for (int k = threadIdx.x; k < RW * 256; k += RT) (&cnt[0][0])[k] = 0;
-    __syncthreads();
-    const int64_t seg = (int64_t)blockIdx.x * RTILE + (int64_t)warp * R_PER_WARP;
-    const unsigned lt = lanemask_lt();
-    // 1. per-warp digit counts
-    for (int r = 0; r < R_PER_WARP; r += 32) {
-        const int64_t i = seg + r + lane;
-        const bool ok = i < n;
-        const unsigned d = ok ? ((kin[i] >> shift) & 255u) : 256u;
-        const unsigned peers = __match_any_sync(0xffffffffu, d);
-        if (ok && (peers & lt) == 0) cnt[warp][d] += __popc(peers);
-        __syncwarp();
-    }
-    __syncthreads();
-    // 2. exclusive prefix over warps, offset by the tile's global digit offset
-    {
-        const int d = threadIdx.x;
-        int run = hist_off[(int64_t)d * ntiles + blockIdx.x];
-        for (int w = 0; w < RW; ++w) {
-            const int c = cnt[w][d];
-            cnt[w][d] = run;
-            run += c;
+    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= nbins) return;
+    const int b0 = bin_start[c], b1 = bin_start[c + 1];
+    if (b1 - b0 < 2) return;
+    constexpr int LOCAL = 16;
+    if (b1 - b0 <= LOCAL) {
+        int v[LOCAL];
+        const int m = b1 - b0;
+        for (int i = 0; i < m; ++i) v[i] = sorted[b0 + i];
+        for (int i = 1; i < m; ++i) {
+            const int t = v[i];
+            int j = i - 1;
+            while (j >= 0 && v[j] > t) {
+                v[j + 1] = v[j];
+                --j;
+            }
+            v[j + 1] = t;
         }
-    }
-    __syncthreads();
-    // 3. scatter in item order
-    for (int r = 0; r < R_PER_WARP; r += 32) {
-        const int64_t i = seg + r + lane;
-        const bool ok = i < n;
-        const uint32_t key = ok ? kin[i] : 0u;
-        const unsigned d = ok ? ((key >> shift) & 255u) : 256u;
-        const unsigned peers = __match_any_sync(0xffffffffu, d);
-        int dest = 0;
-        if (ok) dest = cnt[warp][d] + __popc(peers & lt);
-        __syncwarp();
-        if (ok) {
-            kout[dest] = key;
-            vout[dest] = vin[i];
-            if ((peers & lt) == 0) cnt[warp][d] += __popc(peers);
+        for (int i = 0; i < m; ++i) sorted[b0 + i] = v[i];
+    } else {
+        for (int i = b0 + 1; i < b1; ++i) {
+            const int t = sorted[i];
+            int j = i - 1;
+            while (j >= b0 && sorted[j] > t) {
+                sorted[j + 1] = sorted[j];
+                --j;
+            }
+            sorted[j + 1] = t;
         }
-        __syncwarp();
     }
 }
 
@@ -189,19 +159,35 @@ struct SplatGather
     }
 };
 
-int key_bits(uint32_t max_key)
-{
-    int b = 1;
-    while (b < 32 && (max_key >> b) != 0u) ++b;
-    return b;
-}
-
 }  // namespace
 
-size_t splat_hist_ints(int64_t n_items)
+cudaError_t splat_alloc(SplatWork& w, int64_t items, int64_t cells)
 {
-    const int64_t ntiles = (n_items + RTILE - 1) / RTILE;
-    return (size_t)(256 * (ntiles > 0 ? ntiles : 1)) + 1;
+    splat_free(w);
+    const size_t bins = (size_t)cells + 2;
+    cudaError_t e = cudaSuccess;
+    auto A = [&](void** p, size_t bytes) {
+        if (e == cudaSuccess) e = cudaMalloc(p, bytes ? bytes : 4);
+    };
+    A((void**)&w.keys, 4 * (size_t)items);
+    A((void**)&w.sorted, 4 * (size_t)items);
+    A((void**)&w.bin_count, 4 * bins);
+    A((void**)&w.bin_start, 4 * bins);
+    A((void**)&w.scan_tmp, 4 * scan_tmp_ints((int64_t)bins));
+    if (e != cudaSuccess) {
+        splat_free(w);
+        return e;
+    }
+    w.cap_items = items;
+    w.cells = cells;
+    return cudaSuccess;
+}
+
+void splat_free(SplatWork& w)
+{
+    for (void* p : {(void*)w.keys, (void*)w.sorted, (void*)w.bin_count, (void*)w.bin_start, (void*)w.scan_tmp})
+        cudaFree(p);
+    w = SplatWork{};
 }
 
 void ordered_splat(const Launch& L, const Domain& d, bool items_are_cells, bool pool_deltas, const float* x,
@@ -211,38 +197,24 @@ void ordered_splat(const Launch& L, const Domain& d, bool items_are_cells, bool 
     const int64_t ncell = d.cells;
     const int64_t n = items_are_cells ? d.cells : d.parts;
     // bin counts over ncell + 1 bins (the last one collects invalid items)
-    cudaMemsetAsync(w.hist_scan, 0, sizeof(int32_t) * (size_t)(ncell + 2), L.stream);
-    int32_t* bin_count = w.hist_scan;
+    cudaMemsetAsync(w.bin_count, 0, sizeof(int32_t) * (size_t)(ncell + 2), L.stream);
     if (n > 0) {
         const int2* blk = d.segs ? (items_are_cells ? d.cblk : d.pblk) : nullptr;
         k_splat_keys<<<domain_blocks(n), DOMAIN_TPB, 0, L.stream>>>(d.one, d.segs, blk, items_are_cells, pool_deltas,
-                                                                     n, (uint32_t)ncell, x, y, valid, w.keys_a,
-                                                                     w.vals_a, bin_count);
+                                                                     n, (uint32_t)ncell, x, y, valid, w.keys,
+                                                                     w.bin_count);
         L.count();
     }
-    scan_exclusive_i32(L, bin_count, w.bin_start, ncell + 1, w.scan_tmp);
-    // stable LSD radix sort of (key, item)
-    uint32_t *kin = w.keys_a, *kout = w.keys_b;
-    int32_t *vin = w.vals_a, *vout = w.vals_b;
+    scan_exclusive_i32(L, w.bin_count, w.bin_start, ncell + 1, w.scan_tmp);
     if (n > 0) {
-        const int ntiles = (int)((n + RTILE - 1) / RTILE);
-        const int bits = key_bits((uint32_t)ncell);
-        for (int shift = 0; shift < bits; shift += 8) {
-            k_radix_hist<<<ntiles, RT, 0, L.stream>>>(kin, n, shift, ntiles, w.hist);
-            scan_exclusive_i32(L, w.hist, w.hist_scan, (int64_t)256 * ntiles, w.scan_tmp);
-            k_radix_scatter<<<ntiles, RT, 0, L.stream>>>(kin, vin, kout, vout, n, shift, ntiles, w.hist_scan);
-            L.count(2);
-            uint32_t* tk = kin;
-            kin = kout;
-            kout = tk;
-            int32_t* tv = vin;
-            vin = vout;
-            vout = tv;
-        }
+        k_bin_scatter<<<domain_blocks(n), DOMAIN_TPB, 0, L.stream>>>(n, (uint32_t)ncell, w.keys, w.bin_start,
+                                                                      w.bin_count, w.sorted);
+        k_bin_sort<<<domain_blocks(ncell), DOMAIN_TPB, 0, L.stream>>>(ncell, w.bin_start, w.sorted);
+        L.count(2);
     }
     each_cell(L, d,
-              SplatGather{pool_deltas, x, y, channels, values[0], channels > 1 ? values[1] : nullptr, w.bin_start, vin,
-                          out[0], channels > 1 ? out[1] : nullptr});
+              SplatGather{pool_deltas, x, y, channels, values[0], channels > 1 ? values[1] : nullptr, w.bin_start,
+                          w.sorted, out[0], channels > 1 ? out[1] : nullptr});
 }
 
 }  // namespace fs
