@@ -31,6 +31,7 @@ CG_FLOAT, CG_DOUBLE = 0, 1
 POISSON_FP32, POISSON_FP64, POISSON_MIXED = 0, 1, 2
 INTEGRATOR_EULER, INTEGRATOR_RK2, INTEGRATOR_RK3 = 0, 1, 2
 SMOKE_FP32, SMOKE_FP64 = 0, 1
+RENDER_CLEAR, RENDER_CELLS, RENDER_VELOCITIES, RENDER_PARTICLES, RENDER_METABALLS = range(5)
 TIMED_PHASES = ("classify", "p2g", "forces", "assembly", "cg", "project", "g2p")
 
 
@@ -103,6 +104,17 @@ SIGNATURES = {
     "fs_restore": (_i, [_vp, _vp]),
     "fs_snapshot_destroy": (_i, [_vp]),
     "fs_debug_set_cg_barrier_fault": (_i, [_vp, _i, _d]),
+    "fs_canvas_create": (_i, [_i, _i, _i, C.POINTER(_vp)]),
+    "fs_canvas_destroy": (_i, [_vp]),
+    "fs_canvas_last_error": (C.c_char_p, [_vp]),
+    "fs_canvas_set_pixels": (_i, [_vp, _vp]),
+    "fs_canvas_get_pixels": (_i, [_vp, _vp]),
+    "fs_canvas_set_colors": (_i, [_vp, _vp, _vp]),
+    "fs_canvas_get_colors": (_i, [_vp, _vp, _vp]),
+    "fs_canvas_get_bytes": (_i, [_vp, _vp]),
+    "fs_canvas_write_ppm": (_i, [_vp, C.c_char_p]),
+    "fs_canvas_kernel_launches": (_i64, [_vp]),
+    "fs_render": (_i, [_vp, _vp, _i, _vp]),
     "fs_synchronize": (_i, [_vp]),
     "fs_get_stats": (_i, [_vp, C.POINTER(fs_step_stats)]),
     "fs_set_timing": (_i, [_vp, _i]),
@@ -331,6 +343,11 @@ class FluidSim:
     def reset_particles(self) -> None:
         self._check(self.lib.fs_reset_particles(self.h))
 
+    # rendering (Renderer.cpp onto a device canvas)
+    def render(self, canvas: "Canvas", what: int, area) -> None:
+        a = np.ascontiguousarray(area, dtype=np.float32)
+        self._check(self.lib.fs_render(self.h, canvas.p, what, _ptr(a)))
+
     # snapshots
     def snapshot(self) -> "Snapshot":
         p = C.c_void_p()
@@ -374,6 +391,59 @@ class FluidSim:
         s["pressure"] = self.pressure()
         s["particles"] = self.particles()
         return s
+
+
+class Canvas:
+    """A device canvas of width x height RGB floats (fs_canvas_*)."""
+
+    def __init__(self, width: int, height: int, device: int = 0):
+        self.lib = load_library()
+        p = C.c_void_p()
+        rc = self.lib.fs_canvas_create(width, height, device, C.byref(p))
+        if rc != FS_OK:
+            raise FsError(rc, self.lib.fs_canvas_last_error(None).decode())
+        self.p, self.width, self.height = p, width, height
+
+    def _check(self, rc: int) -> None:
+        if rc != FS_OK:
+            raise FsError(rc, self.lib.fs_canvas_last_error(self.p).decode())
+
+    def close(self) -> None:
+        if getattr(self, "p", None):
+            self.lib.fs_canvas_destroy(self.p)
+            self.p = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_pixels(self, rgb: np.ndarray) -> None:
+        a = np.ascontiguousarray(rgb, dtype=np.float32).reshape(self.height, self.width, 3)
+        self._check(self.lib.fs_canvas_set_pixels(self.p, _ptr(a)))
+
+    def pixels(self) -> np.ndarray:
+        out = np.empty((self.height, self.width, 3), np.float32)
+        self._check(self.lib.fs_canvas_get_pixels(self.p, _ptr(out)))
+        return out
+
+    def set_colors(self, line, fill) -> None:
+        l_, f_ = np.asarray(line, np.float32), np.asarray(fill, np.float32)
+        self._check(self.lib.fs_canvas_set_colors(self.p, _ptr(l_), _ptr(f_)))
+
+    def colors(self) -> np.ndarray:
+        l_, f_ = np.empty(3, np.float32), np.empty(3, np.float32)
+        self._check(self.lib.fs_canvas_get_colors(self.p, _ptr(l_), _ptr(f_)))
+        return np.concatenate([l_, f_])
+
+    def bytes(self) -> np.ndarray:
+        out = np.empty((self.height, self.width, 3), np.uint8)
+        self._check(self.lib.fs_canvas_get_bytes(self.p, _ptr(out)))
+        return out
+
+    def write_ppm(self, path: str) -> None:
+        self._check(self.lib.fs_canvas_write_ppm(self.p, path.encode()))
 
 
 class Snapshot:

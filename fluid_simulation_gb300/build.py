@@ -5,7 +5,8 @@ C++ drop-in classes over the C ABI).  Each .cu file is compiled to its own
 object in parallel; the library links the CUDA runtime statically.
 
 ``-fmad=false`` keeps every float product and sum separately rounded (the
-kernels also spell this out with __f*_rn intrinsics), which the bit-exact
+kernels also spell this out with __f*_rn intrinsics), and ``-ffp-contract=off``
+does the same for host code (the renderer's weight table), which the bit-exact
 parity with the reference's CPU code relies on.
 """
 from __future__ import annotations
@@ -25,6 +26,7 @@ LIB = os.path.join(BUILD, "libfsgpu.so")
 DROPIN_LIB = os.path.join(BUILD, "libfsgpu_dropin.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-fmad=false", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
+              "-Xcompiler", "-ffp-contract=off",
               "-I", os.path.join(ROOT, "include"), "-I", CSRC]
 
 

@@ -9,6 +9,7 @@
 #include <string>
 #include <vector>
 
+#include "fs_render.h"
 #include "fs_step.h"
 
 using namespace fs;
@@ -1072,6 +1073,28 @@ int fs_snapshot_destroy(fs_saved_state* sn)
     cudaFree(sn->parts);
     cudaFree(sn->misc);
     delete sn;
+    return FS_OK;
+}
+
+int fs_render(fs_handle* h, fs_canvas* c, int what, const float* area)
+{
+    if (!h || !c || !area) return h ? fail(h, FS_ERR_INVALID_ARGUMENT, "null render argument") : FS_ERR_INVALID_ARGUMENT;
+    if (c->device != h->device) return fail(h, FS_ERR_INVALID_ARGUMENT, "canvas on another device");
+    cudaSetDevice(h->device);
+    const Launch L = h->L();
+    const View v = render_view(area, c->width, c->height);
+    cudaError_t e = cudaSuccess;
+    switch (what) {
+        case FS_RENDER_CLEAR: render_clear(L, c); break;
+        case FS_RENDER_CELLS: render_cells(L, c, v, h->g, h->labels); break;
+        case FS_RENDER_VELOCITIES: render_velocities(L, c, v, h->g, UF(h), VF(h)); break;
+        case FS_RENDER_PARTICLES: render_particles(L, c, v, h->px, h->py, h->n_part); break;
+        case FS_RENDER_METABALLS: e = render_metaballs(L, c, v, h->px, h->py, h->n_part); break;
+        default: return fail(h, FS_ERR_INVALID_ARGUMENT, "unknown render pass");
+    }
+    if (e == cudaSuccess) e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);  // the canvas is read from any stream
+    if (e != cudaSuccess) return cuda_fail(h, e, "render");
     return FS_OK;
 }
 

@@ -92,6 +92,11 @@ struct SplatWork
     int64_t cap_items = 0;
     int64_t cells = 0;
 };
+// Groups items 0..n-1 by key (keys[k] < nbins; keys[k] == nbins: left out):
+// bin_start[0..nbins] (nbins + 1 entries) and sorted[], each bin's items in
+// increasing k.  bin_count holds nbins + 1 ints, scan_tmp scan_tmp_ints(nbins).
+void group_by_key(const Launch& L, int64_t n, const uint32_t* keys, int64_t nbins, int32_t* bin_count,
+                  int32_t* bin_start, int32_t* scan_tmp, int32_t* sorted);
 // Buffers for up to `items` items over `cells` cells (frees what w held).
 cudaError_t splat_alloc(SplatWork& w, int64_t items, int64_t cells);
 void splat_free(SplatWork& w);

@@ -48,6 +48,14 @@ __global__ void __launch_bounds__(DOMAIN_TPB) k_splat_keys(Seg one, const Seg* _
     atomicAdd(&bin_count[key], 1);
 }
 
+__global__ void k_bin_count(int64_t n, uint32_t invalid, const uint32_t* __restrict__ keys, int32_t* __restrict__ count)
+{
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const uint32_t key = keys[k];
+    if (key != invalid) atomicAdd(&count[key], 1);
+}
+
 // Item k goes to position bin_start[key] + (its rank among the bin's items
 // in arrival order, counted down on the bin's count).
 __global__ void k_bin_scatter(int64_t n, uint32_t invalid, const uint32_t* __restrict__ keys,
@@ -160,6 +168,23 @@ struct SplatGather
 };
 
 }  // namespace
+
+void group_by_key(const Launch& L, int64_t n, const uint32_t* keys, int64_t nbins, int32_t* bin_count,
+                  int32_t* bin_start, int32_t* scan_tmp, int32_t* sorted)
+{
+    cudaMemsetAsync(bin_count, 0, sizeof(int32_t) * (size_t)(nbins + 1), L.stream);
+    if (n > 0) {
+        k_bin_count<<<domain_blocks(n), DOMAIN_TPB, 0, L.stream>>>(n, (uint32_t)nbins, keys, bin_count);
+        L.count();
+    }
+    scan_exclusive_i32(L, bin_count, bin_start, nbins, scan_tmp);
+    if (n > 0) {
+        k_bin_scatter<<<domain_blocks(n), DOMAIN_TPB, 0, L.stream>>>(n, (uint32_t)nbins, keys, bin_start, bin_count,
+                                                                      sorted);
+        k_bin_sort<<<domain_blocks(nbins), DOMAIN_TPB, 0, L.stream>>>(nbins, bin_start, sorted);
+        L.count(2);
+    }
+}
 
 cudaError_t splat_alloc(SplatWork& w, int64_t items, int64_t cells)
 {

@@ -242,6 +242,39 @@ FS_API int fs_snapshot(fs_handle* h, fs_saved_state** out);
 FS_API int fs_restore(fs_handle* h, const fs_saved_state* snap);
 FS_API int fs_snapshot_destroy(fs_saved_state* snap);
 
+/* Headless renderer: Renderer (src/Renderer.cpp) drawing a handle's state
+ * onto a Canvas (src/Canvas.cpp) of width * height RGB floats in device
+ * memory, bit-identical to the reference's CPU drawing.  A new canvas is
+ * white with a black line colour and a white fill colour, as Canvas(w, h).
+ * area = {x_min, x_max, y_min, y_max}, the world rectangle of Renderer(area).
+ * Passes: FS_RENDER_CLEAR (clearCanvas), FS_RENDER_CELLS
+ * (renderGridCellsToCanvas), FS_RENDER_VELOCITIES (renderGridVelocitiesToCanvas),
+ * FS_RENDER_PARTICLES (renderParticlesToCanvas), FS_RENDER_METABALLS
+ * (renderMetaBallsToCanvas); each draws over what the canvas holds and leaves
+ * the line / fill colours the reference leaves.  fs_render returns after the
+ * pass; pixels are rows of {r, g, b} floats. */
+#define FS_RENDER_CLEAR 0
+#define FS_RENDER_CELLS 1
+#define FS_RENDER_VELOCITIES 2
+#define FS_RENDER_PARTICLES 3
+#define FS_RENDER_METABALLS 4
+
+typedef struct fs_canvas fs_canvas;
+FS_API int fs_canvas_create(int width, int height, int device, fs_canvas** out);
+FS_API int fs_canvas_destroy(fs_canvas* c);
+/* NULL c: the message of the last failed fs_canvas_create on this thread. */
+FS_API const char* fs_canvas_last_error(const fs_canvas* c);
+FS_API int fs_canvas_set_pixels(fs_canvas* c, const float* rgb);
+FS_API int fs_canvas_get_pixels(fs_canvas* c, float* rgb);
+FS_API int fs_canvas_set_colors(fs_canvas* c, const float* line_rgb, const float* fill_rgb);
+FS_API int fs_canvas_get_colors(fs_canvas* c, float* line_rgb, float* fill_rgb);
+/* Renderer::writeCanvasToPpm's bytes: CLAMP(c, 0, 1) * 255 truncated, 3 per pixel. */
+FS_API int fs_canvas_get_bytes(fs_canvas* c, uint8_t* rgb8);
+/* Renderer::writeCanvasToPpm: a binary PPM (P6) of those bytes. */
+FS_API int fs_canvas_write_ppm(fs_canvas* c, const char* path);
+FS_API int64_t fs_canvas_kernel_launches(const fs_canvas* c);
+FS_API int fs_render(fs_handle* h, fs_canvas* c, int what, const float* area);
+
 /* Pressure projection alone (no particles): the
  * Poisson system of FluidSolver::pressureSolve (src/FluidSolver.cpp:363-425)
  * built from a label grid (FS_LIQUID = unknown, FS_AIR = pressure 0,

@@ -3,7 +3,7 @@
 * ``oracle/_build/libfsoracle.so`` -- the C restatement ``oracle/fs_oracle.c``.
   Built on every machine (this container and the GPU machine).
 * ``oracle/_ref/libfsref.so`` -- the reference's own sources
-  ``src/{FluidSolver,FluidDomain,MacGrid,MarkerParticleSet,LevelSet}.cpp``,
+  ``src/{FluidSolver,FluidDomain,MacGrid,MarkerParticleSet,LevelSet,Canvas,Renderer}.cpp``,
   compiled where they lie under the reference checkout (``$FS_REFERENCE_DIR``,
   default ``/root/reference``) against the project's Eigen-subset stand-in
   ``oracle/eigen_shim`` plus ``oracle/ref_harness.cpp``.  Built only when the
@@ -26,7 +26,7 @@ BUILD_DIR = os.path.join(HERE, "_build")
 REF_DIR = os.path.join(HERE, "_ref")
 RESTATEMENT_SO = os.path.join(BUILD_DIR, "libfsoracle.so")
 REFERENCE_SO = os.path.join(REF_DIR, "libfsref.so")
-REFERENCE_SOURCES = ("FluidSolver", "FluidDomain", "MacGrid", "MarkerParticleSet", "LevelSet")
+REFERENCE_SOURCES = ("FluidSolver", "FluidDomain", "MacGrid", "MarkerParticleSet", "LevelSet", "Canvas", "Renderer")
 FLAGS = ["-O3", "-DNDEBUG", "-ffp-contract=off", "-fPIC", "-fno-fast-math"]
 
 

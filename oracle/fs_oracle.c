@@ -1208,3 +1208,182 @@ int fso_poisson_solve(int nx, int ny, float lx, float ly, const uint8_t* labels,
     fso_destroy(s);
     return nf;
 }
+
+
+/* ---- Canvas and Renderer (Canvas.cpp, Renderer.cpp): rendering to an RGB float canvas ---- */
+
+typedef struct
+{
+    int w, h;
+    float* px;       /* 3 floats per pixel, row-major */
+    float line[3];
+    float fill[3];
+} fso_canvas;
+
+static void cv_set(fso_canvas* c, int i, int j, const float* col)
+{
+    float* p = c->px + 3 * ((size_t)i + (size_t)j * (size_t)c->w);
+    p[0] = col[0];
+    p[1] = col[1];
+    p[2] = col[2];
+}
+
+/* Canvas::fillRectangle (Canvas.cpp:76-97): bounds clamped through MyFloat,
+ * border pixels in the line colour, inside in the fill colour. */
+static void cv_fill_rect(fso_canvas* c, int x0, int x1, int y0, int y1)
+{
+    x0 = clampi_ref(x0, 0, c->w - 1);
+    x1 = clampi_ref(x1, 0, c->w - 1);
+    y0 = clampi_ref(y0, 0, c->h - 1);
+    y1 = clampi_ref(y1, 0, c->h - 1);
+    for (int j = y0; j <= y1; ++j)
+        for (int i = x0; i <= x1; ++i)
+            cv_set(c, i, j, (i == x0 || i == x1 || j == y0 || j == y1) ? c->line : c->fill);
+}
+
+/* Canvas::drawLine (Canvas.cpp:39-62): one pixel per unit of length, stopping
+ * at the first pixel outside the canvas. */
+static void cv_draw_line(fso_canvas* c, int fx, int fy, int tx, int ty)
+{
+    const float diff_x = (float)(tx - fx);
+    const float diff_y = (float)(ty - fy);
+    const float distance = sqrtf(diff_x * diff_x + diff_y * diff_y);
+    for (int i = 0; (float)i < distance; ++i) {
+        const int x = (int)((float)fx + (diff_x / distance) * (float)i);
+        const int y = (int)((float)fy + (diff_y / distance) * (float)i);
+        if (x < 0 || x >= c->w || y < 0 || y >= c->h) break;
+        cv_set(c, x, y, c->line);
+    }
+}
+
+/* The pixel mapping shared by the Renderer functions (Renderer.cpp:23-27). */
+typedef struct
+{
+    float scale_x, scale_y, translate_x, translate_y;
+} fso_view;
+
+static fso_view view_of(const float* area, int w, int h)
+{
+    fso_view v;
+    v.scale_x = (float)w / (area[1] - area[0]);
+    v.scale_y = (float)h / (area[3] - area[2]);
+    v.translate_x = (float)(0.5 * (double)(area[0] * (float)w));
+    v.translate_y = (float)(0.5 * (double)(area[2] * (float)h));
+    return v;
+}
+
+#ifndef M_PI /* strict C11 leaves it out; the value glibc's math.h gives */
+#define M_PI 3.14159265358979323846
+#endif
+
+/* gaussian (MathDefinitions.h:29-34) with MyFloat arguments. */
+static float gaussian_ref(float x, float sigma, float mu)
+{
+    const float a = (float)(1 / ((double)sigma * sqrt(2 * M_PI)));
+    const float xm = x - mu;
+    return a * expf(-(xm * xm) / (2 * sigma * sigma));
+}
+
+/* Renderer::renderMetaBallsToCanvas's kernel weight of offset (i, j), radius 5
+ * (Renderer.cpp:186-187). */
+float fso_metaball_weight(int i, int j)
+{
+    const float t = clampf_ref((float)(sqrt((double)(i * i + j * j)) / 5), 0, 1);
+    return gaussian_ref(t, 0.4f, 0.0f);
+}
+
+static void render(fso_sim* s, int what, const float* area, fso_canvas* c)
+{
+    const fso_view v = view_of(area, c->w, c->h);
+    if (what == FSO_RENDER_CLEAR) { /* Renderer::clearCanvas (Renderer.cpp:13-16) */
+        const float white[3] = {1, 1, 1};
+        for (int j = 0; j < c->h; ++j)
+            for (int i = 0; i < c->w; ++i) cv_set(c, i, j, white);
+    } else if (what == FSO_RENDER_CELLS) { /* renderGridCellsToCanvas (Renderer.cpp:18-56) */
+        const float csx = s->dx * v.scale_x, csy = s->dy * v.scale_y;
+        c->line[0] = c->line[1] = c->line[2] = 1;
+        for (int j = 0; j < s->ny; ++j)
+            for (int i = 0; i < s->nx; ++i) {
+                const uint8_t t = s->labels[IDX(s, i, j)];
+                if (t == FSO_LIQUID) { c->fill[0] = 0.7f; c->fill[1] = 0.7f; c->fill[2] = 1; }
+                else if (t == FSO_AIR) { c->fill[0] = 1; c->fill[1] = 1; c->fill[2] = 1; }
+                else { c->fill[0] = 0.5f; c->fill[1] = 0.5f; c->fill[2] = 0.5f; }
+                cv_fill_rect(c, (int)(-v.translate_x + (float)i * csx), (int)(-v.translate_x + (float)(i + 1) * csx),
+                             (int)(-v.translate_y + (float)j * csy), (int)(-v.translate_y + (float)(j + 1) * csy));
+            }
+    } else if (what == FSO_RENDER_VELOCITIES) { /* renderGridVelocitiesToCanvas (Renderer.cpp:93-139) */
+        const float csx = s->dx * v.scale_x, csy = s->dy * v.scale_y;
+        const float line_scale = 5;
+        for (int j = 0; j < s->ny - 1; ++j)
+            for (int i = 0; i < s->nx - 1; ++i) {
+                /* MacGrid::velX / velY (MacGrid.h:30-39): the cell's two faces averaged */
+                const float vel_x = (UF(s)[IDX(s, i, j)] + UF(s)[IDX(s, i + 1, j)]) / 2;
+                const float vel_y = (VF(s)[IDX(s, i, j)] + VF(s)[IDX(s, i, j + 1)]) / 2;
+                const int from_x = (int)((double)(-v.translate_x) + (0.5 + i) * (double)csx);
+                const int from_y = (int)((double)(-v.translate_y) + (0.5 + j) * (double)csy);
+                const int to_x = (int)((float)from_x + vel_x * line_scale);
+                const int to_y = (int)((float)from_y + vel_y * line_scale);
+                const float len = (float)sqrt((double)((from_x - to_x) * (from_x - to_x) +
+                                                       (from_y - to_y) * (from_y - to_y)));
+                const float ls = len / (float)(c->w / 40);
+                const float blue = clampf_ref(1 - ls, 0, 1);
+                const float green = clampf_ref(ls, 0, 1) - clampf_ref(ls - 1, 0, 1);
+                const float red = clampf_ref(ls - 1, 0, 1);
+                c->line[0] = red;
+                c->line[1] = green;
+                c->line[2] = blue;
+                cv_draw_line(c, from_x, from_y, to_x, to_y);
+            }
+    } else if (what == FSO_RENDER_PARTICLES) { /* renderParticlesToCanvas (Renderer.cpp:141-161) */
+        c->line[0] = c->fill[0] = 0.3f;
+        c->line[1] = c->fill[1] = 0.6f;
+        c->line[2] = c->fill[2] = 0.9f;
+        for (int64_t k = 0; k < s->n_part; ++k) {
+            const int x = (int)(-v.translate_x + v.scale_x * s->part[4 * k]);
+            const int y = (int)(-v.translate_y + v.scale_y * s->part[4 * k + 1]);
+            cv_fill_rect(c, x - 3 / 2, x + 3 / 2, y - 3 / 2, y + 3 / 2); /* Canvas::drawPoint (Canvas.cpp:64-74) */
+        }
+    } else if (what == FSO_RENDER_METABALLS) { /* renderMetaBallsToCanvas (Renderer.cpp:163-215) */
+        const int w = c->w, h = c->h;
+        float* df = (float*)xcalloc((size_t)w * h, sizeof(float));
+        c->line[0] = 0.5f; c->line[1] = 0.9f; c->line[2] = 1.0f;
+        c->fill[0] = 0.0f; c->fill[1] = 0.5f; c->fill[2] = 0.7f;
+        for (int64_t k = 0; k < s->n_part; ++k) {
+            const int x = (int)(-v.translate_x + v.scale_x * s->part[4 * k]);
+            const int y = (int)(-v.translate_y + v.scale_y * s->part[4 * k + 1]);
+            for (int j = -5; j < 5; ++j)
+                for (int i = -5; i < 5; ++i) {
+                    const float t = fso_metaball_weight(i, j);
+                    const int xi = x + i, yj = y + j;
+                    if (xi >= 0 && xi < w && yj >= 0 && yj < h) df[(size_t)xi + (size_t)yj * w] += t;
+                }
+        }
+        for (int j = 0; j < h; ++j)
+            for (int i = 0; i < w; ++i) {
+                const double d = df[(size_t)i + (size_t)j * w];
+                if (d > 0.6) cv_set(c, i, j, c->fill);
+                else if (d > 0.2) cv_set(c, i, j, c->line);
+            }
+        free(df);
+    }
+}
+
+void fso_render(fso_sim* s, int what, const float* area, int w, int h, float* rgb, float* colors)
+{
+    fso_canvas c;
+    c.w = w;
+    c.h = h;
+    c.px = rgb;
+    memcpy(c.line, colors, 3 * sizeof(float));
+    memcpy(c.fill, colors + 3, 3 * sizeof(float));
+    render(s, what, area, &c);
+    memcpy(colors, c.line, 3 * sizeof(float));
+    memcpy(colors + 3, c.fill, 3 * sizeof(float));
+}
+
+/* Renderer::writeCanvasToPpm's conversion (Renderer.cpp:217-240): CLAMP to
+ * [0, 1], times 255, truncated to a byte. */
+void fso_canvas_bytes(const float* rgb, int64_t n, uint8_t* out)
+{
+    for (int64_t k = 0; k < 3 * n; ++k) out[k] = (uint8_t)(clampf_ref(rgb[k], 0, 1) * 255);
+}

@@ -131,6 +131,17 @@ int fso_poisson_solve(int size_x, int size_y, float length_x, float length_y, co
 /* Name of the implementation ("restatement" or "reference"). */
 const char* fso_kind(void);
 
+/* Renderer (Renderer.cpp) onto a canvas given as w * h RGB floats (row-major,
+ * in/out) and its line / fill colours (colors[0..2], colors[3..5], in/out);
+ * area = {x_min, x_max, y_min, y_max} in world units. */
+enum { FSO_RENDER_CLEAR = 0, FSO_RENDER_CELLS = 1, FSO_RENDER_VELOCITIES = 2, FSO_RENDER_PARTICLES = 3,
+       FSO_RENDER_METABALLS = 4 };
+void fso_render(fso_sim* s, int what, const float* area, int w, int h, float* rgb, float* colors);
+/* Renderer::writeCanvasToPpm's byte conversion of n RGB pixels. */
+void fso_canvas_bytes(const float* rgb, int64_t n, uint8_t* out);
+/* renderMetaBallsToCanvas's weight of pixel offset (i, j), i, j in [-5, 5). */
+float fso_metaball_weight(int i, int j);
+
 #ifdef __cplusplus
 }
 #endif

@@ -68,6 +68,9 @@ def _lib(kind: str) -> C.CDLL:
         "fso_add_source": (None, [vp, f, f, f, f, f, f, f, f, f, i]),
         "fso_update": (None, [vp, f]),
         "fso_clear_sources": (None, [vp]),
+        "fso_render": (None, [vp, i, vp, i, i, vp, vp]),
+        "fso_canvas_bytes": (None, [vp, i64, vp]),
+        "fso_metaball_weight": (f, [i, i]),
         "fso_kind": (C.c_char_p, []),
         "fso_poisson_solve": (i, [i, i, f, f, vp, vp, i, d, i, d, i, vp, C.POINTER(i), C.POINTER(i),
                                   C.POINTER(d)]),
@@ -85,6 +88,22 @@ def _lib(kind: str) -> C.CDLL:
 
 def _ptr(a: np.ndarray) -> int:
     return a.ctypes.data
+
+
+RENDER_CLEAR, RENDER_CELLS, RENDER_VELOCITIES, RENDER_PARTICLES, RENDER_METABALLS = range(5)
+
+
+def canvas_bytes(canvas: np.ndarray, kind: str = "restatement") -> np.ndarray:
+    """Renderer::writeCanvasToPpm's byte conversion of a (h, w, 3) float32 canvas."""
+    lib = _lib(kind)
+    c = np.ascontiguousarray(canvas, dtype=np.float32)
+    out = np.empty(c.shape, np.uint8)
+    lib.fso_canvas_bytes(_ptr(c), c.shape[0] * c.shape[1], _ptr(out))
+    return out
+
+
+def metaball_weight(i: int, j: int, kind: str = "restatement") -> float:
+    return float(_lib(kind).fso_metaball_weight(i, j))
 
 
 def poisson_solve(labels: np.ndarray, rhs: np.ndarray, length_x: float, length_y: float, method: int, tol: float,
@@ -217,6 +236,13 @@ class OracleSim:
 
     def clear_sources(self) -> None:
         self.lib.fso_clear_sources(self.h)
+
+    def render(self, what: int, area, canvas: np.ndarray, colors: np.ndarray) -> None:
+        """Renderer (Renderer.cpp) onto canvas (h, w, 3) float32 and colors (6,) float32, in place."""
+        a = np.ascontiguousarray(area, dtype=np.float32)
+        assert canvas.dtype == np.float32 and canvas.flags.c_contiguous and colors.dtype == np.float32
+        h, w = canvas.shape[:2]
+        self.lib.fso_render(self.h, what, _ptr(a), w, h, _ptr(canvas), _ptr(colors))
 
     def state(self) -> dict[str, np.ndarray]:
         """Every observable array, for comparisons."""

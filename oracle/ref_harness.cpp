@@ -33,6 +33,8 @@
 #include <FluidSolver.h>
 #include <MacGrid.h>
 #include <MarkerParticleSet.h>
+#include <Canvas.h>
+#include <Renderer.h>
 #undef private
 #undef protected
 
@@ -368,5 +370,57 @@ void fso_add_source(fso_sim* s, float x_min, float x_max, float y_min, float y_m
 void fso_update(fso_sim* s, float dt) { s->domain.update(dt); }
 
 void fso_clear_sources(fso_sim* s) { s->domain.clearFluidSources(); }
+
+// The reference's Renderer on its Canvas, the canvas loaded from and stored
+// back to rgb / colors.
+void fso_render(fso_sim* s, int what, const float* area, int w, int h, float* rgb, float* colors)
+{
+    Canvas canvas(w, h);
+    for (int j = 0; j < h; ++j)
+        for (int i = 0; i < w; ++i) {
+            const float* p = rgb + 3 * ((size_t)i + (size_t)j * w);
+            canvas.setPixel(i, j, Color(p[0], p[1], p[2]));
+        }
+    canvas.setLineColor(Color(colors[0], colors[1], colors[2]));
+    canvas.setFillColor(Color(colors[3], colors[4], colors[5]));
+    Renderer r({area[0], area[1], area[2], area[3]});
+    switch (what) {
+        case FSO_RENDER_CLEAR: r.clearCanvas(canvas); break;
+        case FSO_RENDER_CELLS: r.renderGridCellsToCanvas(s->domain.macGrid(), canvas); break;
+        case FSO_RENDER_VELOCITIES: r.renderGridVelocitiesToCanvas(s->domain.macGrid(), canvas); break;
+        case FSO_RENDER_PARTICLES: r.renderParticlesToCanvas(s->domain.markerParticleSet(), canvas); break;
+        case FSO_RENDER_METABALLS: r.renderMetaBallsToCanvas(s->domain.markerParticleSet(), canvas); break;
+        default: break;
+    }
+    for (int j = 0; j < h; ++j)
+        for (int i = 0; i < w; ++i) {
+            const Color c = canvas.pixel(i, j);
+            float* p = rgb + 3 * ((size_t)i + (size_t)j * w);
+            p[0] = c.r;
+            p[1] = c.g;
+            p[2] = c.b;
+        }
+    const Color lc = canvas.lineColor(), fc = canvas.fillColor();
+    colors[0] = lc.r;
+    colors[1] = lc.g;
+    colors[2] = lc.b;
+    colors[3] = fc.r;
+    colors[4] = fc.g;
+    colors[5] = fc.b;
+}
+
+// The byte conversion of Renderer::writeCanvasToPpm (Renderer.cpp:217-240),
+// written out here because the reference writes it straight to a file.
+void fso_canvas_bytes(const float* rgb, int64_t n, uint8_t* out)
+{
+    for (int64_t k = 0; k < 3 * n; ++k) out[k] = static_cast<unsigned char>(CLAMP(rgb[k], 0, 1) * 255);
+}
+
+float fso_metaball_weight(int i, int j)
+{
+    const int radius = 5;
+    MyFloat t = CLAMP(sqrt((i * i + j * j)) / radius, 0, 1);
+    return gaussian(t, 0.4, 0);
+}
 
 }  // extern "C"

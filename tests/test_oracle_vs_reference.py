@@ -122,3 +122,54 @@ def test_clear_sources_matches_reference():
         a, b = sims[0].state(), sims[1].state()
         for key in a:
             assert np.array_equal(a[key].view(np.uint8), b[key].view(np.uint8)), (k, key)
+
+
+def _render_pair(steps=12):
+    sims = []
+    for kind in ("restatement", "reference"):
+        sc = scenes.dam_break_small()
+        s = po.OracleSim(kind, sc.size_x, sc.size_y, sc.length_x, sc.length_y, sc.density, sc.pic_ratio)
+        s.set_cg(sc.cg_tolerance, 400)
+        s.set_solid_mask(scenes.disc_mask(64, 64, 45.0, 20.0, 8.0))
+        parts = sc.particles.copy()
+        parts[:7, 0] = [-3.0, 70.0, 10.0, 63.9, 0.0, 20.0, 30.0]  # off the canvas and on its edges
+        s.set_particles(parts)
+        for _ in range(steps):
+            s.step(po.STEP_PICFLIP, sc.dt)
+        sims.append(s)
+    return sims
+
+
+@pytest.mark.parametrize("what", [po.RENDER_CLEAR, po.RENDER_CELLS, po.RENDER_VELOCITIES, po.RENDER_PARTICLES,
+                                  po.RENDER_METABALLS])
+# (the reference offsets the canvas by half of x_min * width pixels, so only
+# small offsets of the area keep the drawing on the canvas)
+@pytest.mark.parametrize("size,area", [((96, 80), (0.0, 64.0, 0.0, 64.0)), ((160, 200), (-0.05, 66.0, 0.02, 60.0)),
+                                       ((30, 25), (0.0, 64.0, 0.0, 64.0))])
+def test_renderer_restatement_matches_reference(what, size, area):
+    """Renderer.cpp / Canvas.cpp: the restatement paints the same canvas bit
+    for bit, from a random starting canvas (the renderers draw over it)."""
+    w, h = size
+    rng = np.random.default_rng(what * 7 + w)
+    start = rng.random((h, w, 3), dtype=np.float32)
+    cols = rng.random(6, dtype=np.float32)
+    out = []
+    for s in _render_pair():
+        c, k = start.copy(), cols.copy()
+        s.render(what, area, c, k)
+        out.append((c, k))
+    (a, ka), (b, kb) = out
+    assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+    assert np.array_equal(ka.view(np.uint32), kb.view(np.uint32))
+    if what != po.RENDER_CLEAR:
+        assert not np.array_equal(a, start)  # something was drawn
+
+
+def test_canvas_bytes_and_metaball_weights_match_reference():
+    rng = np.random.default_rng(3)
+    c = (rng.random((40, 50, 3), dtype=np.float32) * 1.4 - 0.2).astype(np.float32)
+    assert np.array_equal(po.canvas_bytes(c, "restatement"), po.canvas_bytes(c, "reference"))
+    for j in range(-5, 5):
+        for i in range(-5, 5):
+            a, b = po.metaball_weight(i, j, "restatement"), po.metaball_weight(i, j, "reference")
+            assert np.float32(a).view(np.uint32) == np.float32(b).view(np.uint32)
