@@ -145,7 +145,12 @@ __global__ void k_vel_mark(int32_t* __restrict__ owner, float* __restrict__ colo
     }
     const float ddx = (float)(L.tx - L.fx), ddy = (float)(L.ty - L.fy);
     const float dist = __fsqrt_rn(fadd(fmul(ddx, ddx), fmul(ddy, ddy)));
-    for (int s = 0; (float)s < dist; ++s) {
+    // Each step moves about one pixel along the line's longer axis (positions
+    // come from the step count, not from accumulation), so a line leaves the
+    // canvas within about 1.5 * max(w, h) steps: the cap never cuts a pixel
+    // the reference paints, and bounds the loop for extreme velocities.
+    const int cap = 2 * (w + h) + 16;
+    for (int s = 0; (float)s < dist && s < cap; ++s) {
         const int x = trunc_i(fadd((float)L.fx, fmul(fdiv(ddx, dist), (float)s)));
         const int y = trunc_i(fadd((float)L.fy, fmul(fdiv(ddy, dist), (float)s)));
         if (x < 0 || x >= w || y < 0 || y >= h) break;
