@@ -31,7 +31,7 @@ CG_FLOAT, CG_DOUBLE = 0, 1
 POISSON_FP32, POISSON_FP64, POISSON_MIXED = 0, 1, 2
 INTEGRATOR_EULER, INTEGRATOR_RK2, INTEGRATOR_RK3 = 0, 1, 2
 SMOKE_FP32, SMOKE_FP64 = 0, 1
-RENDER_CLEAR, RENDER_CELLS, RENDER_VELOCITIES, RENDER_PARTICLES, RENDER_METABALLS = range(5)
+RENDER_CLEAR, RENDER_CELLS, RENDER_VELOCITIES, RENDER_PARTICLES, RENDER_METABALLS, RENDER_LEVEL_SET = range(6)
 TIMED_PHASES = ("classify", "p2g", "forces", "assembly", "cg", "project", "g2p")
 
 
@@ -115,6 +115,10 @@ SIGNATURES = {
     "fs_canvas_write_ppm": (_i, [_vp, C.c_char_p]),
     "fs_canvas_kernel_launches": (_i64, [_vp]),
     "fs_render": (_i, [_vp, _vp, _i, _vp]),
+    "fs_get_level_set": (_i, [_vp, _vp]),
+    "fs_set_level_set": (_i, [_vp, _vp]),
+    "fs_advect_level_set": (_i, [_vp, _f]),
+    "fs_classify_level_set": (_i, [_vp]),
     "fs_synchronize": (_i, [_vp]),
     "fs_get_stats": (_i, [_vp, C.POINTER(fs_step_stats)]),
     "fs_set_timing": (_i, [_vp, _i]),
@@ -342,6 +346,22 @@ class FluidSim:
 
     def reset_particles(self) -> None:
         self._check(self.lib.fs_reset_particles(self.h))
+
+    # level set (FluidDomain::levelSet / advectLevelSet / classifyCells(LevelSet&))
+    def level_set(self) -> np.ndarray:
+        out = np.empty((self.ny, self.nx), np.float32)
+        self._check(self.lib.fs_get_level_set(self.h, _ptr(out)))
+        return out
+
+    def set_level_set(self, ls: np.ndarray) -> None:
+        a = np.ascontiguousarray(ls, dtype=np.float32).reshape(self.ny, self.nx)
+        self._check(self.lib.fs_set_level_set(self.h, _ptr(a)))
+
+    def advect_level_set(self, dt: float) -> None:
+        self._check(self.lib.fs_advect_level_set(self.h, dt))
+
+    def classify_level_set(self) -> None:
+        self._check(self.lib.fs_classify_level_set(self.h))
 
     # rendering (Renderer.cpp onto a device canvas)
     def render(self, canvas: "Canvas", what: int, area) -> None:

@@ -72,6 +72,8 @@ struct fs_handle
     float *u_prev = nullptr, *v_prev = nullptr, *u_diff = nullptr, *v_diff = nullptr;
     uint8_t* labels = nullptr;
     uint8_t* solid = nullptr;
+    float* level_set = nullptr;      // FluidDomain::_level_set
+    float* level_set_tmp = nullptr;  // the new LevelSet of an advection
     uint8_t* vmx[2] = {nullptr, nullptr};
     uint8_t* vmy[2] = {nullptr, nullptr};
     int32_t *fidx = nullptr, *cell_of = nullptr, *counts32 = nullptr;
@@ -329,7 +331,7 @@ void destroy_all(fs_handle* h)
     cudaSetDevice(h->device);
     if (h->stream) cudaStreamSynchronize(h->stream);
     clear_graphs(h);
-    void* ptrs[] = {h->u[0], h->u[1], h->v[0], h->v[1], h->u_prev, h->v_prev, h->u_diff, h->v_diff, h->labels,
+    void* ptrs[] = {h->level_set, h->level_set_tmp, h->u[0], h->u[1], h->v[0], h->v[1], h->u_prev, h->v_prev, h->u_diff, h->v_diff, h->labels,
                     h->solid, h->vmx[0], h->vmx[1], h->vmy[0], h->vmy[1], h->fidx, h->cell_of, h->counts32,
                     h->counts8, h->acc[0], h->acc[1], h->acc[2], h->acc[3], h->grid_tmp, h->sl[0], h->sl[1],
                     h->sl[2], h->sl[3], h->sl[4], h->sl[5], h->sl_ok[0], h->sl_ok[1], h->px, h->py, h->pvx,
@@ -500,6 +502,8 @@ int fs_create(const fs_config* cfg, fs_handle** out)
     A(dalloc(&h->u_diff, N));
     A(dalloc(&h->v_diff, N));
     A(dalloc(&h->labels, N));
+    A(dalloc(&h->level_set, N));
+    A(dalloc(&h->level_set_tmp, N));
     A(dalloc(&h->fidx, N));
     A(dalloc(&h->cell_of, N));
     A(dalloc(&h->counts32, N));
@@ -537,7 +541,8 @@ int fs_create(const fs_config* cfg, fs_handle** out)
             A(cudaMemsetAsync(h->vmx[b], 0, N, h->stream));
             A(cudaMemsetAsync(h->vmy[b], 0, N, h->stream));
         }
-        for (float* p : {h->u_prev, h->v_prev, h->u_diff, h->v_diff, h->cg.x}) A(cudaMemsetAsync(p, 0, N * 4, h->stream));
+        for (float* p : {h->u_prev, h->v_prev, h->u_diff, h->v_diff, h->cg.x, h->level_set})
+            A(cudaMemsetAsync(p, 0, N * 4, h->stream));
         A(cudaMemsetAsync(h->fidx, 0, N * 4, h->stream));
         A(cudaMemsetAsync(h->counts8, 0, N, h->stream));
         A(cudaMemsetAsync(h->d_nfluid, 0, 4, h->stream));
@@ -976,7 +981,7 @@ std::vector<std::pair<void*, size_t>> snapshot_cells(fs_handle* h)
 {
     return {{h->u[0], 4}, {h->u[1], 4}, {h->v[0], 4},   {h->v[1], 4},   {h->u_prev, 4},  {h->v_prev, 4},
             {h->u_diff, 4}, {h->v_diff, 4}, {h->labels, 1}, {h->vmx[0], 1}, {h->vmx[1], 1}, {h->vmy[0], 1},
-            {h->vmy[1], 1}, {h->fidx, 4},  {h->counts8, 1}, {h->cg.x, 4}};
+            {h->vmy[1], 1}, {h->fidx, 4},  {h->counts8, 1}, {h->cg.x, 4},   {h->level_set, 4}};
 }
 
 cudaError_t copy_snapshot(fs_handle* h, fs_saved_state* sn, bool save)
@@ -1076,6 +1081,38 @@ int fs_snapshot_destroy(fs_saved_state* sn)
     return FS_OK;
 }
 
+int fs_get_level_set(fs_handle* h, float* out)
+{
+    if (!h) return FS_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(h->device);
+    return copy_out(h, out, h->level_set, (size_t)h->ncell);
+}
+
+int fs_set_level_set(fs_handle* h, const float* in)
+{
+    if (!h) return FS_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(h->device);
+    return copy_in(h, h->level_set, in, (size_t)h->ncell);
+}
+
+int fs_advect_level_set(fs_handle* h, float dt)
+{
+    if (!h) return FS_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(h->device);
+    advect_level_set(h->L(), domain(h), h->level_set, UF(h), VF(h), dt, h->level_set_tmp);
+    std::swap(h->level_set, h->level_set_tmp);  // _level_set = std::move(new_level_set)
+    clear_graphs(h);                             // no step graph reads the level set, but keep pointers current
+    return check_launch(h, "level set advection");
+}
+
+int fs_classify_level_set(fs_handle* h)
+{
+    if (!h) return FS_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(h->device);
+    classify_level_set(h->L(), domain(h), h->level_set, h->labels, h->solid);
+    return check_launch(h, "level set classification");
+}
+
 int fs_render(fs_handle* h, fs_canvas* c, int what, const float* area)
 {
     if (!h || !c || !area) return h ? fail(h, FS_ERR_INVALID_ARGUMENT, "null render argument") : FS_ERR_INVALID_ARGUMENT;
@@ -1086,7 +1123,8 @@ int fs_render(fs_handle* h, fs_canvas* c, int what, const float* area)
     cudaError_t e = cudaSuccess;
     switch (what) {
         case FS_RENDER_CLEAR: render_clear(L, c); break;
-        case FS_RENDER_CELLS: render_cells(L, c, v, h->g, h->labels); break;
+        case FS_RENDER_CELLS: render_cells(L, c, v, h->g, h->labels, nullptr); break;
+        case FS_RENDER_LEVEL_SET: render_cells(L, c, v, h->g, h->labels, h->level_set); break;
         case FS_RENDER_VELOCITIES: render_velocities(L, c, v, h->g, UF(h), VF(h)); break;
         case FS_RENDER_PARTICLES: render_particles(L, c, v, h->px, h->py, h->n_part); break;
         case FS_RENDER_METABALLS: e = render_metaballs(L, c, v, h->px, h->py, h->n_part); break;

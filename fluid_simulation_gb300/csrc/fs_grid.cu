@@ -313,7 +313,73 @@ struct PressureToGrid
     }
 };
 
+// A grid element by its linear index; 0 past the end of the array (where the
+// reference's std::vector read is undefined).
+__device__ __forceinline__ float at_lin(const float* a, int64_t idx, int64_t n) { return idx < n ? a[idx] : 0.0f; }
+
+// FluidDomain::advectLevelSet (src/FluidDomain.cpp:104-125) as written: its
+// loops run j < sizeX, i < sizeY, so for size_x != size_y several iterations
+// can write one element; element e takes the last of them in loop order
+// (largest j), whose linear index i + j * size_x is e itself.  MacGrid::velX /
+// velY (include/MacGrid.h:30-39) average a face with the next one through the
+// linear index; LevelSet::computeUpwindGradient{X,Y} (src/LevelSet.cpp:27-59)
+// clamp through float.
+struct AdvectLevelSet
+{
+    const float *ls, *uf, *vf;
+    float* out;
+    float dt;
+    __device__ void operator()(const Seg& s, int64_t e, int, int) const
+    {
+        const Geom& g = s.g;
+        const int64_t n = (int64_t)g.nx * g.ny;
+        const int jt = (int)min((int64_t)(g.nx - 1), e / g.nx);
+        const int it = (int)(e - (int64_t)jt * g.nx);
+        if (it >= g.ny) {  // no iteration writes e: the new LevelSet's 0
+            out[e] = 0.0f;
+            return;
+        }
+        const float vel_x = fdiv(fadd(at_lin(uf, e, n), at_lin(uf, e + 1, n)), 2.0f);
+        const float vel_y = fdiv(fadd(at_lin(vf, e, n), at_lin(vf, e + g.nx, n)), 2.0f);
+        auto L = [&](int i, int j) { return ls[(int64_t)i + (int64_t)j * g.nx]; };
+        const int i = clampi(it, 0, g.nx - 1), j = clampi(jt, 0, g.ny - 1);
+        const int ip = clampi(it + 1, 0, g.nx - 1), im = clampi(it - 1, 0, g.nx - 1);
+        const int jp = clampi(jt + 1, 0, g.ny - 1), jm = clampi(jt - 1, 0, g.ny - 1);
+        const float gx = vel_x < 0 ? fsub(L(ip, j), L(i, j)) : fsub(L(i, j), L(im, j));
+        const float gy = vel_y < 0 ? fsub(L(i, jp), L(i, j)) : fsub(L(i, j), L(i, jm));
+        const float change = -fadd(fmul(vel_x, gx), fmul(vel_y, gy));
+        out[e] = fadd(at_lin(ls, e, n), fmul(fmul(change, dt), 5.0f));
+    }
+};
+
+// FluidDomain::classifyCells(LevelSet&) (src/FluidDomain.cpp:127-148), then
+// the persistent solid mask.
+struct ClassifyLevelSet
+{
+    const float* ls;
+    uint8_t* lab;
+    const uint8_t* solid;
+    __device__ void operator()(const Seg& s, int64_t c, int i, int j) const
+    {
+        const bool border = i == 0 || j == 0 || i == s.g.nx - 1 || j == s.g.ny - 1;
+        uint8_t t = ls[c] < 0 ? LIQUID : AIR;
+        if (border || (solid && solid[c])) t = SOLID;
+        lab[c] = t;
+    }
+};
+
 }  // namespace
+
+void advect_level_set(const Launch& L, const Domain& d, const float* ls, const float* uf, const float* vf, float dt,
+                      float* out)
+{
+    each_cell(L, d, AdvectLevelSet{ls, uf, vf, out, dt});
+}
+
+void classify_level_set(const Launch& L, const Domain& d, const float* ls, uint8_t* lab, const uint8_t* solid)
+{
+    each_cell(L, d, ClassifyLevelSet{ls, lab, solid});
+}
 
 void labels_clear(const Launch& L, const Domain& d, uint8_t* lab) { each_cell(L, d, LabelsClear{lab}); }
 

@@ -140,6 +140,11 @@ void project(const Launch& L, const Domain& d, const int32_t* fidx, const int32_
              float* uf, float* vf, float* ub, float* vb, float dt);
 void pressure_to_grid(const Launch& L, const Domain& d, const int32_t* fidx, const int32_t* nfluid,
                       const float* x, float* out);
+// The level set (one simulation): FluidDomain::advectLevelSet into out, and
+// FluidDomain::classifyCells(LevelSet&).
+void advect_level_set(const Launch& L, const Domain& d, const float* ls, const float* uf, const float* vf, float dt,
+                      float* out);
+void classify_level_set(const Launch& L, const Domain& d, const float* ls, uint8_t* lab, const uint8_t* solid);
 
 // ---- particle kernels (fs_particles.cu) ----------------------------------
 enum G2PMode

@@ -75,14 +75,22 @@ __device__ __forceinline__ void cell_fill(uint8_t t, float& r, float& g, float& 
     else { r = 0.5f; g = 0.5f; b = 0.5f; }
 }
 
-// Renderer::renderGridCellsToCanvas (Renderer.cpp:18-56).
+// Renderer::renderGridCellsToCanvas (Renderer.cpp:18-56), or with level-set
+// values (lsv non-null) renderLevelSetFunctionValuesToCanvas (:58-91), whose
+// cells are filled with (value, value, value).
+__device__ __forceinline__ void cell_color(const uint8_t* lab, const float* lsv, size_t c, float& r, float& g, float& b)
+{
+    if (lsv) r = g = b = lsv[c];
+    else cell_fill(lab[c], r, g, b);
+}
+
 __global__ void k_cells(float* __restrict__ px, float* __restrict__ colors, int w, int h, View v, float csx,
-                        float csy, int nx, int ny, const uint8_t* __restrict__ lab)
+                        float csy, int nx, int ny, const uint8_t* __restrict__ lab, const float* __restrict__ lsv)
 {
     const int64_t k = (int64_t)blockIdx.x * TPB + threadIdx.x;
     if (k == 0) {  // the canvas's colours afterwards: white lines, the last cell's fill
         float r, g, b;
-        cell_fill(lab[(size_t)(nx - 1) + (size_t)(ny - 1) * nx], r, g, b);
+        cell_color(lab, lsv, (size_t)(nx - 1) + (size_t)(ny - 1) * nx, r, g, b);
         colors[0] = colors[1] = colors[2] = 1.0f;
         colors[3] = r;
         colors[4] = g;
@@ -97,7 +105,7 @@ __global__ void k_cells(float* __restrict__ px, float* __restrict__ colors, int 
     const bool border = X == bound(ntx, csx, i, w) || X == bound(ntx, csx, i + 1, w) || Y == bound(nty, csy, j, h) ||
                         Y == bound(nty, csy, j + 1, h);
     float r = 1.0f, g = 1.0f, b = 1.0f;
-    if (!border) cell_fill(lab[(size_t)i + (size_t)j * nx], r, g, b);
+    if (!border) cell_color(lab, lsv, (size_t)i + (size_t)j * nx, r, g, b);
     put(px, w, X, Y, r, g, b);
 }
 
@@ -355,11 +363,12 @@ void render_clear(const Launch& L, fs_canvas* c)
     L.count();
 }
 
-void render_cells(const Launch& L, fs_canvas* c, const View& v, const Geom& g, const uint8_t* labels)
+void render_cells(const Launch& L, fs_canvas* c, const View& v, const Geom& g, const uint8_t* labels,
+                  const float* level_set)
 {
     const float csx = g.dx * v.scale_x, csy = g.dy * v.scale_y;
     k_cells<<<nblk((int64_t)c->width * c->height), TPB, 0, L.stream>>>(c->px, c->colors, c->width, c->height, v, csx,
-                                                                        csy, g.nx, g.ny, labels);
+                                                                        csy, g.nx, g.ny, labels, level_set);
     L.count();
 }
 

@@ -33,7 +33,9 @@ View render_view(const float* area, int width, int height);
 
 // The render passes, on L.stream (st = the simulation's state).
 void render_clear(const Launch& L, fs_canvas* c);
-void render_cells(const Launch& L, fs_canvas* c, const View& v, const Geom& g, const uint8_t* labels);
+// labels' cell types, or with level_set non-null the level-set values
+void render_cells(const Launch& L, fs_canvas* c, const View& v, const Geom& g, const uint8_t* labels,
+                  const float* level_set);
 void render_velocities(const Launch& L, fs_canvas* c, const View& v, const Geom& g, const float* uf, const float* vf);
 void render_particles(const Launch& L, fs_canvas* c, const View& v, const float* px, const float* py, int64_t n);
 cudaError_t render_metaballs(const Launch& L, fs_canvas* c, const View& v, const float* px, const float* py, int64_t n);

@@ -434,33 +434,24 @@ void FluidDomain::classifyCells(MarkerParticleSet&)
     deviceUpdated();
 }
 
-// src/FluidDomain.cpp:129-148 (host; no step uses the level set).
-void FluidDomain::classifyCells(LevelSet& level_set)
+// src/FluidDomain.cpp:127-148 on the GPU; like the reference it labels from
+// the domain's own level set, whatever level set is passed.
+void FluidDomain::classifyCells(LevelSet&)
 {
-    _mac_grid.clearCellTypeBuffer();
-    for (int j = 0; j < _mac_grid.sizeY(); ++j)
-        for (int i = 0; i < _mac_grid.sizeX(); ++i) {
-            if (level_set(i, j) < 0) _mac_grid.setCellType(i, j, LIQUID);
-            if (i == 0 || j == 0 || i == _mac_grid.sizeX() - 1 || j == _mac_grid.sizeY() - 1)
-                _mac_grid.setCellType(i, j, SOLID);
-        }
+    pushToDevice();
+    check(_h, fs_set_level_set(_h, _level_set.raw()));
+    check(_h, fs_classify_level_set(_h));
+    deviceUpdated();
 }
 
-// src/FluidDomain.cpp:104-127 (host), including its loop bounds, which run j
-// over sizeX and i over sizeY.
+// src/FluidDomain.cpp:104-125 on the GPU (the level set goes to the device,
+// is advected there with the device's velocities, and comes back).
 void FluidDomain::advectLevelSet(MyFloat dt)
 {
-    LevelSet next(_level_set.sizeX(), _level_set.sizeY(), _level_set.lengthX(), _level_set.lengthY());
-    for (int j = 0; j < _level_set.sizeX(); ++j)
-        for (int i = 0; i < _level_set.sizeY(); ++i) {
-            const MyFloat vx = _mac_grid.velX(i, j);
-            const MyFloat vy = _mac_grid.velY(i, j);
-            const MyFloat gx = _level_set.computeUpwindGradientX(i, j, vx);
-            const MyFloat gy = _level_set.computeUpwindGradientY(i, j, vy);
-            const MyFloat rate = -(vx * gx + vy * gy);
-            next(i, j) = _level_set(i, j) + rate * dt * 5;
-        }
-    _level_set = std::move(next);
+    pushToDevice();
+    check(_h, fs_set_level_set(_h, _level_set.raw()));
+    check(_h, fs_advect_level_set(_h, dt));
+    check(_h, fs_get_level_set(_h, _level_set.raw()));
 }
 
 // ---------------------------------------------------------------- FluidSolverMemoryPool / FluidSolver

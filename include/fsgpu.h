@@ -231,6 +231,20 @@ FS_API int fs_num_fluid_sources(fs_handle* h, int* n);
 FS_API int fs_set_fluid_source_state(fs_handle* h, int index, float time_since_last, int n_spawns);
 FS_API int fs_reset_particles(fs_handle* h);
 
+/* The level-set path the reference keeps beside the particle labelling
+ * (FluidDomain::levelSet / advectLevelSet / classifyCells(LevelSet&),
+ * src/FluidDomain.cpp:104-148, src/LevelSet.cpp): the level set is
+ * size_x * size_y floats, zero at creation.  The advection follows the
+ * reference as written (loops over j < size_x, i < size_y; velocities through
+ * the linear index); where the reference reads past the end of its arrays
+ * (the last row) the read is 0 here.  Classification leaves a SOLID border,
+ * LIQUID where the level set is negative, AIR elsewhere, then applies the
+ * persistent solid mask. */
+FS_API int fs_get_level_set(fs_handle* h, float* out);
+FS_API int fs_set_level_set(fs_handle* h, const float* in);
+FS_API int fs_advect_level_set(fs_handle* h, float dt);
+FS_API int fs_classify_level_set(fs_handle* h);
+
 /* Snapshots: a device copy of a handle's simulation state -- the eight
  * velocity grids, labels, extension masks, fluid indices, particle counts,
  * pressure, particles, the last CG result and warnings, buffer parities and
@@ -258,6 +272,7 @@ FS_API int fs_snapshot_destroy(fs_saved_state* snap);
 #define FS_RENDER_VELOCITIES 2
 #define FS_RENDER_PARTICLES 3
 #define FS_RENDER_METABALLS 4
+#define FS_RENDER_LEVEL_SET 5 /* renderLevelSetFunctionValuesToCanvas */
 
 typedef struct fs_canvas fs_canvas;
 FS_API int fs_canvas_create(int width, int height, int device, fs_canvas** out);

@@ -60,6 +60,8 @@ struct fso_sim
     int vfront;           /* index of the front valid-mask buffers */
     float *sum_u, *sum_v, *w_u, *w_v;
 
+    float* level_set;     /* FluidDomain::_level_set (LevelSet.cpp:3-13: zero) */
+
     float* part;          /* {x, y, vx, vy} per particle */
     int64_t n_part, cap_part;
 
@@ -202,6 +204,7 @@ fso_sim* fso_create(int nx, int ny, float lx, float ly, float density, float pic
     s->u_diff = (float*)xcalloc(n, sizeof(float));
     s->v_diff = (float*)xcalloc(n, sizeof(float));
     s->labels = (uint8_t*)xcalloc(n, 1);
+    s->level_set = (float*)xcalloc(n, sizeof(float));
     s->fidx = (int32_t*)xcalloc(n, sizeof(int32_t));
     s->counts = (uint8_t*)xcalloc(n, 1);
     s->sum_u = (float*)xcalloc(n, sizeof(float));
@@ -243,7 +246,7 @@ void fso_destroy(fso_sim* s)
     free(s->u_prev); free(s->v_prev); free(s->u_diff); free(s->v_diff);
     free(s->labels); free(s->solid); free(s->fidx); free(s->counts);
     free(s->sum_u); free(s->sum_v); free(s->w_u); free(s->w_v);
-    free(s->part); free(s->pressure); free(s->src);
+    free(s->part); free(s->pressure); free(s->src); free(s->level_set);
     free(s->cg_b); free(s->cg_x); free(s->cg_r); free(s->cg_p); free(s->cg_q); free(s->cg_z);
     free(s->cg_diag); free(s->cg_inv); free(s->cg_down); free(s->cg_up); free(s->cg_left);
     free(s->cg_right); free(s->cg_acc); free(s->cg_accf); free(s->cg_nns);
@@ -1343,6 +1346,16 @@ static void render(fso_sim* s, int what, const float* area, fso_canvas* c)
             const int y = (int)(-v.translate_y + v.scale_y * s->part[4 * k + 1]);
             cv_fill_rect(c, x - 3 / 2, x + 3 / 2, y - 3 / 2, y + 3 / 2); /* Canvas::drawPoint (Canvas.cpp:64-74) */
         }
+    } else if (what == FSO_RENDER_LEVEL_SET) { /* renderLevelSetFunctionValuesToCanvas (Renderer.cpp:58-91) */
+        const float csx = s->dx * v.scale_x, csy = s->dy * v.scale_y;
+        c->line[0] = c->line[1] = c->line[2] = 1;
+        for (int j = 0; j < s->ny; ++j)
+            for (int i = 0; i < s->nx; ++i) {
+                const float val = s->level_set[IDX(s, i, j)];
+                c->fill[0] = c->fill[1] = c->fill[2] = val;
+                cv_fill_rect(c, (int)(-v.translate_x + (float)i * csx), (int)(-v.translate_x + (float)(i + 1) * csx),
+                             (int)(-v.translate_y + (float)j * csy), (int)(-v.translate_y + (float)(j + 1) * csy));
+            }
     } else if (what == FSO_RENDER_METABALLS) { /* renderMetaBallsToCanvas (Renderer.cpp:163-215) */
         const int w = c->w, h = c->h;
         float* df = (float*)xcalloc((size_t)w * h, sizeof(float));
@@ -1386,4 +1399,77 @@ void fso_render(fso_sim* s, int what, const float* area, int w, int h, float* rg
 void fso_canvas_bytes(const float* rgb, int64_t n, uint8_t* out)
 {
     for (int64_t k = 0; k < 3 * n; ++k) out[k] = (uint8_t)(clampf_ref(rgb[k], 0, 1) * 255);
+}
+
+
+/* ---- level set (FluidDomain.cpp:104-148, LevelSet.cpp:27-59) ------------ */
+
+void fso_get_level_set(const fso_sim* s, float* out) { memcpy(out, s->level_set, (size_t)s->nx * s->ny * sizeof(float)); }
+void fso_set_level_set(fso_sim* s, const float* in) { memcpy(s->level_set, in, (size_t)s->nx * s->ny * sizeof(float)); }
+
+/* An element of a grid by its linear index; 0 past the end, where the
+ * reference's std::vector read is undefined. */
+static float at_lin(const float* a, size_t idx, size_t n) { return idx < n ? a[idx] : 0.0f; }
+
+/* LevelSet::computeUpwindGradientX / Y (LevelSet.cpp:27-59). */
+static float upwind_x(const fso_sim* s, int i, int j, float vel)
+{
+    int ip = i + 1, im = i - 1;
+    i = clampi_ref(i, 0, s->nx - 1);
+    j = clampi_ref(j, 0, s->ny - 1);
+    ip = clampi_ref(ip, 0, s->nx - 1);
+    im = clampi_ref(im, 0, s->nx - 1);
+    const float* L = s->level_set;
+    return vel < 0 ? L[IDX(s, ip, j)] - L[IDX(s, i, j)] : L[IDX(s, i, j)] - L[IDX(s, im, j)];
+}
+
+static float upwind_y(const fso_sim* s, int i, int j, float vel)
+{
+    int jp = j + 1, jm = j - 1;
+    i = clampi_ref(i, 0, s->nx - 1);
+    j = clampi_ref(j, 0, s->ny - 1);
+    jp = clampi_ref(jp, 0, s->ny - 1);
+    jm = clampi_ref(jm, 0, s->ny - 1);
+    const float* L = s->level_set;
+    return vel < 0 ? L[IDX(s, i, jp)] - L[IDX(s, i, j)] : L[IDX(s, i, j)] - L[IDX(s, i, jm)];
+}
+
+/* FluidDomain::advectLevelSet (FluidDomain.cpp:104-125) as written: the loops
+ * run j < sizeX, i < sizeY; MacGrid::velX / velY (MacGrid.h:30-39) average the
+ * cell's face with the next one through the linear index (Grid.h:27-31); an
+ * access past the end of an array reads 0 and a write past it is dropped. */
+void fso_advect_level_set(fso_sim* s, float dt)
+{
+    const size_t n = (size_t)s->nx * s->ny, nx = (size_t)s->nx;
+    float* nl = (float*)xcalloc(n, sizeof(float));
+    for (int j = 0; j < s->nx; ++j)
+        for (int i = 0; i < s->ny; ++i) {
+            const size_t lin = (size_t)i + (size_t)j * nx;
+            const float vel_x = (at_lin(UF(s), lin, n) + at_lin(UF(s), lin + 1, n)) / 2;
+            const float vel_y = (at_lin(VF(s), lin, n) + at_lin(VF(s), lin + nx, n)) / 2;
+            const float gx = upwind_x(s, i, j, vel_x);
+            const float gy = upwind_y(s, i, j, vel_y);
+            const float change = -(vel_x * gx + vel_y * gy);
+            const float v = at_lin(s->level_set, lin, n) + change * dt * 5;
+            if (lin < n) nl[lin] = v;
+        }
+    memcpy(s->level_set, nl, n * sizeof(float));
+    free(nl);
+}
+
+/* FluidDomain::classifyCells(LevelSet&) (FluidDomain.cpp:127-148): border
+ * SOLID, negative level set LIQUID, else AIR; then the persistent solid mask,
+ * as after the particle classification. */
+void fso_classify_level_set(fso_sim* s)
+{
+    for (int j = 0; j < s->ny; ++j)
+        for (int i = 0; i < s->nx; ++i) {
+            uint8_t t = (i > 0 && j > 0 && i < s->nx - 1 && j < s->ny - 1) ? FSO_AIR : FSO_SOLID;
+            if (s->level_set[IDX(s, i, j)] < 0) t = FSO_LIQUID;
+            if (i == 0 || j == 0 || i == s->nx - 1 || j == s->ny - 1) t = FSO_SOLID;
+            s->labels[IDX(s, i, j)] = t;
+        }
+    if (s->solid)
+        for (size_t c = 0; c < (size_t)s->nx * s->ny; ++c)
+            if (s->solid[c]) s->labels[c] = FSO_SOLID;
 }

@@ -135,8 +135,15 @@ const char* fso_kind(void);
  * in/out) and its line / fill colours (colors[0..2], colors[3..5], in/out);
  * area = {x_min, x_max, y_min, y_max} in world units. */
 enum { FSO_RENDER_CLEAR = 0, FSO_RENDER_CELLS = 1, FSO_RENDER_VELOCITIES = 2, FSO_RENDER_PARTICLES = 3,
-       FSO_RENDER_METABALLS = 4 };
+       FSO_RENDER_METABALLS = 4, FSO_RENDER_LEVEL_SET = 5 };
 void fso_render(fso_sim* s, int what, const float* area, int w, int h, float* rgb, float* colors);
+/* The level set (FluidDomain::levelSet, LevelSet.h), size_x * size_y floats. */
+void fso_get_level_set(const fso_sim* s, float* out);
+void fso_set_level_set(fso_sim* s, const float* in);
+/* FluidDomain::advectLevelSet (FluidDomain.cpp:104-125). */
+void fso_advect_level_set(fso_sim* s, float dt);
+/* FluidDomain::classifyCells(LevelSet&) (FluidDomain.cpp:127-148). */
+void fso_classify_level_set(fso_sim* s);
 /* Renderer::writeCanvasToPpm's byte conversion of n RGB pixels. */
 void fso_canvas_bytes(const float* rgb, int64_t n, uint8_t* out);
 /* renderMetaBallsToCanvas's weight of pixel offset (i, j), i, j in [-5, 5). */

@@ -69,6 +69,10 @@ def _lib(kind: str) -> C.CDLL:
         "fso_update": (None, [vp, f]),
         "fso_clear_sources": (None, [vp]),
         "fso_render": (None, [vp, i, vp, i, i, vp, vp]),
+        "fso_get_level_set": (None, [vp, vp]),
+        "fso_set_level_set": (None, [vp, vp]),
+        "fso_advect_level_set": (None, [vp, f]),
+        "fso_classify_level_set": (None, [vp]),
         "fso_canvas_bytes": (None, [vp, i64, vp]),
         "fso_metaball_weight": (f, [i, i]),
         "fso_kind": (C.c_char_p, []),
@@ -90,7 +94,7 @@ def _ptr(a: np.ndarray) -> int:
     return a.ctypes.data
 
 
-RENDER_CLEAR, RENDER_CELLS, RENDER_VELOCITIES, RENDER_PARTICLES, RENDER_METABALLS = range(5)
+RENDER_CLEAR, RENDER_CELLS, RENDER_VELOCITIES, RENDER_PARTICLES, RENDER_METABALLS, RENDER_LEVEL_SET = range(6)
 
 
 def canvas_bytes(canvas: np.ndarray, kind: str = "restatement") -> np.ndarray:
@@ -236,6 +240,21 @@ class OracleSim:
 
     def clear_sources(self) -> None:
         self.lib.fso_clear_sources(self.h)
+
+    def level_set(self) -> np.ndarray:
+        out = np.empty((self.ny, self.nx), np.float32)
+        self.lib.fso_get_level_set(self.h, _ptr(out))
+        return out
+
+    def set_level_set(self, ls: np.ndarray) -> None:
+        a = np.ascontiguousarray(ls, dtype=np.float32).reshape(self.ny, self.nx)
+        self.lib.fso_set_level_set(self.h, _ptr(a))
+
+    def advect_level_set(self, dt: float) -> None:
+        self.lib.fso_advect_level_set(self.h, dt)
+
+    def classify_level_set(self) -> None:
+        self.lib.fso_classify_level_set(self.h)
 
     def render(self, what: int, area, canvas: np.ndarray, colors: np.ndarray) -> None:
         """Renderer (Renderer.cpp) onto canvas (h, w, 3) float32 and colors (6,) float32, in place."""

@@ -83,15 +83,20 @@ bool stock_ok(const fso_sim* s)
     return s->use_stock && s->solid.empty() && s->gx == 0.0f && s->gy == -9.82f && s->n_ext == 2;
 }
 
+// The persistent solid mask (an extension), applied after a classification.
+void apply_solid_mask(fso_sim* s)
+{
+    if (s->solid.empty()) return;
+    MacGrid& g = s->domain.macGrid();
+    for (int j = 0; j < g.sizeY(); ++j)
+        for (int i = 0; i < g.sizeX(); ++i)
+            if (s->solid[static_cast<size_t>(i + j * g.sizeX())]) g.setCellType(i, j, SOLID);
+}
+
 void classify(fso_sim* s)
 {
     s->domain.classifyCells(s->domain.markerParticleSet());
-    if (!s->solid.empty()) {
-        MacGrid& g = s->domain.macGrid();
-        for (int j = 0; j < g.sizeY(); ++j)
-            for (int i = 0; i < g.sizeX(); ++i)
-                if (s->solid[static_cast<size_t>(i + j * g.sizeX())]) g.setCellType(i, j, SOLID);
-    }
+    apply_solid_mask(s);
 }
 
 void pressure(fso_sim* s, float dt)
@@ -390,6 +395,7 @@ void fso_render(fso_sim* s, int what, const float* area, int w, int h, float* rg
         case FSO_RENDER_VELOCITIES: r.renderGridVelocitiesToCanvas(s->domain.macGrid(), canvas); break;
         case FSO_RENDER_PARTICLES: r.renderParticlesToCanvas(s->domain.markerParticleSet(), canvas); break;
         case FSO_RENDER_METABALLS: r.renderMetaBallsToCanvas(s->domain.markerParticleSet(), canvas); break;
+        case FSO_RENDER_LEVEL_SET: r.renderLevelSetFunctionValuesToCanvas(s->domain.levelSet(), canvas); break;
         default: break;
     }
     for (int j = 0; j < h; ++j)
@@ -414,6 +420,28 @@ void fso_render(fso_sim* s, int what, const float* area, int w, int h, float* rg
 void fso_canvas_bytes(const float* rgb, int64_t n, uint8_t* out)
 {
     for (int64_t k = 0; k < 3 * n; ++k) out[k] = static_cast<unsigned char>(CLAMP(rgb[k], 0, 1) * 255);
+}
+
+void fso_get_level_set(const fso_sim* s, float* out)
+{
+    const LevelSet& L = s->domain.levelSet();
+    for (int j = 0; j < L.sizeY(); ++j)
+        for (int i = 0; i < L.sizeX(); ++i) out[i + (size_t)j * L.sizeX()] = L.value(i, j);
+}
+
+void fso_set_level_set(fso_sim* s, const float* in)
+{
+    LevelSet& L = s->domain.levelSet();
+    for (int j = 0; j < L.sizeY(); ++j)
+        for (int i = 0; i < L.sizeX(); ++i) L(i, j) = in[i + (size_t)j * L.sizeX()];
+}
+
+void fso_advect_level_set(fso_sim* s, float dt) { s->domain.advectLevelSet(dt); }
+
+void fso_classify_level_set(fso_sim* s)
+{
+    s->domain.classifyCells(s->domain.levelSet());
+    apply_solid_mask(s);
 }
 
 float fso_metaball_weight(int i, int j)

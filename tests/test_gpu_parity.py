@@ -323,3 +323,37 @@ def test_cg_barrier_timeout_is_reported_and_the_handle_recovers():
         g.step(fsg.STEP_PICFLIP, sc.dt)
         o.step(po.STEP_PICFLIP, sc.dt)
         assert_same(g.state(), o.state(), where="after recovery, step %d" % k)
+
+
+@pytest.mark.parametrize("shape", [(64, 64), (40, 64)])
+def test_level_set_path_matches_oracle(shape):
+    """FluidDomain::advectLevelSet and classifyCells(LevelSet&) on the device,
+    square and narrow grids (the reference's swapped loop bounds), several
+    advections interleaved with steps, then the level-set render pass."""
+    nx, ny = shape
+    sc = scenes.dam_break_small()
+    g = fsg.FluidSim(nx, ny, float(nx), float(ny), 0.005, 0.02, cg_tolerance=1e-6, cg_max_iterations=400)
+    o = po.OracleSim("restatement", nx, ny, float(nx), float(ny), 0.005, 0.02)
+    o.set_cg(1e-6, 400)
+    parts = scenes.block_particles(nx, ny, float(nx), float(ny), 1, nx // 2, 1, ny // 2, 4, 9)
+    g.set_particles(parts)
+    o.set_particles(parts)
+    jj, ii = np.meshgrid(np.arange(ny), np.arange(nx), indexing="ij")
+    ls = (np.hypot(ii + 0.5 - nx / 3, jj + 0.5 - ny / 3) - nx / 5).astype(np.float32)
+    g.set_level_set(ls)
+    o.set_level_set(ls)
+    for k in range(4):
+        g.step(fsg.STEP_PICFLIP, sc.dt)
+        o.step(po.STEP_PICFLIP, sc.dt)
+        g.advect_level_set(0.05)
+        o.advect_level_set(0.05)
+        assert np.array_equal(g.level_set().view(np.uint32), o.level_set().view(np.uint32)), k
+    g.classify_level_set()
+    o.classify_level_set()
+    assert np.array_equal(g.labels(), o.labels())
+    c = fsg.Canvas(90, 70)
+    g.render(c, fsg.RENDER_LEVEL_SET, (0.0, float(nx), 0.0, float(ny)))
+    ref, k6 = np.ones((70, 90, 3), np.float32), np.array([0, 0, 0, 1, 1, 1], np.float32)
+    o.render(po.RENDER_LEVEL_SET, (0.0, float(nx), 0.0, float(ny)), ref, k6)
+    assert np.array_equal(c.pixels().view(np.uint32), ref.view(np.uint32))
+    assert np.array_equal(c.colors().view(np.uint32), k6.view(np.uint32))

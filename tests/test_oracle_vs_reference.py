@@ -173,3 +173,51 @@ def test_canvas_bytes_and_metaball_weights_match_reference():
         for i in range(-5, 5):
             a, b = po.metaball_weight(i, j, "restatement"), po.metaball_weight(i, j, "reference")
             assert np.float32(a).view(np.uint32) == np.float32(b).view(np.uint32)
+
+
+def _level_set_pair(nx, ny, steps=6):
+    sims = []
+    for kind in ("restatement", "reference"):
+        s = po.OracleSim(kind, nx, ny, float(nx), float(ny), 0.005, 0.02)
+        s.set_cg(1e-6, 400)
+        s.set_particles(scenes.block_particles(nx, ny, float(nx), float(ny), 1, nx // 2, 1, ny // 2, 4, 9))
+        for _ in range(steps):
+            s.step(po.STEP_PICFLIP, 0.005)
+        jj, ii = np.meshgrid(np.arange(ny), np.arange(nx), indexing="ij")
+        s.set_level_set((np.hypot(ii + 0.5 - nx / 3, jj + 0.5 - ny / 3) - nx / 5).astype(np.float32))
+        sims.append(s)
+    return sims
+
+
+def test_level_set_square_grid_matches_reference():
+    """FluidDomain::advectLevelSet on a square grid: every row but the last,
+    whose velocities the reference reads past the end of its arrays; then
+    classifyCells(LevelSet&) and the level-set render pass."""
+    a, b = _level_set_pair(64, 64)
+    for s in (a, b):
+        s.advect_level_set(0.05)
+    la, lb = a.level_set(), b.level_set()
+    assert np.array_equal(la[:-1].view(np.uint32), lb[:-1].view(np.uint32))
+    assert not np.array_equal(la[:-1], _level_set_pair(64, 64, steps=0)[0].level_set()[:-1])
+    for s in (a, b):
+        s.set_level_set(la)  # the same (defined) field on both, then classify and draw it
+        s.classify_level_set()
+    assert np.array_equal(a.labels(), b.labels())
+    start = np.random.default_rng(1).random((70, 90, 3), dtype=np.float32)
+    out = []
+    for s in (a, b):
+        c, k = start.copy(), np.zeros(6, np.float32)
+        s.render(po.RENDER_LEVEL_SET, (0.0, 64.0, 0.0, 64.0), c, k)
+        out.append((c, k))
+    assert np.array_equal(out[0][0].view(np.uint32), out[1][0].view(np.uint32))
+    assert np.array_equal(out[0][1].view(np.uint32), out[1][1].view(np.uint32))
+
+
+def test_level_set_narrow_grid_matches_reference_everywhere():
+    """size_x < size_y: the swapped loop bounds (FluidDomain.cpp:111-113) alias
+    writes but stay inside the arrays, so every cell is defined and equal."""
+    a, b = _level_set_pair(40, 64)
+    for k in range(3):
+        for s in (a, b):
+            s.advect_level_set(0.05)
+        assert np.array_equal(a.level_set().view(np.uint32), b.level_set().view(np.uint32)), k
