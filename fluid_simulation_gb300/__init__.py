@@ -28,7 +28,8 @@ STEP_SEMI_LAGRANGIAN, STEP_PIC, STEP_FLIP, STEP_PICFLIP = range(4)
  PH_G2P_PICFLIP, PH_G2P_PIC, PH_G2P_FLIP, PH_ADVECT_SAFE, PH_ADVECT, PH_SL_VELOCITY, PH_SL_PARTICLES,
  PH_SWAP) = range(16)
 CG_FLOAT, CG_DOUBLE = 0, 1
-POISSON_FP32, POISSON_FP64, POISSON_MIXED = 0, 1, 2
+POISSON_FP32, POISSON_FP64, POISSON_MIXED, POISSON_MGPCG = 0, 1, 2, 3
+SOLVER_JACOBI_PCG, SOLVER_MGPCG = 0, 1
 INTEGRATOR_EULER, INTEGRATOR_RK2, INTEGRATOR_RK3 = 0, 1, 2
 SMOKE_FP32, SMOKE_FP64 = 0, 1
 RENDER_CLEAR, RENDER_CELLS, RENDER_VELOCITIES, RENDER_PARTICLES, RENDER_METABALLS, RENDER_LEVEL_SET = range(6)
@@ -78,6 +79,7 @@ SIGNATURES = {
     "fs_set_cg": (_i, [_vp, _d, _i]),
     "fs_set_cg_precision": (_i, [_vp, _i]),
     "fs_set_extension_iterations": (_i, [_vp, _i]),
+    "fs_set_pressure_solver": (_i, [_vp, _i]),
     "fs_set_solid_mask": (_i, [_vp, _vp]),
     "fs_set_particles": (_i, [_vp, _vp, _i64]),
     "fs_set_particles_device": (_i, [_vp, _vp, _i64]),
@@ -254,6 +256,10 @@ class FluidSim:
     def set_cg_precision(self, precision: int) -> None:
         """CG_FLOAT (0, the reference's precision) or CG_DOUBLE (1)."""
         self._check(self.lib.fs_set_cg_precision(self.h, int(precision)))
+
+    def set_pressure_solver(self, solver: int) -> None:
+        """SOLVER_JACOBI_PCG (the reference's, bit-exact) or SOLVER_MGPCG (multigrid-preconditioned)."""
+        self._check(self.lib.fs_set_pressure_solver(self.h, int(solver)))
 
     def set_gravity(self, gx: float, gy: float) -> None:
         self._check(self.lib.fs_set_gravity(self.h, gx, gy))

@@ -9,6 +9,7 @@
 #include <string>
 #include <vector>
 
+#include "fs_mg.h"
 #include "fs_render.h"
 #include "fs_step.h"
 
@@ -111,6 +112,10 @@ struct fs_handle
     int cg_maxit = 100;
     int cg_fp64 = 0;
     int n_ext = 2;
+    int solver = FS_SOLVER_JACOBI_PCG;
+    MgSolver* mg = nullptr;  // FS_SOLVER_MGPCG, made on first use
+    float* mg_b = nullptr;
+    cudaError_t mg_error = cudaSuccess;
 
     bool timing = false;
     bool graphs = true;
@@ -246,6 +251,22 @@ Domain domain(const fs_handle* h) { return Domain::single(seg(h)); }
 void solve_hook(void* owner, const Launch& L)
 {
     fs_handle* h = static_cast<fs_handle*>(owner);
+    if (h->solver == FS_SOLVER_MGPCG) {
+        // the system on the cell grid, its solution back in fluid-index order
+        mg_set_labels(h->mg, L.stream, h->labels, L.counter);
+        mg_fluid_to_cells<float>(L, h->ncell, h->fidx, h->d_nfluid, h->cg_b, h->mg_b);
+        int iters = 0;
+        double rr = 0, bb = 0;
+        float* xc = nullptr;
+        cudaError_t e = mg_solve(h->mg, L.stream, h->mg_b, h->cg_tol, h->cg_maxit, L.counter, &iters, &rr, &bb, &xc);
+        if (e == cudaSuccess) {
+            mg_cells_to_fluid<float>(L, h->ncell, h->d_nfluid, h->cell_of, xc, h->cg.x);
+            const CgResult r{iters, 0, rr, bb};
+            e = cudaMemcpy(h->cg.result, &r, sizeof(r), cudaMemcpyHostToDevice);
+        }
+        if (e != cudaSuccess && h->mg_error == cudaSuccess) h->mg_error = e;
+        return;
+    }
     cg_solve(L, h->cg, h->d_nfluid, h->cg_b, h->diag_tab, h->cg_down, h->cg_up, h->cg_flags, h->off, h->cg_tol,
              h->cg_maxit, h->cg_fp64, h->d_status);
 }
@@ -304,10 +325,17 @@ StepState state(fs_handle* h)
     return st;
 }
 
-void run_step(fs_handle* h, int method, float dt)
+int run_step(fs_handle* h, int method, float dt)
 {
     StepState st = state(h);
     enqueue_step(h->L(), st, method, dt);
+    if (h->mg_error != cudaSuccess) {
+        cudaGetLastError();
+        const cudaError_t e = h->mg_error;
+        h->mg_error = cudaSuccess;
+        return cuda_fail(h, e, "multigrid pressure solve");
+    }
+    return FS_OK;
 }
 
 int check_launch(fs_handle* h, const char* what)
@@ -340,6 +368,8 @@ void destroy_all(fs_handle* h)
                     h->cg_flags, h->d_nfluid, h->d_status, h->d_warn, h->scan_tmp};
     for (void* p : ptrs) cudaFree(p);
     splat_free(h->sw);
+    mg_destroy(h->mg);
+    cudaFree(h->mg_b);
     for (DevSource& src : h->sources) {
         cudaFree(src.d_xs);
         cudaFree(src.d_ys);
@@ -610,6 +640,22 @@ int fs_set_cg_precision(fs_handle* h, int precision)
     return FS_OK;
 }
 
+int fs_set_pressure_solver(fs_handle* h, int solver)
+{
+    if (!h || (solver != FS_SOLVER_JACOBI_PCG && solver != FS_SOLVER_MGPCG))
+        return h ? fail(h, FS_ERR_INVALID_ARGUMENT, "unknown pressure solver") : FS_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(h->device);
+    if (solver == FS_SOLVER_MGPCG && !h->mg) {
+        if (mg_create(&h->mg, h->g.nx, h->g.ny, h->g.dx, h->device) != 0)
+            return fail(h, FS_ERR_OUT_OF_MEMORY, "multigrid levels");
+        const cudaError_t e = dalloc(&h->mg_b, (size_t)h->ncell);
+        if (e != cudaSuccess) return cuda_fail(h, e, "multigrid right-hand side");
+    }
+    if (solver != h->solver) clear_graphs(h);
+    h->solver = solver;
+    return FS_OK;
+}
+
 int fs_set_extension_iterations(fs_handle* h, int n)
 {
     if (!h || n < 0) return h ? fail(h, FS_ERR_INVALID_ARGUMENT, "negative extension iterations") : 1;
@@ -796,9 +842,10 @@ int fs_step(fs_handle* h, int method, float dt)
         if (e != cudaSuccess) return cuda_fail(h, e, "semi-Lagrangian scratch");
     }
     h->timed_valid = h->timing;
-    if (!h->graphs || h->timing) {  // per-phase events are recorded by direct launches
-        run_step(h, method, dt);
-        return check_launch(h, "step");
+    // per-phase events are recorded by direct launches; the multigrid solve polls its flag from the host
+    if (!h->graphs || h->timing || h->solver == FS_SOLVER_MGPCG) {
+        const int rc = run_step(h, method, dt);
+        return rc ? rc : check_launch(h, "step");
     }
     const uint32_t db = float_bits(dt);
     for (auto& ge : h->graph_cache) {
@@ -837,8 +884,8 @@ int fs_step(fs_handle* h, int method, float dt)
         h->graphs = false;
         h->front = ge.front_in;
         h->vfront = ge.vfront_in;
-        run_step(h, method, dt);
-        return check_launch(h, "step");
+        const int rc = run_step(h, method, dt);
+        return rc ? rc : check_launch(h, "step");
     }
     e = cudaGraphInstantiate(&ge.exec, graph, 0);
     cudaGraphDestroy(graph);
@@ -847,8 +894,8 @@ int fs_step(fs_handle* h, int method, float dt)
         h->graphs = false;
         h->front = ge.front_in;
         h->vfront = ge.vfront_in;
-        run_step(h, method, dt);
-        return check_launch(h, "step");
+        const int rc = run_step(h, method, dt);
+        return rc ? rc : check_launch(h, "step");
     }
     if (h->graph_cache.size() >= 8) {  // particle counts that changed (fluid sources) leave unused graphs
         cudaGraphExecDestroy(h->graph_cache.front().exec);

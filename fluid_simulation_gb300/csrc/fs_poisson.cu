@@ -19,7 +19,7 @@
 #include <string>
 #include <vector>
 
-#include "fs_internal.h"
+#include "fs_mg.h"
 
 namespace fs {
 namespace {
@@ -426,6 +426,9 @@ struct fs_poisson
     Mat64 m{};
     int grid64 = 0;
     bool ready = false;
+    MgSolver* mg = nullptr;  // FS_POISSON_MGPCG, made on first use
+    float* mg_b = nullptr;   // its right-hand side on the cells
+    bool mg_labels = false;  // its cell types are those of the current problem
     int64_t launches = 0;
     cudaEvent_t ev[2] = {};
 };
@@ -457,6 +460,8 @@ void destroy(fs_poisson* p)
     for (void* q : ptrs) cudaFree(q);
     for (auto& e : p->ev)
         if (e) cudaEventDestroy(e);
+    mg_destroy(p->mg);
+    cudaFree(p->mg_b);
     if (p->stream) cudaStreamDestroy(p->stream);
     delete p;
 }
@@ -489,7 +494,28 @@ int solve_impl(fs_poisson* p, int method, double tol, int max_iterations, double
     cudaMemsetAsync(p->status, 0, 4, p->stream);
     cudaEventRecord(p->ev[0], p->stream);
     const int fp64dots = inner_precision == FS_CG_DOUBLE ? 1 : 0;
-    if (method == FS_POISSON_FP32) {
+    if (method == FS_POISSON_MGPCG) {
+        if (!p->mg) {
+            if (mg_create(&p->mg, p->g.nx, p->g.ny, p->g.dx, p->device) != 0)
+                return fail(FS_ERR_OUT_OF_MEMORY, "multigrid levels");
+            if (cudaMalloc(&p->mg_b, 4 * (size_t)p->ncell) != cudaSuccess)
+                return fail(FS_ERR_OUT_OF_MEMORY, "multigrid right-hand side");
+            p->mg_labels = false;
+        }
+        if (!p->mg_labels) {
+            mg_set_labels(p->mg, p->stream, p->labels, &p->launches);
+            p->mg_labels = true;
+        }
+        mg_fluid_to_cells<double>(L, p->ncell, p->fidx, p->nfluid, p->b, p->mg_b);
+        int iters = 0;
+        double rr = 0, bb = 0;
+        float* xc = nullptr;
+        const cudaError_t e = mg_solve(p->mg, p->stream, p->mg_b, tol, max_iterations, &p->launches, &iters, &rr, &bb, &xc);
+        if (e != cudaSuccess) return cuda_check(e, "multigrid solve");
+        mg_cells_to_fluid<double>(L, p->ncell, p->nfluid, p->cell_of, xc, p->x);
+        st.inner_iterations = iters;
+        st.outer_iterations = 1;
+    } else if (method == FS_POISSON_FP32) {
         k_to_f32<<<nb, 256, 0, p->stream>>>(p->nfluid, p->b, p->b32);
         cg_solve(L, p->cg, p->nfluid, p->b32, p->diag32, p->down, p->up, p->flags, p->off32, tol, max_iterations,
                  fp64dots, p->status);
@@ -678,6 +704,7 @@ FS_API int fs_poisson_set_problem(fs_poisson* p, const uint8_t* labels, const do
     p->m.up = p->up;
     p->m.flags = p->flags;
     p->ready = true;
+    p->mg_labels = false;
     return cuda_check(cudaStreamSynchronize(p->stream), "fs_poisson_set_problem");
 }
 
@@ -685,7 +712,8 @@ FS_API int fs_poisson_solve(fs_poisson* p, int method, double tol, int max_itera
                             int inner_precision, fs_poisson_stats* stats)
 {
     if (!p || !p->ready || !(tol >= 0) || max_iterations < 0 ||
-        (method != FS_POISSON_FP32 && method != FS_POISSON_FP64 && method != FS_POISSON_MIXED))
+        (method != FS_POISSON_FP32 && method != FS_POISSON_FP64 && method != FS_POISSON_MIXED &&
+         method != FS_POISSON_MGPCG))
         return fail(FS_ERR_INVALID_ARGUMENT, "invalid Poisson solve");
     cudaSetDevice(p->device);
     return solve_impl(p, method, tol, max_iterations, inner_tolerance, inner_precision, stats);
@@ -726,6 +754,7 @@ int poisson_set_labels_device(fs_poisson* p, const uint8_t* d_labels)
     p->m.up = p->up;
     p->m.flags = p->flags;
     p->ready = true;
+    p->mg_labels = false;
     return cuda_check(cudaStreamSynchronize(p->stream), "Poisson labels");
 }
 

@@ -160,6 +160,14 @@ FS_API int fs_set_gravity(fs_handle* h, float gx, float gy);
 FS_API int fs_set_cg(fs_handle* h, double tolerance, int max_iterations);
 FS_API int fs_set_cg_precision(fs_handle* h, int precision);
 FS_API int fs_set_extension_iterations(fs_handle* h, int n);
+/* Pressure solver of the step.  FS_SOLVER_JACOBI_PCG (default): the
+ * reference's Jacobi-preconditioned CG, bit-exact.  FS_SOLVER_MGPCG: CG
+ * preconditioned by a geometric multigrid V-cycle on the same system, to the
+ * same relative residual -- far fewer iterations, a different converged
+ * pressure (not the reference's result); steps with it are direct launches. */
+#define FS_SOLVER_JACOBI_PCG 0
+#define FS_SOLVER_MGPCG 1
+FS_API int fs_set_pressure_solver(fs_handle* h, int solver);
 /* Persistent solid cells re-applied after every classification (extension;
  * the reference re-labels only the border).  mask: size_x*size_y bytes,
  * non-zero = solid; NULL clears. */
@@ -306,6 +314,10 @@ FS_API int fs_render(fs_handle* h, fs_canvas* c, int what, const float* area);
 #define FS_POISSON_FP32 0
 #define FS_POISSON_FP64 1
 #define FS_POISSON_MIXED 2
+/* Not the reference's method: CG preconditioned by a geometric multigrid
+ * V-cycle on the cell grid (float vectors, double dot products); far fewer
+ * iterations than the Jacobi-preconditioned CG, a different converged x. */
+#define FS_POISSON_MGPCG 3
 
 typedef struct fs_poisson fs_poisson;
 typedef struct fs_poisson_stats
