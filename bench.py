@@ -18,9 +18,12 @@ workload.  Under torchrun (N > 1) every rank runs an independent replica
 (nothing on the data path is exchanged); rank 0 prints.
 
 At N = 1 the line also carries `forms`: the batched form (512 independent
-simulations of sides 32..256 stepped as one graph-replayed batch step) and the
-mixed-precision form (the 4096^2 pressure projection to relative residual
-1e-10 by FP64 iterative refinement around float CG, against an FP64-only CG).
+simulations of sides 32..256 stepped as one graph-replayed batch step), the
+multigrid form (the same 1024^2 workload with a multigrid-preconditioned
+pressure solve, not the reference's solver) and the mixed-precision form (the
+4096^2 pressure projection to relative residual 1e-10 by FP64 iterative
+refinement around float multigrid or Jacobi CG corrections, against an
+FP64-only CG).
 --no-forms skips them; --only-form measures one of them alone.
 """
 from __future__ import annotations
@@ -59,7 +62,7 @@ def parse():
     ap.add_argument("--projection-size", type=int, default=4096, help="grid side of the mixed-precision form")
     ap.add_argument("--batch-plan", type=int, choices=[1, 2, 4, 8], default=None,
                     help="batched form: CG chunks per CTA instead of the autotuner's choice")
-    ap.add_argument("--only-form", choices=["batched", "mixed_precision"], default=None,
+    ap.add_argument("--only-form", choices=["batched", "mixed_precision", "multigrid"], default=None,
                     help="measure one form alone (profiling runs) and print its JSON object")
     return ap.parse_args()
 
@@ -321,7 +324,8 @@ def measure_projection(args, local_rank):
     ps.set_problem(labels, rhs)
     out = {"workload": "%dx%d projection, 5%% solids, N(0,1) rhs, relative residual 1e-10" % (n, n),
            "fluid_cells": int((labels == 0).sum())}
-    for name, method, inner in (("mixed_f32_dots", fsg.POISSON_MIXED, fsg.CG_FLOAT),
+    for name, method, inner in (("mixed_multigrid", fsg.POISSON_MIXED_MG, fsg.CG_FLOAT),
+                                ("mixed_f32_dots", fsg.POISSON_MIXED, fsg.CG_FLOAT),
                                 ("mixed_f64_dots", fsg.POISSON_MIXED, fsg.CG_DOUBLE),
                                 ("fp64", fsg.POISSON_FP64, fsg.CG_FLOAT)):
         st = ps.solve(method, 1e-10, 200000, inner_tol=1e-3, inner_precision=inner)
@@ -329,9 +333,44 @@ def measure_projection(args, local_rank):
                      "inner_iterations": st["inner_iterations"],
                      "cell_solves_per_s": n * n / (st["ms"] / 1000.0)}
     out["speedup_mixed_vs_fp64"] = out["fp64"]["ms"] / out["mixed_f32_dots"]["ms"]
+    out["speedup_mixed_multigrid_vs_fp64"] = out["fp64"]["ms"] / out["mixed_multigrid"]["ms"]
     out["speedup_mixed_f64_dots_vs_fp64"] = out["fp64"]["ms"] / out["mixed_f64_dots"]["ms"]
     ps.close()
     return out
+
+
+def measure_multigrid(args, local_rank, plain_value, flush):
+    """The 1024^2 workload stepped with the multigrid-preconditioned pressure
+    solver (FS_SOLVER_MGPCG) to the same relative residual: not the
+    reference's pressure, reported beside the bit-exact plain path."""
+    import torch
+
+    import fluid_simulation_gb300 as fsg
+
+    sc = workload(args.size)
+    sim = fsg.FluidSim.from_scene(sc, device=local_rank)
+    sim.set_pressure_solver(fsg.SOLVER_MGPCG)
+    for _ in range(args.warmup):
+        sim.step(fsg.STEP_PICFLIP, sc.dt)
+    sim.synchronize()
+    stream = torch.cuda.ExternalStream(sim.stream(), device=local_rank)
+    ms, its = [], []
+    for _ in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+        sim.step(fsg.STEP_PICFLIP, sc.dt)
+        e1.record(stream)
+        st = sim.stats()
+        ms.append(e0.elapsed_time(e1))
+        its.append(st["cg_iterations"])
+    t = sum(ms) / 1000.0
+    value = sc.cells * args.steps / t
+    return {"workload": "the plain workload with the multigrid-preconditioned CG (not the reference's solver)",
+            "value": value, "unit": UNIT, "ms_per_step": 1000.0 * t / args.steps, "vs_plain": value / plain_value,
+            "cg_iterations_mean": float(np.mean(its))}
 
 
 def run_gpu(args, rank, world, local_rank):
@@ -352,6 +391,8 @@ def run_gpu(args, rank, world, local_rank):
             flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda:%d" % local_rank)
             if args.only_form == "batched":
                 out = measure_batched(args, local_rank, float("nan"), flush)
+            elif args.only_form == "multigrid":
+                out = measure_multigrid(args, local_rank, float("nan"), flush)
             else:
                 out = measure_projection(args, local_rank)
             print(json.dumps({"form": args.only_form, **out}), flush=True)
@@ -425,6 +466,7 @@ def run_gpu(args, rank, world, local_rank):
     forms = None
     if world == 1 and not args.no_forms:
         forms = {"batched": measure_batched(args, local_rank, value, flush),
+                 "multigrid": measure_multigrid(args, local_rank, value, flush),
                  "mixed_precision": measure_projection(args, local_rank)}
     # roofline of the dominant kernel (the CG)
     peak, peak_kind = peaks()

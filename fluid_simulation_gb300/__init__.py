@@ -28,7 +28,7 @@ STEP_SEMI_LAGRANGIAN, STEP_PIC, STEP_FLIP, STEP_PICFLIP = range(4)
  PH_G2P_PICFLIP, PH_G2P_PIC, PH_G2P_FLIP, PH_ADVECT_SAFE, PH_ADVECT, PH_SL_VELOCITY, PH_SL_PARTICLES,
  PH_SWAP) = range(16)
 CG_FLOAT, CG_DOUBLE = 0, 1
-POISSON_FP32, POISSON_FP64, POISSON_MIXED, POISSON_MGPCG = 0, 1, 2, 3
+POISSON_FP32, POISSON_FP64, POISSON_MIXED, POISSON_MGPCG, POISSON_MIXED_MG = 0, 1, 2, 3, 4
 SOLVER_JACOBI_PCG, SOLVER_MGPCG = 0, 1
 INTEGRATOR_EULER, INTEGRATOR_RK2, INTEGRATOR_RK3 = 0, 1, 2
 SMOKE_FP32, SMOKE_FP64 = 0, 1

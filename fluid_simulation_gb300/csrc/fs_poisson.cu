@@ -494,7 +494,8 @@ int solve_impl(fs_poisson* p, int method, double tol, int max_iterations, double
     cudaMemsetAsync(p->status, 0, 4, p->stream);
     cudaEventRecord(p->ev[0], p->stream);
     const int fp64dots = inner_precision == FS_CG_DOUBLE ? 1 : 0;
-    if (method == FS_POISSON_MGPCG) {
+    const bool use_mg = method == FS_POISSON_MGPCG || method == FS_POISSON_MIXED_MG;
+    if (use_mg) {
         if (!p->mg) {
             if (mg_create(&p->mg, p->g.nx, p->g.ny, p->g.dx, p->device) != 0)
                 return fail(FS_ERR_OUT_OF_MEMORY, "multigrid levels");
@@ -506,6 +507,8 @@ int solve_impl(fs_poisson* p, int method, double tol, int max_iterations, double
             mg_set_labels(p->mg, p->stream, p->labels, &p->launches);
             p->mg_labels = true;
         }
+    }
+    if (method == FS_POISSON_MGPCG) {
         mg_fluid_to_cells<double>(L, p->ncell, p->fidx, p->nfluid, p->b, p->mg_b);
         int iters = 0;
         double rr = 0, bb = 0;
@@ -553,7 +556,8 @@ int solve_impl(fs_poisson* p, int method, double tol, int max_iterations, double
         st.inner_iterations = r.iterations;
         st.outer_iterations = 1;
     } else {
-        // FP64 iterative refinement around float-vector CG corrections.
+        // FP64 iterative refinement around float-vector corrections (the
+        // Jacobi-preconditioned CG, or the multigrid one for MIXED_MG).
         cudaMemsetAsync(p->x, 0, 8 * (size_t)p->ncell, p->stream);
         k_copy64<<<nb, 256, 0, p->stream>>>(p->nfluid, p->b, p->r);
         p->launches += 1;
@@ -563,15 +567,27 @@ int solve_impl(fs_poisson* p, int method, double tol, int max_iterations, double
         double rr = bb;
         for (int outer = 0; outer < 64; ++outer) {
             if (!(rr >= thr) || bb == 0.0) break;
-            k_to_f32<<<nb, 256, 0, p->stream>>>(p->nfluid, p->r, p->b32);
-            cg_solve(L, p->cg, p->nfluid, p->b32, p->diag32, p->down, p->up, p->flags, p->off32, inner_tolerance,
-                     max_iterations, fp64dots, p->status);
+            CgResult r{};
+            if (method == FS_POISSON_MIXED_MG) {
+                mg_fluid_to_cells<double>(L, p->ncell, p->fidx, p->nfluid, p->r, p->mg_b);
+                double rr_in = 0, bb_in = 0;
+                float* xc = nullptr;
+                const cudaError_t e = mg_solve(p->mg, p->stream, p->mg_b, inner_tolerance, max_iterations, &p->launches,
+                                               &r.iterations, &rr_in, &bb_in, &xc);
+                if (e != cudaSuccess) return cuda_check(e, "multigrid correction");
+                mg_cells_to_fluid<float>(L, p->ncell, p->nfluid, p->cell_of, xc, p->cg.x);
+            } else {
+                k_to_f32<<<nb, 256, 0, p->stream>>>(p->nfluid, p->r, p->b32);
+                cg_solve(L, p->cg, p->nfluid, p->b32, p->diag32, p->down, p->up, p->flags, p->off32, inner_tolerance,
+                         max_iterations, fp64dots, p->status);
+                p->launches += 1;
+            }
             k_add_f32<<<nb, 256, 0, p->stream>>>(p->nfluid, p->cg.x, p->x, 0);
             k_residual64<<<nb, 256, 0, p->stream>>>(p->m, p->nfluid, p->b, p->x, p->r);
-            p->launches += 3;
+            p->launches += 2;
             dot64(p, p->r, p->r, 1);
-            CgResult r{};
-            cudaMemcpyAsync(&r, p->cg.result, sizeof(r), cudaMemcpyDeviceToHost, p->stream);
+            if (method != FS_POISSON_MIXED_MG)
+                cudaMemcpyAsync(&r, p->cg.result, sizeof(r), cudaMemcpyDeviceToHost, p->stream);
             const double rr_new = read_scalar(p, 1);
             st.inner_iterations += r.iterations;
             st.outer_iterations = outer + 1;
@@ -713,7 +729,7 @@ FS_API int fs_poisson_solve(fs_poisson* p, int method, double tol, int max_itera
 {
     if (!p || !p->ready || !(tol >= 0) || max_iterations < 0 ||
         (method != FS_POISSON_FP32 && method != FS_POISSON_FP64 && method != FS_POISSON_MIXED &&
-         method != FS_POISSON_MGPCG))
+         method != FS_POISSON_MGPCG && method != FS_POISSON_MIXED_MG))
         return fail(FS_ERR_INVALID_ARGUMENT, "invalid Poisson solve");
     cudaSetDevice(p->device);
     return solve_impl(p, method, tol, max_iterations, inner_tolerance, inner_precision, stats);

@@ -318,6 +318,8 @@ FS_API int fs_render(fs_handle* h, fs_canvas* c, int what, const float* area);
  * V-cycle on the cell grid (float vectors, double dot products); far fewer
  * iterations than the Jacobi-preconditioned CG, a different converged x. */
 #define FS_POISSON_MGPCG 3
+/* FS_POISSON_MIXED with multigrid-preconditioned float corrections. */
+#define FS_POISSON_MIXED_MG 4
 
 typedef struct fs_poisson fs_poisson;
 typedef struct fs_poisson_stats

@@ -117,3 +117,22 @@ def test_step_with_multigrid_pressure_solver():
     for _ in range(100):
         ref.step(fsg.STEP_PICFLIP, sc.dt)
     assert np.isfinite(ref.particles()).all()
+
+
+def test_mixed_precision_with_multigrid_corrections_reaches_1e10():
+    fsbuild.build()
+    n = 128
+    labels, rhs = scenes.projection_problem(n, seed=11)
+    ps = fsg.PoissonSolver(n, n, float(n), float(n))
+    ps.set_problem(labels, rhs)
+    mm = ps.solve(fsg.POISSON_MIXED_MG, 1e-10, 2000, inner_tol=1e-3)
+    x = ps.solution()
+    mj = ps.solve(fsg.POISSON_MIXED, 1e-10, 20000, inner_tol=1e-3)
+    xd, singular, comp = direct_solve(labels, rhs)
+    for c in singular:
+        m = comp == c
+        x[m] -= x[m].mean()
+    err = np.linalg.norm(x - xd) / np.linalg.norm(xd)
+    print("mixed+MG", mm, "mixed+Jacobi", mj, "error", err)
+    assert mm["residual"] < 1e-10 and err < 1e-8
+    assert mm["inner_iterations"] * 10 < mj["inner_iterations"]
