@@ -357,3 +357,32 @@ def test_level_set_path_matches_oracle(shape):
     o.render(po.RENDER_LEVEL_SET, (0.0, float(nx), 0.0, float(ny)), ref, k6)
     assert np.array_equal(c.pixels().view(np.uint32), ref.view(np.uint32))
     assert np.array_equal(c.colors().view(np.uint32), k6.view(np.uint32))
+
+
+def test_p2g_weight_threshold_edge():
+    """transferVelocityToGridSpread keeps a face's previous back value unless
+    its weight exceeds 1e-6 (src/FluidSolver.cpp:898-917): isolated particles
+    a hair from a grid line put weights just below, at and above it."""
+    n = 32
+    rng = np.random.default_rng(5)
+    offs = np.array([1e-7, 4e-7, 9.9e-7, 1e-6, 1.05e-6, 3e-6, 1 - 1e-7, 1 - 9.9e-7, 1 - 1.05e-6], np.float64)
+    parts = []
+    for k, f in enumerate(offs):
+        i, j = 3 + 3 * k, 4 + (k % 3) * 7
+        parts.append([i + f, j + 0.5 + f, 1.0 + k, -2.0 + k])  # u footprint at (x, y - 0.5)
+        parts.append([i + 0.5 + f, j + 1 - f, -1.0 - k, 3.0 - k])
+    parts = np.array(parts, np.float32)
+    g = fsg.FluidSim(n, n, float(n), float(n), 1.0, 0.0)
+    o = po.OracleSim("restatement", n, n, float(n), float(n), 1.0, 0.0)
+    grids = [rng.standard_normal((n, n)).astype(np.float32) for _ in range(8)]
+    for s in (g, o):
+        for w, arr in enumerate(grids):
+            s.set_grid(w, arr)
+        s.set_particles(parts)
+    g.phase(fsg.PH_P2G, 0.005)
+    o.phase(po.PH_P2G, 0.005)
+    assert_same(g.state(), o.state(), where="P2G threshold")
+    # the edge is exercised: some touched faces kept their old value, others were replaced
+    ub0 = grids[fsg.U_BACK]
+    uf = g.grid(fsg.U_FRONT)  # the back buffer became the front
+    assert (uf == ub0).sum() > 0 and (uf != ub0).sum() > 0

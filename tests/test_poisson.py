@@ -130,3 +130,24 @@ def test_gpu_methods_error_against_fp64_direct_solve():
     print("relative error vs FP64 direct solve:", errs)
     assert errs["fp64"] < 1e-8 and errs["mixed"] < 1e-8, errs
     assert errs["fp32"] < 1e-2, errs
+
+
+def test_restated_float_cg_against_scipy_cg():
+    """The restatement's Jacobi-preconditioned float CG (the reference's
+    solver) against scipy.sparse.linalg.cg and an FP64 direct solve of the
+    same system: same convergence, solutions within the tolerance."""
+    import scipy.sparse.linalg as spla
+
+    n = 48
+    labels, rhs = scenes.projection_problem(n, seed=3)
+    labels = labels.copy()
+    labels[n // 2:, 1:-1][labels[n // 2:, 1:-1] == 0] = 1  # AIR above: nonsingular
+    rhs = np.where(labels == 0, rhs, 0.0)
+    A, b, fluid = _system(labels, rhs)
+    x, st = po.poisson_solve(labels, rhs, float(n), float(n), 0, 1e-6, 5000)
+    xs, info = spla.cg(-A, -b, rtol=1e-6, maxiter=5000, M=spla.LinearOperator(A.shape, matvec=lambda v: v / -A.diagonal()))
+    xd = spla.spsolve(A.tocsc(), b)
+    assert info == 0
+    xr = x[fluid]
+    assert np.linalg.norm(xr - xd) / np.linalg.norm(xd) < 1e-4
+    assert np.linalg.norm(xs - xd) / np.linalg.norm(xd) < 1e-4
