@@ -28,10 +28,12 @@
 // The search direction p_new = z + beta p_old is not exchanged through a third
 // barrier: z and p_old of every cell are published to global memory in the
 // previous phase, and each CTA recomputes p_new of the neighbours it needs
-// with the same float operations.  Each CTA keeps the state of its own cells
-// in shared memory (up to KREG chunks of 1024 cells per CTA, ~200 KB) or, for
-// larger systems, streams it from global memory.  Waits are bounded: a CTA that
-// waits longer than about two seconds sets ST_TIMEOUT and every CTA returns.
+// with the same float operations.  A CTA that owns at most KREG chunks of 1024
+// cells keeps their state in registers and shared memory and stages the p_new
+// values its rows read from other CTAs into a shared-memory halo once per
+// iteration; larger systems stream the state from global memory.  Waits are
+// bounded: a CTA that waits longer than about two seconds sets ST_TIMEOUT and
+// every CTA returns.
 #include "fs_internal.h"
 
 namespace fs {
@@ -39,11 +41,14 @@ namespace {
 
 constexpr int CG_THREADS = 1024;
 constexpr int CHUNK = CG_THREADS;
-constexpr int KREG = 8;                   // chunks per CTA kept in shared memory
-constexpr size_t RESIDENT_BYTES = (size_t)KREG * CHUNK * 25;
+constexpr int KREG = 8;                   // most chunks per CTA in the register-resident form
+constexpr size_t DYN_BYTES = 204800;      // dynamic shared memory of k_cg: 12 B per resident cell + halo
 constexpr int SINGLE_CTA_CHUNKS = 16;       // systems this small run in one CTA
 constexpr int MAX_CHUNKS = 32 * 1024;       // all-read reduction limit (33.5M cells)
 constexpr uint64_t WAIT_LIMIT_NS = 2000000000ull;
+
+// Dynamic shared memory of the cluster kernel with K chunks per CTA.
+__host__ __device__ constexpr size_t cluster_dyn_bytes(int K) { return (size_t)K * CHUNK * 25; }
 
 struct CgArgs
 {
@@ -66,6 +71,7 @@ struct CgArgs
     CgResult* result;
     unsigned missing;          // arrivals the grid barrier waits for beyond the grid (test hook; normally 0)
     uint64_t wait_ns;          // bound of a barrier wait
+    int dyn_bytes;             // dynamic shared memory of the launch
 };
 
 struct Smem
@@ -83,6 +89,7 @@ struct Smem
     float dtab[5];
     float itab[5];
     int flag;
+    int hlo, hhi;  // halo extent of the register-resident body
 };
 
 // Arithmetic of the reduction type R, each operation rounded on its own.
@@ -295,37 +302,10 @@ __device__ __forceinline__ float remote_p(const CgArgs& a, int n, bool first, fl
     return first ? zn : fadd(zn, fmul(beta, __ldcg(&a.p[n])));
 }
 
-// Shared-memory-resident state of this CTA's cells (K > 0): slot s of
-// thread t is element (c0 + s) * CHUNK + t, stored at [s * CHUNK + t].
-struct Resident
-{
-    float* x;
-    float* r;
-    float* zq;  // z, and q between the SpMV and the update
-    float* p;
-    int32_t* dn;
-    int32_t* up;
-    uint8_t* fl;
-};
-
-__device__ __forceinline__ Resident resident(unsigned char* dyn, int K)
-{
-    Resident R;
-    const int n = K * CHUNK;
-    R.x = reinterpret_cast<float*>(dyn);
-    R.r = R.x + n;
-    R.zq = R.r + n;
-    R.p = R.zq + n;
-    R.dn = reinterpret_cast<int32_t*>(R.p + n);
-    R.up = R.dn + n;
-    R.fl = reinterpret_cast<uint8_t*>(R.up + n);
-    return R;
-}
-
-// One CG solve.  K > 0: the CTA's cells (at most K chunks) live in shared
-// memory; K == 0: the state streams from global memory.
-template <int K, typename R, class Sync>
-__device__ __forceinline__ void cg_body(const CgArgs& a, Smem& sm, unsigned char* dyn, int nf, int nchunks, Sync& sync)
+// One CG solve with the state streamed from global memory: the form for
+// CTAs whose cells do not fit the register-resident form below.
+template <typename R, class Sync>
+__device__ __forceinline__ void cg_stream(const CgArgs& a, Smem& sm, int nf, int nchunks, Sync& sync)
 {
     const int tid = threadIdx.x;
     const int ncta = sync.size();
@@ -335,13 +315,12 @@ __device__ __forceinline__ void cg_body(const CgArgs& a, Smem& sm, unsigned char
     const int kb = c1 - c0;                // chunks owned
     const int e0 = c0 * CHUNK;             // owned element range [e0, e1)
     const int e1 = min(c1 * CHUNK, nf);
-    // One CTA owning every chunk keeps the reductions in shared memory and,
-    // with its state resident, publishes nothing for other CTAs.
+    // One CTA owning every chunk keeps the reductions in shared memory.
     const bool local = ncta == 1 && nchunks <= 32;
-    const bool publish = !(local && K > 0);
-    const Resident RS = resident(dyn, K > 0 ? K : 1);
     const float* dtab = sm.dtab;
     const float* itab = sm.itab;
+    (void)e0;
+    (void)e1;
 
     // ---- initialisation: x = 0, r = b, z = M^-1 r; bb = r.r, rz = r.z
     for (int base = 0; base < kb; base += 32) {
@@ -354,22 +333,11 @@ __device__ __forceinline__ void cg_body(const CgArgs& a, Smem& sm, unsigned char
                 const float r = a.b[e];
                 const uint8_t fl = a.flags[e];
                 const float z = fmul(itab[fl >> 2], r);
-                if (publish) __stcg(&a.z[e], z);
+                __stcg(&a.z[e], z);
                 v[0] = Ar<R>::prod(r, r);
                 v[1] = Ar<R>::prod(r, z);
-                if (K > 0) {
-                    const int l = s * CHUNK + tid;
-                    RS.x[l] = 0.0f;
-                    RS.r[l] = r;
-                    RS.zq[l] = z;
-                    RS.p[l] = 0.0f;
-                    RS.dn[l] = a.down[e];
-                    RS.up[l] = a.up[e];
-                    RS.fl[l] = fl;
-                } else {
-                    __stcg(&a.x[e], 0.0f);
-                    __stcg(&a.r[e], r);
-                }
+                __stcg(&a.x[e], 0.0f);
+                __stcg(&a.r[e], r);
             }
             level1<R, 2>(v, sl, sm);
         }
@@ -396,48 +364,24 @@ __device__ __forceinline__ void cg_body(const CgArgs& a, Smem& sm, unsigned char
     float beta = 0.0f;
     for (int it = 1; !done && it <= a.maxit; ++it) {
         // ---- phase A: p_new = z + beta p, q = A p_new, partial p.q
-        if (K > 0) {
-            for (int s = 0; s < kb; ++s) {
-                const int l = s * CHUNK + tid;
-                if ((c0 + s) * CHUNK + tid < nf) RS.p[l] = first ? RS.zq[l] : fadd(RS.zq[l], fmul(beta, RS.p[l]));
-            }
-            __syncthreads();
-        }
         for (int base = 0; base < kb; base += 32) {
             const int nslot = min(32, kb - base);
             for (int sl = 0; sl < nslot; ++sl) {
                 const int s = base + sl;
                 const int e = (c0 + s) * CHUNK + tid;
-                const int l = s * CHUNK + tid;
                 R v[1] = {R(0)};
                 if (e < nf) {
-                    float pe;
-                    unsigned fl;
-                    int dn, up;
-                    if (K > 0) {
-                        pe = RS.p[l];
-                        fl = RS.fl[l];
-                        dn = RS.dn[l];
-                        up = RS.up[l];
-                    } else {
-                        pe = remote_p(a, e, first, beta);
-                        fl = a.flags[e];
-                        dn = a.down[e];
-                        up = a.up[e];
-                    }
-                    auto pv = [&](int n) -> float {
-                        if (K > 0 && n >= e0 && n < e1) return RS.p[n - e0];
-                        return remote_p(a, n, first, beta);
-                    };
+                    const float pe = remote_p(a, e, first, beta);
+                    const unsigned fl = a.flags[e];
+                    const int dn = a.down[e], up = a.up[e];
                     float acc = 0.0f;
-                    if (dn >= 0) acc = fadd(acc, fmul(a.off, pv(dn)));
-                    if (fl & 1u) acc = fadd(acc, fmul(a.off, pv(e - 1)));
+                    if (dn >= 0) acc = fadd(acc, fmul(a.off, remote_p(a, dn, first, beta)));
+                    if (fl & 1u) acc = fadd(acc, fmul(a.off, remote_p(a, e - 1, first, beta)));
                     acc = fadd(acc, fmul(dtab[fl >> 2], pe));
-                    if (fl & 2u) acc = fadd(acc, fmul(a.off, pv(e + 1)));
-                    if (up >= 0) acc = fadd(acc, fmul(a.off, pv(up)));
+                    if (fl & 2u) acc = fadd(acc, fmul(a.off, remote_p(a, e + 1, first, beta)));
+                    if (up >= 0) acc = fadd(acc, fmul(a.off, remote_p(a, up, first, beta)));
                     v[0] = Ar<R>::prod(pe, acc);
-                    if (K > 0) RS.zq[l] = acc;  // z is no longer needed: it is folded into p
-                    else __stcg(&a.q[e], acc);
+                    __stcg(&a.q[e], acc);
                 }
                 level1<R, 1>(v, sl, sm);
             }
@@ -460,37 +404,18 @@ __device__ __forceinline__ void cg_body(const CgArgs& a, Smem& sm, unsigned char
                 const int e = (c0 + s) * CHUNK + tid;
                 R v[2] = {R(0), R(0)};
                 if (e < nf) {
-                    float pn, x, r, q;
-                    unsigned fl;
-                    const int l = s * CHUNK + tid;
-                    if (K > 0) {
-                        pn = RS.p[l];
-                        x = RS.x[l];
-                        r = RS.r[l];
-                        q = RS.zq[l];
-                        fl = RS.fl[l];
-                    } else {
-                        pn = remote_p(a, e, first, beta);
-                        x = __ldcg(&a.x[e]);
-                        r = __ldcg(&a.r[e]);
-                        q = __ldcg(&a.q[e]);
-                        fl = a.flags[e];
-                    }
+                    const float pn = remote_p(a, e, first, beta);
+                    float x = __ldcg(&a.x[e]);
+                    float r = __ldcg(&a.r[e]);
+                    const float q = __ldcg(&a.q[e]);
+                    const unsigned fl = a.flags[e];
                     x = fadd(x, fmul(alpha, pn));
                     r = fsub(r, fmul(alpha, q));
                     const float z = fmul(itab[fl >> 2], r);
-                    if (K > 0) {
-                        RS.x[l] = x;
-                        RS.r[l] = r;
-                        RS.zq[l] = z;
-                    } else {
-                        __stcg(&a.x[e], x);
-                        __stcg(&a.r[e], r);
-                    }
-                    if (publish) {
-                        __stcg(&a.z[e], z);
-                        __stcg(&a.p[e], pn);
-                    }
+                    __stcg(&a.x[e], x);
+                    __stcg(&a.r[e], r);
+                    __stcg(&a.z[e], z);
+                    __stcg(&a.p[e], pn);
                     v[0] = Ar<R>::prod(r, r);
                     v[1] = Ar<R>::prod(r, z);
                 }
@@ -511,13 +436,6 @@ __device__ __forceinline__ void cg_body(const CgArgs& a, Smem& sm, unsigned char
         rz = red2[1];
         first = false;
     }
-    // ---- the solution (x stayed 0 if no update ran)
-    if (K > 0) {
-        for (int s = 0; s < kb; ++s) {
-            const int e = (c0 + s) * CHUNK + tid;
-            if (e < nf) a.x[e] = RS.x[s * CHUNK + tid];
-        }
-    }
     if (cta == 0 && tid == 0) {
         a.result->iterations = iters;
         a.result->rr = (double)rr;
@@ -526,6 +444,240 @@ __device__ __forceinline__ void cg_body(const CgArgs& a, Smem& sm, unsigned char
     }
 }
 
+// Register-resident form of the solve, for CTAs that own at most K chunks.  The owned cells' r and z (q
+// between the SpMV and the update) live in registers, and p too for K <= 4
+// (slot s of thread t is element (c0 + s) * CHUNK + t); shared memory holds
+// what other threads read, and x:
+//   pv[K * CHUNK + hcap + 1]: p of the owned cells at [s * CHUNK + t], then
+//     the halo -- p_new of the remote cells the rows read, which lie in
+//     [lo, e0) and [e1, hi) of the fluid order, staged once per iteration from
+//     the published z and p_old -- then one +0 that absent neighbours index;
+//   nb[K * CHUNK]: the pv indices of each row's down, left, right and up
+//     neighbours, 16 bits each;
+//   xs[K * CHUNK]: x.
+// A row adds its five terms in the same order as cg_stream; an absent
+// neighbour contributes off * (+0) = +0, and adding +0 leaves the running sum
+// unchanged because the sum starts at +0 and so is never -0.  Returns false,
+// before any exchange with other CTAs, when the halo does not fit; the caller
+// then runs the streaming body, whose arithmetic and exchanges are the same.
+__device__ __forceinline__ int lean_halo_cap(int K, int dyn_bytes)
+{
+    const int cells = K * CHUNK;
+    const int cap = (dyn_bytes - 12 * cells - 8) / 4 - cells - 1;
+    return min(cap, 65535 - cells);
+}
+
+template <int K, typename R, class Sync>
+__device__ __forceinline__ bool cg_lean(const CgArgs& a, Smem& sm, unsigned char* dyn, int nf, int nchunks,
+                                        Sync& sync)
+{
+    const int tid = threadIdx.x;
+    const int ncta = sync.size();
+    const int cta = sync.rank();
+    const int c0 = (int)(((int64_t)cta * nchunks) / ncta);
+    const int c1 = (int)(((int64_t)(cta + 1) * nchunks) / ncta);
+    const int kb = c1 - c0;
+    const int e0 = c0 * CHUNK;
+    const int e1 = min(c1 * CHUNK, nf);
+    const bool local = ncta == 1 && nchunks <= 32;
+    const bool publish = !local;
+    constexpr int OWN = K * CHUNK;
+    const int hcap = lean_halo_cap(K, a.dyn_bytes);
+    float* pv = reinterpret_cast<float*>(dyn);
+    uint2* nb = reinterpret_cast<uint2*>(dyn + (((size_t)(OWN + hcap + 1) * 4 + 7) & ~(size_t)7));
+    float* xs = reinterpret_cast<float*>(nb + OWN);
+    constexpr bool PREG = K <= 4;  // p of the owned cells in registers (else read back from pv)
+    const float* dtab = sm.dtab;
+    const float* itab = sm.itab;
+    const float off = a.off;
+
+    // ---- halo extent: the lowest down/left and highest up/right neighbour outside [e0, e1)
+    if (tid == 0) {
+        sm.hlo = e0;
+        sm.hhi = e1;
+    }
+    __syncthreads();
+    {
+        int lo = e0, hi = e1;
+#pragma unroll
+        for (int s = 0; s < K; ++s) {
+            const int e = (c0 + s) * CHUNK + tid;
+            if (s < kb && e < nf) {
+                const int dn = a.down[e], up = a.up[e];
+                const unsigned fl = a.flags[e];
+                if (dn >= 0 && dn < e0) lo = min(lo, dn);
+                if ((fl & 1u) && e - 1 < e0) lo = min(lo, e - 1);
+                if (up >= e1) hi = max(hi, up + 1);
+                if ((fl & 2u) && e + 1 >= e1) hi = max(hi, e + 2);
+            }
+        }
+        if (lo < e0) atomicMin(&sm.hlo, lo);
+        if (hi > e1) atomicMax(&sm.hhi, hi);
+    }
+    __syncthreads();
+    const int lo = sm.hlo, hi = sm.hhi;
+    const int nbelow = e0 - lo;
+    const int nhalo = nbelow + (hi - e1);
+    if (nhalo > hcap) return false;  // uniform over the CTA
+    const unsigned zero_i = (unsigned)(OWN + hcap);
+    auto slot_of = [&](int n) -> unsigned {
+        if (n < 0) return zero_i;
+        if (n >= e0 && n < e1) return (unsigned)(n - e0);
+        if (n < e0) return (unsigned)(OWN + n - lo);
+        return (unsigned)(OWN + nbelow + n - e1);
+    };
+
+    // ---- initialisation: x = 0, r = b, z = M^-1 r; bb = r.r, rz = r.z
+    float r[K], zq[K], pn[PREG ? K : 1];
+    unsigned cnts = 0;  // non-solid neighbour count of slot s in bits 4s..4s+2
+    if (tid == 0) pv[zero_i] = 0.0f;
+#pragma unroll
+    for (int s = 0; s < K; ++s) {
+        r[s] = 0.0f;
+        zq[s] = 0.0f;
+        if constexpr (PREG) pn[s] = 0.0f;
+        if (s < kb) {
+            const int e = (c0 + s) * CHUNK + tid;
+            R v[2] = {R(0), R(0)};
+            if (e < nf) {
+                const float rb = a.b[e];
+                const unsigned fl = a.flags[e];
+                const float z = fmul(itab[fl >> 2], rb);
+                if (publish) __stcg(&a.z[e], z);
+                v[0] = Ar<R>::prod(rb, rb);
+                v[1] = Ar<R>::prod(rb, z);
+                r[s] = rb;
+                zq[s] = z;
+                xs[s * CHUNK + tid] = 0.0f;
+                if constexpr (!PREG) pv[s * CHUNK + tid] = 0.0f;
+                cnts |= (fl >> 2) << (4 * s);
+                const unsigned i_dn = slot_of(a.down[e]);
+                const unsigned i_l = (fl & 1u) ? slot_of(e - 1) : zero_i;
+                const unsigned i_r = (fl & 2u) ? slot_of(e + 1) : zero_i;
+                const unsigned i_up = slot_of(a.up[e]);
+                nb[s * CHUNK + tid] = make_uint2(i_dn | (i_l << 16), i_r | (i_up << 16));
+            }
+            level1<R, 2>(v, s, sm);
+        }
+    }
+    if (!local) level2<R, 2>(a, 0, c0, kb, sm);
+    R red2[2];
+    if (local) {
+        local_reduce<R, 2>(nchunks, sm, red2);
+    } else {
+        if (!sync.barrier(a, sm)) return true;
+        reduce_all<R, 2>(a, 0, nchunks, sm, red2);
+    }
+    const R bb = red2[0];
+    R rz = red2[1];
+    R rr = bb;
+    int iters = 0;
+    bool done = bb == R(0);
+    const R tolr = (R)a.tol;
+    R thr = Ar<R>::mul(Ar<R>::mul(tolr, tolr), bb);
+    if (thr < Ar<R>::tiny()) thr = Ar<R>::tiny();
+    if (!done && rr < thr) done = true;
+
+    bool first = true;
+    float beta = 0.0f;
+    for (int it = 1; !done && it <= a.maxit; ++it) {
+        // ---- phase A: p_new = z + beta p (own cells and halo), q = A p_new, partial p.q
+#pragma unroll
+        for (int s = 0; s < K; ++s) {
+            if (s < kb && (c0 + s) * CHUNK + tid < nf) {
+                float& ps = PREG ? pn[s] : pv[s * CHUNK + tid];
+                const float np = first ? zq[s] : fadd(zq[s], fmul(beta, ps));
+                if constexpr (PREG) pn[s] = np;
+                pv[s * CHUNK + tid] = np;
+            }
+        }
+        for (int h = tid; h < nhalo; h += CHUNK) {
+            const int n = h < nbelow ? lo + h : e1 + (h - nbelow);
+            const float zn = __ldcg(&a.z[n]);
+            pv[OWN + h] = first ? zn : fadd(zn, fmul(beta, __ldcg(&a.p[n])));
+        }
+        __syncthreads();
+#pragma unroll
+        for (int s = 0; s < K; ++s) {
+            if (s < kb) {
+                R v[1] = {R(0)};
+                if ((c0 + s) * CHUNK + tid < nf) {
+                    const uint2 w = nb[s * CHUNK + tid];
+                    const float ps = PREG ? pn[s] : pv[s * CHUNK + tid];
+                    float acc = 0.0f;
+                    acc = fadd(acc, fmul(off, pv[w.x & 0xffffu]));
+                    acc = fadd(acc, fmul(off, pv[w.x >> 16]));
+                    acc = fadd(acc, fmul(dtab[(cnts >> (4 * s)) & 7u], ps));
+                    acc = fadd(acc, fmul(off, pv[w.y & 0xffffu]));
+                    acc = fadd(acc, fmul(off, pv[w.y >> 16]));
+                    v[0] = Ar<R>::prod(ps, acc);
+                    zq[s] = acc;
+                }
+                level1<R, 1>(v, s, sm);
+            }
+        }
+        if (!local) level2<R, 1>(a, 1, c0, kb, sm);
+        R red1[1];
+        if (local) {
+            local_reduce<R, 1>(nchunks, sm, red1);
+        } else {
+            if (!sync.barrier(a, sm)) return true;
+            reduce_all<R, 1>(a, 1, nchunks, sm, red1);
+        }
+        const float alpha = Ar<R>::ratio(rz, red1[0]);
+
+        // ---- phase B: x += alpha p, r -= alpha q, z = M^-1 r; publish z, p; partial r.r, r.z
+#pragma unroll
+        for (int s = 0; s < K; ++s) {
+            if (s < kb) {
+                const int e = (c0 + s) * CHUNK + tid;
+                R v[2] = {R(0), R(0)};
+                if (e < nf) {
+                    const float ps = PREG ? pn[s] : pv[s * CHUNK + tid];
+                    const int l = s * CHUNK + tid;
+                    xs[l] = fadd(xs[l], fmul(alpha, ps));
+                    r[s] = fsub(r[s], fmul(alpha, zq[s]));
+                    const float z = fmul(itab[(cnts >> (4 * s)) & 7u], r[s]);
+                    zq[s] = z;
+                    if (publish) {
+                        __stcg(&a.z[e], z);
+                        __stcg(&a.p[e], ps);
+                    }
+                    v[0] = Ar<R>::prod(r[s], r[s]);
+                    v[1] = Ar<R>::prod(r[s], z);
+                }
+                level1<R, 2>(v, s, sm);
+            }
+        }
+        if (!local) level2<R, 2>(a, 0, c0, kb, sm);
+        if (local) {
+            local_reduce<R, 2>(nchunks, sm, red2);
+        } else {
+            if (!sync.barrier(a, sm)) return true;
+            reduce_all<R, 2>(a, 0, nchunks, sm, red2);
+        }
+        rr = red2[0];
+        iters = it;
+        if (rr < thr) break;
+        beta = Ar<R>::ratio(red2[1], rz);
+        rz = red2[1];
+        first = false;
+    }
+#pragma unroll
+    for (int s = 0; s < K; ++s) {
+        const int e = (c0 + s) * CHUNK + tid;
+        if (s < kb && e < nf) a.x[e] = xs[s * CHUNK + tid];
+    }
+    if (cta == 0 && tid == 0) {
+        a.result->iterations = iters;
+        a.result->rr = (double)rr;
+        a.result->bb = (double)bb;
+        a.result->status = 0;
+    }
+    return true;
+}
+
+template <typename R>
 __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(CgArgs a)
 {
     __shared__ Smem sm;
@@ -555,19 +707,15 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(CgArgs a)
     const int per_cta = grid ? (nchunks + gridDim.x - 1) / gridDim.x : nchunks;
     const bool resident = per_cta <= KREG;
     GridSync sync{grid, 0u};
-    if (a.fp64) {
-        if (resident) cg_body<KREG, double>(a, sm, dyn, nf, nchunks, sync);
-        else cg_body<0, double>(a, sm, dyn, nf, nchunks, sync);
-    } else {
-        if (resident) cg_body<KREG, float>(a, sm, dyn, nf, nchunks, sync);
-        else cg_body<0, float>(a, sm, dyn, nf, nchunks, sync);
-    }
+    const bool ran = resident && (per_cta <= 4 ? cg_lean<4, R>(a, sm, dyn, nf, nchunks, sync)
+                                               : cg_lean<KREG, R>(a, sm, dyn, nf, nchunks, sync));
+    if (!ran) cg_stream<R>(a, sm, nf, nchunks, sync);
 }
 
 // A batch of independent systems: one thread-block cluster per system (the
 // simulation order[cluster]); up to K chunks per CTA in shared memory.  The
 // reduction tree, and so every result, is that of k_cg.
-template <int K>
+template <int K, typename R>
 __global__ void __launch_bounds__(CG_THREADS, 1) k_cg_cluster(CgBatchArgs ba)
 {
     __shared__ Smem sm;
@@ -598,6 +746,7 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg_cluster(CgBatchArgs ba)
     a.result = ba.result + sim;
     a.missing = 0;
     a.wait_ns = WAIT_LIMIT_NS;
+    a.dyn_bytes = (int)cluster_dyn_bytes(K);
     if (threadIdx.x < 5) {
         sm.dtab[threadIdx.x] = sy.dtab[threadIdx.x];
         sm.itab[threadIdx.x] = sy.itab[threadIdx.x];
@@ -618,13 +767,7 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg_cluster(CgBatchArgs ba)
     // A system that outgrew the cluster's shared memory streams its state
     // from global memory instead (same arithmetic, same results).
     const bool resident = nchunks <= K * sync.size();
-    if (a.fp64) {
-        if (resident) cg_body<K, double>(a, sm, dyn, nf, nchunks, sync);
-        else cg_body<0, double>(a, sm, dyn, nf, nchunks, sync);
-    } else {
-        if (resident) cg_body<K, float>(a, sm, dyn, nf, nchunks, sync);
-        else cg_body<0, float>(a, sm, dyn, nf, nchunks, sync);
-    }
+    if (!(resident && cg_lean<K, R>(a, sm, dyn, nf, nchunks, sync))) cg_stream<R>(a, sm, nf, nchunks, sync);
 }
 
 }  // namespace
@@ -633,11 +776,16 @@ int cg_prepare(CgWork& w, int device)
 {
     int sms = 0, per_sm = 0;
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) return -1;
-    if (cudaFuncSetAttribute(k_cg, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)RESIDENT_BYTES) != cudaSuccess)
+    if (cudaFuncSetAttribute(k_cg<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)DYN_BYTES) !=
+            cudaSuccess ||
+        cudaFuncSetAttribute(k_cg<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)DYN_BYTES) !=
+            cudaSuccess)
         return -1;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cg, CG_THREADS, RESIDENT_BYTES) != cudaSuccess)
-        return -1;
-    if (per_sm < 1) return -1;
+    for (const void* f : {(const void*)k_cg<float>, (const void*)k_cg<double>}) {
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, f, CG_THREADS, DYN_BYTES) != cudaSuccess)
+            return -1;
+        if (per_sm < 1) return -1;
+    }
     w.grid = sms;  // one CTA per SM: fewer barrier arrivals
     return 0;
 }
@@ -672,9 +820,11 @@ void cg_solve(const Launch& L, CgWork& w, const int32_t* nfluid, const float* b,
     a.result = w.result;
     a.missing = w.missing_arrivals;
     a.wait_ns = w.wait_ns;
+    a.dyn_bytes = (int)DYN_BYTES;
     cudaMemsetAsync(w.barrier, 0, sizeof(unsigned), L.stream);
     void* args[] = {&a};
-    cudaLaunchCooperativeKernel((const void*)k_cg, dim3(w.grid), dim3(CG_THREADS), args, RESIDENT_BYTES, L.stream);
+    const void* kernel = fp64 ? (const void*)k_cg<double> : (const void*)k_cg<float>;
+    cudaLaunchCooperativeKernel(kernel, dim3(w.grid), dim3(CG_THREADS), args, DYN_BYTES, L.stream);
     L.count();
 }
 
@@ -683,8 +833,11 @@ namespace {
 template <int K>
 int prepare_cluster_kernel(int cluster)
 {
-    const size_t bytes = (size_t)K * CHUNK * 25;
-    if (cudaFuncSetAttribute(k_cg_cluster<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) != cudaSuccess)
+    const size_t bytes = cluster_dyn_bytes(K);
+    if (cudaFuncSetAttribute(k_cg_cluster<K, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) !=
+            cudaSuccess ||
+        cudaFuncSetAttribute(k_cg_cluster<K, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) !=
+            cudaSuccess)
         return -1;
     cudaLaunchConfig_t cfg = {};
     cudaLaunchAttribute attr[1];
@@ -697,9 +850,10 @@ int prepare_cluster_kernel(int cluster)
     cfg.dynamicSmemBytes = bytes;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    int n = 0;
-    if (cudaOccupancyMaxActiveClusters(&n, k_cg_cluster<K>, &cfg) != cudaSuccess) return -1;
-    return n;
+    int n = 0, n64 = 0;
+    if (cudaOccupancyMaxActiveClusters(&n, k_cg_cluster<K, float>, &cfg) != cudaSuccess) return -1;
+    if (cudaOccupancyMaxActiveClusters(&n64, k_cg_cluster<K, double>, &cfg) != cudaSuccess) return -1;
+    return n < n64 ? n : n64;
 }
 
 template <int K>
@@ -713,11 +867,12 @@ cudaError_t launch_cluster(const Launch& L, const CgBatchArgs& ba, int nsys, int
     attr[0].val.clusterDim.z = 1;
     cfg.gridDim = dim3((unsigned)(nsys * cluster));
     cfg.blockDim = dim3(CG_THREADS);
-    cfg.dynamicSmemBytes = (size_t)K * CHUNK * 25;
+    cfg.dynamicSmemBytes = cluster_dyn_bytes(K);
     cfg.stream = L.stream;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    const cudaError_t e = cudaLaunchKernelEx(&cfg, k_cg_cluster<K>, ba);
+    const cudaError_t e = ba.fp64 ? cudaLaunchKernelEx(&cfg, k_cg_cluster<K, double>, ba)
+                                  : cudaLaunchKernelEx(&cfg, k_cg_cluster<K, float>, ba);
     L.count();
     return e;
 }
