@@ -444,17 +444,18 @@ __device__ __forceinline__ void cg_stream(const CgArgs& a, Smem& sm, int nf, int
     }
 }
 
-// Register-resident form of the solve, for CTAs that own at most K chunks.  The owned cells' r and z (q
-// between the SpMV and the update) live in registers, and p too for K <= 4
-// (slot s of thread t is element (c0 + s) * CHUNK + t); shared memory holds
-// what other threads read, and x:
+// Register-resident form of the solve, for CTAs that own at most K chunks.
+// The owned cells' z (q between the SpMV and the update) live in registers,
+// and r and p too for K <= 4 (slot s of thread t is element
+// (c0 + s) * CHUNK + t); shared memory holds what other threads read, x, and
+// r for K > 4:
 //   pv[K * CHUNK + hcap + 1]: p of the owned cells at [s * CHUNK + t], then
 //     the halo -- p_new of the remote cells the rows read, which lie in
 //     [lo, e0) and [e1, hi) of the fluid order, staged once per iteration from
 //     the published z and p_old -- then one +0 that absent neighbours index;
 //   nb[K * CHUNK]: the pv indices of each row's down, left, right and up
 //     neighbours, 16 bits each;
-//   xs[K * CHUNK]: x.
+//   xs[K * CHUNK]: x;  rsm[K * CHUNK]: r (K > 4).
 // A row adds its five terms in the same order as cg_stream; an absent
 // neighbour contributes off * (+0) = +0, and adding +0 leaves the running sum
 // unchanged because the sum starts at +0 and so is never -0.  Returns false,
@@ -463,7 +464,7 @@ __device__ __forceinline__ void cg_stream(const CgArgs& a, Smem& sm, int nf, int
 __device__ __forceinline__ int lean_halo_cap(int K, int dyn_bytes)
 {
     const int cells = K * CHUNK;
-    const int cap = (dyn_bytes - 12 * cells - 8) / 4 - cells - 1;
+    const int cap = (dyn_bytes - (K <= 4 ? 12 : 16) * cells - 8) / 4 - cells - 1;
     return min(cap, 65535 - cells);
 }
 
@@ -486,6 +487,7 @@ __device__ __forceinline__ bool cg_lean(const CgArgs& a, Smem& sm, unsigned char
     float* pv = reinterpret_cast<float*>(dyn);
     uint2* nb = reinterpret_cast<uint2*>(dyn + (((size_t)(OWN + hcap + 1) * 4 + 7) & ~(size_t)7));
     float* xs = reinterpret_cast<float*>(nb + OWN);
+    float* rsm = xs + OWN;
     constexpr bool PREG = K <= 4;  // p of the owned cells in registers (else read back from pv)
     const float* dtab = sm.dtab;
     const float* itab = sm.itab;
@@ -528,12 +530,12 @@ __device__ __forceinline__ bool cg_lean(const CgArgs& a, Smem& sm, unsigned char
     };
 
     // ---- initialisation: x = 0, r = b, z = M^-1 r; bb = r.r, rz = r.z
-    float r[K], zq[K], pn[PREG ? K : 1];
+    float rreg[PREG ? K : 1], zq[K], pn[PREG ? K : 1];
     unsigned cnts = 0;  // non-solid neighbour count of slot s in bits 4s..4s+2
     if (tid == 0) pv[zero_i] = 0.0f;
 #pragma unroll
     for (int s = 0; s < K; ++s) {
-        r[s] = 0.0f;
+        if constexpr (PREG) rreg[s] = 0.0f;
         zq[s] = 0.0f;
         if constexpr (PREG) pn[s] = 0.0f;
         if (s < kb) {
@@ -546,7 +548,8 @@ __device__ __forceinline__ bool cg_lean(const CgArgs& a, Smem& sm, unsigned char
                 if (publish) __stcg(&a.z[e], z);
                 v[0] = Ar<R>::prod(rb, rb);
                 v[1] = Ar<R>::prod(rb, z);
-                r[s] = rb;
+                if constexpr (PREG) rreg[s] = rb;
+                else rsm[s * CHUNK + tid] = rb;
                 zq[s] = z;
                 xs[s * CHUNK + tid] = 0.0f;
                 if constexpr (!PREG) pv[s * CHUNK + tid] = 0.0f;
@@ -636,15 +639,17 @@ __device__ __forceinline__ bool cg_lean(const CgArgs& a, Smem& sm, unsigned char
                     const float ps = PREG ? pn[s] : pv[s * CHUNK + tid];
                     const int l = s * CHUNK + tid;
                     xs[l] = fadd(xs[l], fmul(alpha, ps));
-                    r[s] = fsub(r[s], fmul(alpha, zq[s]));
-                    const float z = fmul(itab[(cnts >> (4 * s)) & 7u], r[s]);
+                    float& rr_ = PREG ? rreg[s] : rsm[l];
+                    const float rn = fsub(rr_, fmul(alpha, zq[s]));
+                    rr_ = rn;
+                    const float z = fmul(itab[(cnts >> (4 * s)) & 7u], rn);
                     zq[s] = z;
                     if (publish) {
                         __stcg(&a.z[e], z);
                         __stcg(&a.p[e], ps);
                     }
-                    v[0] = Ar<R>::prod(r[s], r[s]);
-                    v[1] = Ar<R>::prod(r[s], z);
+                    v[0] = Ar<R>::prod(rn, rn);
+                    v[1] = Ar<R>::prod(rn, z);
                 }
                 level1<R, 2>(v, s, sm);
             }
