@@ -34,6 +34,8 @@
 // iteration; larger systems stream the state from global memory.  Waits are
 // bounded: a CTA that waits longer than about two seconds sets ST_TIMEOUT and
 // every CTA returns.
+#include <type_traits>
+
 #include "fs_internal.h"
 
 namespace fs {
@@ -563,12 +565,30 @@ __device__ __forceinline__ bool cg_lean(const CgArgs& a, Smem& sm, unsigned char
             level1<R, 2>(v, s, sm);
         }
     }
+    // Across the grid, the first HALO_PRE halo cells' z and p_old are loaded
+    // right after the barrier that publishes them, so that their round trip
+    // overlaps the partial-sum loads of reduce_all instead of following it.
+    // (A cluster barrier has no such round trip to hide behind.)
+    constexpr int HALO_PRE = std::is_same<Sync, GridSync>::value ? 2 : 0;
+    float hz[HALO_PRE > 0 ? HALO_PRE : 1], hp[HALO_PRE > 0 ? HALO_PRE : 1];
+    auto prefetch = [&](bool with_p) {
+#pragma unroll
+        for (int j = 0; j < HALO_PRE; ++j) {
+            const int h = tid + j * CHUNK;
+            if (h < nhalo) {
+                const int n = h < nbelow ? lo + h : e1 + (h - nbelow);
+                hz[j] = __ldcg(&a.z[n]);
+                if (with_p) hp[j] = __ldcg(&a.p[n]);
+            }
+        }
+    };
     if (!local) level2<R, 2>(a, 0, c0, kb, sm);
     R red2[2];
     if (local) {
         local_reduce<R, 2>(nchunks, sm, red2);
     } else {
         if (!sync.barrier(a, sm)) return true;
+        prefetch(false);
         reduce_all<R, 2>(a, 0, nchunks, sm, red2);
     }
     const R bb = red2[0];
@@ -594,7 +614,12 @@ __device__ __forceinline__ bool cg_lean(const CgArgs& a, Smem& sm, unsigned char
                 pv[s * CHUNK + tid] = np;
             }
         }
-        for (int h = tid; h < nhalo; h += CHUNK) {
+#pragma unroll
+        for (int j = 0; j < HALO_PRE; ++j) {
+            const int h = tid + j * CHUNK;
+            if (h < nhalo) pv[OWN + h] = first ? hz[j] : fadd(hz[j], fmul(beta, hp[j]));
+        }
+        for (int h = tid + HALO_PRE * CHUNK; h < nhalo; h += CHUNK) {
             const int n = h < nbelow ? lo + h : e1 + (h - nbelow);
             const float zn = __ldcg(&a.z[n]);
             pv[OWN + h] = first ? zn : fadd(zn, fmul(beta, __ldcg(&a.p[n])));
@@ -659,6 +684,7 @@ __device__ __forceinline__ bool cg_lean(const CgArgs& a, Smem& sm, unsigned char
             local_reduce<R, 2>(nchunks, sm, red2);
         } else {
             if (!sync.barrier(a, sm)) return true;
+            prefetch(true);
             reduce_all<R, 2>(a, 0, nchunks, sm, red2);
         }
         rr = red2[0];
