@@ -10,7 +10,9 @@ device time).  A "step" is one stepPICFLIP of the evolving simulation.
 
 --impl gpu (default) prints one JSON line with the device-time throughput
 (`value`), the end-to-end throughput through the C ABI with host particle
-buffers (`e2e`), the CG kernel's roofline, the CPU baseline of the same
+buffers (`e2e`: the same steps replayed from the timed region's start state,
+the particles uploaded from and downloaded to pinned host memory every step,
+wall-clock time), the CG kernel's roofline, the CPU baseline of the same
 workload and the SM clocks seen during the timed region.  --impl reference
 times the reference's CPU implementation of the path (the reference's own
 sources when built here, else the C restatement of them) on the same
@@ -412,6 +414,7 @@ def run_gpu(args, rank, world, local_rank):
     sim.set_timing(True)
     sim.step(fsg.STEP_PICFLIP, sc.dt)  # records the timed graph variant; not counted
     sim.synchronize()
+    start = sim.snapshot()  # the end-to-end run below replays the timed steps from here
     if world > 1:
         import torch.distributed as dist
 
@@ -440,15 +443,18 @@ def run_gpu(args, rank, world, local_rank):
     t_dev = max_over_ranks(sum(step_ms) / 1000.0, "cuda:%d" % local_rank)
     value = sc.cells * args.steps * world / t_dev
 
-    # end to end through the C ABI with host (pinned) particle buffers
+    # end to end through the C ABI with host (pinned) particle buffers: the same
+    # steps as the timed region (replayed from its start state), each with the
+    # particles uploaded before and downloaded after
     sim.set_timing(False)
     n = sim.num_particles()
     host_in = torch.empty((n, 4), dtype=torch.float32, pin_memory=True).numpy()
     host_out = torch.empty((n, 4), dtype=torch.float32, pin_memory=True).numpy()
-    host_in[:] = sim.particles()
-    e2e_steps = max(3, args.steps // 2)
-    sim.set_particles(host_in)
+    e2e_steps = args.steps
     sim.step(fsg.STEP_PICFLIP, sc.dt)  # graph for this configuration
+    sim.restore(start)
+    start.close()
+    host_in[:] = sim.particles()
     sim.synchronize()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
