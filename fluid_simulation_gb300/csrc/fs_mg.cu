@@ -12,11 +12,19 @@
 // spacing.  Smoothing is damped Jacobi (omega = 2/3; two sweeps before and
 // after), restriction averages the children's residuals, prolongation copies
 // the coarse correction to the children, and the coarsest level takes 64
-// Jacobi sweeps in one CTA, so the V-cycle is a fixed symmetric linear
-// operator.  The CG runs on -A (positive) with dot products accumulated in
-// double along a fixed order; its scalars stay on the device and every kernel
-// of an iteration returns at once after convergence, so chunks of iterations
-// are replayed from one CUDA graph and the host only polls a flag.
+// Jacobi sweeps, so the V-cycle is a fixed symmetric linear operator.  The CG
+// runs on -A (positive) with dot products accumulated in double along a fixed
+// order; its scalars stay on the device and every kernel of an iteration
+// returns at once after convergence, so iterations are replayed from a CUDA
+// graph and the host only polls a flag.
+//
+// Launches are few and fused: a cell's neighbour types are one precomputed
+// byte per level; on a level finer than 64 cells a side the two pre-smoothing
+// sweeps (the first is pointwise, from zero) are one kernel, the residual is
+// computed inside restriction, and prolongation inside the first
+// post-smoothing sweep; all levels of at most 64 cells a side run in one CTA
+// in shared memory; the CG's p update and SpMV are one kernel, and each
+// reduction finishes in the last block of its kernel.
 #include <algorithm>
 #include <cmath>
 #include <vector>
@@ -27,19 +35,24 @@ namespace fs {
 namespace {
 
 constexpr int TPB = 256;
-constexpr int COARSE = 16;
+constexpr int COARSE = 16;         // the coarsest level is at most this many cells a side
 constexpr int COARSE_SWEEPS = 64;
+constexpr int FUSE = 64;           // levels at most this many cells a side run in one CTA
+constexpr int FUSED_THREADS = 1024;
+constexpr int MAX_FUSED = 8;
 constexpr float OMEGA = 2.0f / 3.0f;
-constexpr int CHUNK = 8;  // CG iterations per graph replay
 
 unsigned nblk(int64_t n) { return (unsigned)((n + TPB - 1) / TPB); }
 
+// nbi byte of a cell: bits 0-3 its left, right, down, up neighbour is LIQUID;
+// bits 4-6 the number of non-SOLID neighbours; bit 7 the cell is LIQUID.
 struct Level
 {
     int nx, ny;
     float inv_h2;   // 1 / h^2 of this level
     uint8_t* type;  // LIQUID / AIR / SOLID
-    float *x, *b, *r;
+    uint8_t* nbi;
+    float *x, *b, *tmp;
 };
 
 // Scalars of the CG on the device.
@@ -48,31 +61,49 @@ struct Scal
     double pq, rr, rz, bb, thr;
     float alpha, beta;
     int it, done, maxit;
+    int cur;          // p_old is p[cur], p_new p[cur ^ 1]
+    unsigned ticket;  // blocks of the running kernel done with their partial
 };
 
-__device__ __forceinline__ uint8_t type_at(const Level& L, int i, int j)
+struct Fused
 {
-    if (i < 0 || j < 0 || i >= L.nx || j >= L.ny) return SOLID;
-    return L.type[i + (int64_t)j * L.nx];
+    Level lv[MAX_FUSED];
+    int n;
+};
+
+__device__ __forceinline__ bool liquid(uint8_t m) { return (m & 0x80u) != 0; }
+__device__ __forceinline__ int nsolid_free(uint8_t m) { return (m >> 4) & 7; }
+
+// (-A x)_c of a LIQUID cell from its neighbour byte: (n x_c - sum of the
+// LIQUID neighbours, in the order left, right, down, up) / h^2.
+template <class X>
+__device__ __forceinline__ float neg_apply(uint8_t m, int c, int nx, float inv_h2, X xv)
+{
+    float s = 0.0f;
+    if (m & 1u) s += xv(c - 1);
+    if (m & 2u) s += xv(c + 1);
+    if (m & 4u) s += xv(c - nx);
+    if (m & 8u) s += xv(c + nx);
+    return ((float)nsolid_free(m) * xv(c) - s) * inv_h2;
 }
 
-// (-A x)_c for a LIQUID cell: (n x_c - sum of liquid neighbours) / h^2.
-__device__ __forceinline__ float neg_apply(const Level& L, const float* __restrict__ x, int i, int j, float& diag)
+// One damped Jacobi sweep at cell c from the input values xv: 0 off LIQUID
+// cells (and where no neighbour is non-SOLID).
+template <class X>
+__device__ __forceinline__ float sweep_at(uint8_t m, int c, int nx, float inv_h2, float bc, X xv)
 {
-    const int64_t c = i + (int64_t)j * L.nx;
-    int n = 0;
-    float s = 0.0f;
-    const int di[4] = {-1, 1, 0, 0}, dj[4] = {0, 0, -1, 1};
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-        const uint8_t t = type_at(L, i + di[k], j + dj[k]);
-        if (t != SOLID) {
-            ++n;
-            if (t == LIQUID) s += x[c + di[k] + (int64_t)dj[k] * L.nx];
-        }
-    }
-    diag = (float)n * L.inv_h2;
-    return ((float)n * x[c] - s) * L.inv_h2;
+    if (!liquid(m)) return 0.0f;
+    const float d = (float)nsolid_free(m) * inv_h2;
+    if (!(d > 0.0f)) return 0.0f;
+    return xv(c) + OMEGA * (bc - neg_apply(m, c, nx, inv_h2, xv)) / d;
+}
+
+// The first sweep from a zero guess, which is pointwise.
+__device__ __forceinline__ float first_sweep(uint8_t m, float inv_h2, float bc)
+{
+    if (!liquid(m)) return 0.0f;
+    const float d = (float)nsolid_free(m) * inv_h2;
+    return d > 0.0f ? 0.0f + OMEGA * (bc - 0.0f) / d : 0.0f;
 }
 
 __global__ void k_types0(int64_t n, const uint8_t* __restrict__ labels, uint8_t* __restrict__ type)
@@ -98,132 +129,273 @@ __global__ void k_coarsen_types(Level F, Level C)
     C.type[c] = air ? AIR : liq ? LIQUID : SOLID;
 }
 
-// Damped Jacobi sweep: x_out = x_in + omega D^-1 (b - (-A) x_in) on LIQUID
-// cells (x_in == nullptr: a zero initial guess); others 0.
-__global__ void k_smooth(Level L, const float* __restrict__ xin, float* __restrict__ xout, const Scal* __restrict__ S)
+__device__ __forceinline__ uint8_t type_at(const Level& L, int i, int j)
 {
-    if (S->done) return;
+    if (i < 0 || j < 0 || i >= L.nx || j >= L.ny) return SOLID;
+    return L.type[i + (int64_t)j * L.nx];
+}
+
+__global__ void k_nbi(Level L)
+{
     const int64_t c = (int64_t)blockIdx.x * TPB + threadIdx.x;
     if (c >= (int64_t)L.nx * L.ny) return;
-    if (L.type[c] != LIQUID) {
-        xout[c] = 0.0f;
-        return;
-    }
     const int i = (int)(c % L.nx), j = (int)(c / L.nx);
-    float diag = 0.0f, ax = 0.0f;
-    if (xin) ax = neg_apply(L, xin, i, j, diag);
-    else {
-        int n = 0;
-        const int di[4] = {-1, 1, 0, 0}, dj[4] = {0, 0, -1, 1};
-        for (int k = 0; k < 4; ++k) n += type_at(L, i + di[k], j + dj[k]) != SOLID;
-        diag = (float)n * L.inv_h2;
+    const int di[4] = {-1, 1, 0, 0}, dj[4] = {0, 0, -1, 1};
+    unsigned m = 0, n = 0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const uint8_t t = type_at(L, i + di[k], j + dj[k]);
+        if (t != SOLID) ++n;
+        if (t == LIQUID) m |= 1u << k;
     }
-    const float x0 = xin ? xin[c] : 0.0f;
-    xout[c] = diag > 0.0f ? x0 + OMEGA * (L.b[c] - ax) / diag : 0.0f;
+    m |= n << 4;
+    if (L.type[c] == LIQUID) m |= 0x80u;
+    L.nbi[c] = (uint8_t)m;
 }
 
-// r = b - (-A) x
-__global__ void k_residual(Level L, const Scal* __restrict__ S)
+// ---- V-cycle kernels of the levels finer than FUSE cells a side ------------
+
+// The two pre-smoothing sweeps from zero: x = sweep(sweep_0(b)).
+__global__ void k_pre(Level L, const Scal* __restrict__ S)
 {
     if (S->done) return;
-    const int64_t c = (int64_t)blockIdx.x * TPB + threadIdx.x;
-    if (c >= (int64_t)L.nx * L.ny) return;
-    if (L.type[c] != LIQUID) {
-        L.r[c] = 0.0f;
-        return;
-    }
-    float diag;
-    L.r[c] = L.b[c] - neg_apply(L, L.x, (int)(c % L.nx), (int)(c / L.nx), diag);
+    const int64_t c64 = (int64_t)blockIdx.x * TPB + threadIdx.x;
+    if (c64 >= (int64_t)L.nx * L.ny) return;
+    const int c = (int)c64;
+    const uint8_t m = L.nbi[c];
+    auto x1 = [&](int k) { return first_sweep(L.nbi[k], L.inv_h2, L.b[k]); };
+    L.x[c] = sweep_at(m, c, L.nx, L.inv_h2, L.b[c], x1);
 }
 
-// Coarse right-hand side: the average of the LIQUID children's residuals.
+// Coarse right-hand side: the average of the LIQUID children's residuals
+// b - (-A) x, computed here.
 __global__ void k_restrict(Level F, Level C, const Scal* __restrict__ S)
 {
     if (S->done) return;
-    const int64_t c = (int64_t)blockIdx.x * TPB + threadIdx.x;
-    if (c >= (int64_t)C.nx * C.ny) return;
-    if (C.type[c] != LIQUID) {
+    const int64_t c64 = (int64_t)blockIdx.x * TPB + threadIdx.x;
+    if (c64 >= (int64_t)C.nx * C.ny) return;
+    const int c = (int)c64;
+    if (!liquid(C.nbi[c])) {
         C.b[c] = 0.0f;
         return;
     }
-    const int I = (int)(c % C.nx), J = (int)(c / C.nx);
+    const int I = c % C.nx, J = c / C.nx;
+    auto xv = [&](int k) { return F.x[k]; };
     float s = 0.0f;
     for (int dj = 0; dj < 2; ++dj)
         for (int di = 0; di < 2; ++di) {
             const int i = 2 * I + di, j = 2 * J + dj;
-            if (i < F.nx && j < F.ny && F.type[i + (int64_t)j * F.nx] == LIQUID) s += F.r[i + (int64_t)j * F.nx];
+            if (i >= F.nx || j >= F.ny) continue;
+            const int f = i + j * F.nx;
+            const uint8_t m = F.nbi[f];
+            if (liquid(m)) s += F.b[f] - neg_apply(m, f, F.nx, F.inv_h2, xv);
         }
     C.b[c] = 0.25f * s;
 }
 
-// x_fine += the coarse correction of the parent (LIQUID fine cells).
-__global__ void k_prolong(Level F, Level C, const Scal* __restrict__ S)
+// First post-smoothing sweep of x + (the parent's coarse correction) into tmp.
+__global__ void k_post1(Level F, Level C, const Scal* __restrict__ S)
 {
     if (S->done) return;
-    const int64_t c = (int64_t)blockIdx.x * TPB + threadIdx.x;
-    if (c >= (int64_t)F.nx * F.ny) return;
-    if (F.type[c] != LIQUID) return;
-    const int i = (int)(c % F.nx), j = (int)(c / F.nx);
-    F.x[c] += C.x[(i / 2) + (int64_t)(j / 2) * C.nx];
+    const int64_t c64 = (int64_t)blockIdx.x * TPB + threadIdx.x;
+    if (c64 >= (int64_t)F.nx * F.ny) return;
+    const int c = (int)c64;
+    auto xp = [&](int k) { return F.x[k] + C.x[(k % F.nx) / 2 + ((k / F.nx) / 2) * C.nx]; };
+    F.tmp[c] = sweep_at(F.nbi[c], c, F.nx, F.inv_h2, F.b[c], xp);
 }
 
-// The coarsest level: COARSE_SWEEPS damped Jacobi sweeps from 0, one CTA.
-__global__ void __launch_bounds__(1024) k_coarse(Level L, const Scal* __restrict__ S)
+// ---- reductions: a fixed tree per block, the last block sums the blocks ----
+
+// Adds v over the block (fixed tree), stores the block partial and returns
+// true in the last block of the grid to do so, with the fixed-order sum of all
+// partials in *total (every thread of that block).
+__device__ __forceinline__ bool block_reduce(double v, double* __restrict__ part, unsigned* ticket, double* total)
+{
+    __shared__ double sh[32];
+    __shared__ bool last;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+    for (int s = 16; s >= 1; s >>= 1) v += __shfl_down_sync(0xffffffffu, v, s);
+    if (lane == 0) sh[warp] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double b = 0.0;
+        for (int w = 0; w < nw; ++w) b += sh[w];
+        part[blockIdx.x] = b;
+        __threadfence();
+        last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!last) return false;
+    __threadfence();
+    double acc = 0.0;
+    for (int k = threadIdx.x; k < (int)gridDim.x; k += blockDim.x) acc += __ldcg(&part[k]);
+#pragma unroll
+    for (int s = 16; s >= 1; s >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, s);
+    __syncthreads();
+    if (lane == 0) sh[warp] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int w = 0; w < nw; ++w) t += sh[w];
+        sh[0] = t;
+        *ticket = 0;
+    }
+    __syncthreads();
+    *total = sh[0];
+    return true;
+}
+
+// Last post-smoothing sweep; at level 0 (z = M^-1 r) also r.z and beta.
+__global__ void k_post2(Level L, const float* __restrict__ r0, double* __restrict__ part, Scal* __restrict__ S)
 {
     if (S->done) return;
-    __shared__ float xs[2][COARSE * COARSE];
+    const int64_t c64 = (int64_t)blockIdx.x * TPB + threadIdx.x;
     const int n = L.nx * L.ny;
-    for (int c = threadIdx.x; c < n; c += blockDim.x) xs[0][c] = 0.0f;
+    const int c = (int)c64;
+    float z = 0.0f;
+    if (c64 < n) {
+        auto tv = [&](int k) { return L.tmp[k]; };
+        z = sweep_at(L.nbi[c], c, L.nx, L.inv_h2, L.b[c], tv);
+        L.x[c] = z;
+    }
+    if (!r0) return;  // uniform over the grid
+    double rz;
+    if (block_reduce(c64 < n ? (double)r0[c] * z : 0.0, part, &S->ticket, &rz) && threadIdx.x == 0) {
+        S->beta = S->it == 0 ? 0.0f : (float)(rz / S->rz);
+        S->rz = rz;
+    }
+}
+
+// ---- the levels of at most FUSE cells a side, in one CTA -------------------
+
+__global__ void __launch_bounds__(FUSED_THREADS, 1)
+    k_fused(Fused fu, const float* __restrict__ r0, Scal* __restrict__ S)
+{
+    if (S->done) return;
+    extern __shared__ __align__(16) unsigned char smem[];
+    float* X[MAX_FUSED];
+    float* T[MAX_FUSED];
+    float* B[MAX_FUSED];
+    uint8_t* M[MAX_FUSED];
+    {
+        float* f = reinterpret_cast<float*>(smem);
+        for (int k = 0; k < fu.n; ++k) {
+            const int n = fu.lv[k].nx * fu.lv[k].ny;
+            X[k] = f;
+            T[k] = f + n;
+            B[k] = f + 2 * n;
+            f += 3 * n;
+        }
+        uint8_t* u = reinterpret_cast<uint8_t*>(f);
+        for (int k = 0; k < fu.n; ++k) {
+            M[k] = u;
+            u += fu.lv[k].nx * fu.lv[k].ny;
+        }
+    }
+    const int tid = threadIdx.x;
+    for (int k = 0; k < fu.n; ++k) {
+        const int n = fu.lv[k].nx * fu.lv[k].ny;
+        for (int c = tid; c < n; c += FUSED_THREADS) M[k][c] = fu.lv[k].nbi[c];
+    }
+    {
+        const int n = fu.lv[0].nx * fu.lv[0].ny;
+        for (int c = tid; c < n; c += FUSED_THREADS) B[0][c] = fu.lv[0].b[c];
+    }
     __syncthreads();
-    for (int s = 0; s < COARSE_SWEEPS; ++s) {
-        const float* xin = xs[s & 1];
-        float* xout = xs[(s + 1) & 1];
-        for (int c = threadIdx.x; c < n; c += blockDim.x) {
-            if (L.type[c] != LIQUID) {
-                xout[c] = 0.0f;
-                continue;
+    // down: pre-smoothing and restriction
+    for (int k = 0; k + 1 < fu.n; ++k) {
+        const Level& L = fu.lv[k];
+        const int n = L.nx * L.ny;
+        for (int c = tid; c < n; c += FUSED_THREADS) T[k][c] = first_sweep(M[k][c], L.inv_h2, B[k][c]);
+        __syncthreads();
+        {
+            const float* t = T[k];
+            auto tv = [&](int q) { return t[q]; };
+            for (int c = tid; c < n; c += FUSED_THREADS) X[k][c] = sweep_at(M[k][c], c, L.nx, L.inv_h2, B[k][c], tv);
+        }
+        __syncthreads();
+        const Level& C = fu.lv[k + 1];
+        const int nc = C.nx * C.ny;
+        const float* x = X[k];
+        auto xv = [&](int q) { return x[q]; };
+        for (int c = tid; c < nc; c += FUSED_THREADS) {
+            float s = 0.0f;
+            if (liquid(M[k + 1][c])) {
+                const int I = c % C.nx, J = c / C.nx;
+                for (int dj = 0; dj < 2; ++dj)
+                    for (int di = 0; di < 2; ++di) {
+                        const int i = 2 * I + di, j = 2 * J + dj;
+                        if (i >= L.nx || j >= L.ny) continue;
+                        const int f = i + j * L.nx;
+                        const uint8_t m = M[k][f];
+                        if (liquid(m)) s += B[k][f] - neg_apply(m, f, L.nx, L.inv_h2, xv);
+                    }
+                s = 0.25f * s;
             }
-            float diag;
-            const float ax = neg_apply(L, xin, c % L.nx, c / L.nx, diag);
-            xout[c] = diag > 0.0f ? xin[c] + OMEGA * (L.b[c] - ax) / diag : 0.0f;
+            B[k + 1][c] = s;
         }
         __syncthreads();
     }
-    for (int c = threadIdx.x; c < n; c += blockDim.x) L.x[c] = xs[COARSE_SWEEPS & 1][c];
+    // the coarsest level: COARSE_SWEEPS sweeps from 0
+    {
+        const int k = fu.n - 1;
+        const Level& L = fu.lv[k];
+        const int n = L.nx * L.ny;
+        for (int c = tid; c < n; c += FUSED_THREADS) X[k][c] = 0.0f;
+        __syncthreads();
+        for (int s = 0; s < COARSE_SWEEPS; ++s) {
+            const float* xin = (s & 1) ? T[k] : X[k];
+            float* xout = (s & 1) ? X[k] : T[k];
+            auto xv = [&](int q) { return xin[q]; };
+            for (int c = tid; c < n; c += FUSED_THREADS) xout[c] = sweep_at(M[k][c], c, L.nx, L.inv_h2, B[k][c], xv);
+            __syncthreads();
+        }
+        static_assert((COARSE_SWEEPS & 1) == 0, "the coarse result ends in X");
+    }
+    // up: prolongation and post-smoothing
+    for (int k = fu.n - 2; k >= 0; --k) {
+        const Level& L = fu.lv[k];
+        const Level& C = fu.lv[k + 1];
+        const int n = L.nx * L.ny;
+        {
+            const float* x = X[k];
+            const float* xc = X[k + 1];
+            auto xp = [&](int q) { return x[q] + xc[(q % L.nx) / 2 + ((q / L.nx) / 2) * C.nx]; };
+            for (int c = tid; c < n; c += FUSED_THREADS) T[k][c] = sweep_at(M[k][c], c, L.nx, L.inv_h2, B[k][c], xp);
+        }
+        __syncthreads();
+        {
+            const float* t = T[k];
+            auto tv = [&](int q) { return t[q]; };
+            for (int c = tid; c < n; c += FUSED_THREADS) X[k][c] = sweep_at(M[k][c], c, L.nx, L.inv_h2, B[k][c], tv);
+        }
+        __syncthreads();
+    }
+    const int n0 = fu.lv[0].nx * fu.lv[0].ny;
+    for (int c = tid; c < n0; c += FUSED_THREADS) fu.lv[0].x[c] = X[0][c];
+    if (!r0) return;
+    // the whole V-cycle ran here: r.z and beta over level 0, fixed order
+    __shared__ double sh[32];
+    double v = 0.0;
+    for (int c = tid; c < n0; c += FUSED_THREADS) v += (double)r0[c] * X[0][c];
+#pragma unroll
+    for (int s = 16; s >= 1; s >>= 1) v += __shfl_down_sync(0xffffffffu, v, s);
+    if ((tid & 31) == 0) sh[tid >> 5] = v;
+    __syncthreads();
+    if (tid == 0) {
+        double rz = 0.0;
+        for (int w = 0; w < FUSED_THREADS / 32; ++w) rz += sh[w];
+        S->beta = S->it == 0 ? 0.0f : (float)(rz / S->rz);
+        S->rz = rz;
+    }
 }
 
 // ---- CG kernels (level-0 cell vectors; every one returns once done) -------
 
-// Block partial of sum a*b (double) over LIQUID cells: fixed tree per block.
-__device__ __forceinline__ void block_partial(double v, double* __restrict__ part)
-{
-    __shared__ double sh[TPB];
-    sh[threadIdx.x] = v;
-    __syncthreads();
-    for (int w = TPB / 2; w > 0; w >>= 1) {
-        if ((int)threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) part[blockIdx.x] = sh[0];
-}
-
-__device__ __forceinline__ double fixed_sum(const double* __restrict__ part, int nb)
-{
-    __shared__ double sh[TPB];
-    double acc = 0.0;
-    for (int k = threadIdx.x; k < nb; k += TPB) acc += part[k];
-    sh[threadIdx.x] = acc;
-    __syncthreads();
-    for (int w = TPB / 2; w > 0; w >>= 1) {
-        if ((int)threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
-        __syncthreads();
-    }
-    return sh[0];
-}
-
 // Start: x = 0, r = -b (the system -A x = -b), bb, threshold.
 __global__ void k_cg_init(Level L, const float* __restrict__ b, float* __restrict__ x, float* __restrict__ r,
-                          double* __restrict__ part)
+                          double* __restrict__ part, Scal* __restrict__ S, double tol, int maxit)
 {
     const int64_t c = (int64_t)blockIdx.x * TPB + threadIdx.x;
     double v = 0.0;
@@ -233,102 +405,69 @@ __global__ void k_cg_init(Level L, const float* __restrict__ b, float* __restric
         r[c] = rv;
         v = (double)rv * rv;
     }
-    block_partial(v, part);
-}
-
-__global__ void k_cg_init_final(const double* __restrict__ part, int nb, Scal* __restrict__ S, double tol, int maxit)
-{
-    const double bb = fixed_sum(part, nb);
-    if (threadIdx.x == 0) {
+    double bb;
+    if (block_reduce(v, part, &S->ticket, &bb) && threadIdx.x == 0) {
         S->bb = bb;
         S->rr = bb;
         S->thr = tol * tol * bb;
         S->it = 0;
         S->maxit = maxit;
         S->beta = 0.0f;
+        S->cur = 0;
         S->done = (bb == 0.0 || bb < S->thr || maxit == 0) ? 1 : 0;
     }
 }
 
-// rz partial (z = M^-1 r just computed).
-__global__ void k_dot_rz(int64_t n, const float* __restrict__ r, const float* __restrict__ z, double* __restrict__ part,
-                         const Scal* __restrict__ S)
+// p_new = z + beta p_old (first iteration: z), q = (-A) p_new, p.q and alpha.
+__global__ void k_p_spmv(Level L, const float* __restrict__ z, float* __restrict__ p0, float* __restrict__ p1,
+                         float* __restrict__ q, double* __restrict__ part, Scal* __restrict__ S)
 {
     if (S->done) return;
-    const int64_t c = (int64_t)blockIdx.x * TPB + threadIdx.x;
-    block_partial(c < n ? (double)r[c] * z[c] : 0.0, part);
-}
-
-__global__ void k_rz_final(const double* __restrict__ part, int nb, Scal* __restrict__ S)
-{
-    if (S->done) return;
-    const double rz = fixed_sum(part, nb);
-    if (threadIdx.x == 0) {
-        S->beta = S->it == 0 ? 0.0f : (float)(rz / S->rz);
-        S->rz = rz;
-    }
-}
-
-// p = z + beta p, then q = (-A) p and the p.q partial (two kernels: q needs
-// the neighbours' p).
-__global__ void k_update_p(int64_t n, const float* __restrict__ z, float* __restrict__ p, const Scal* __restrict__ S)
-{
-    if (S->done) return;
-    const int64_t c = (int64_t)blockIdx.x * TPB + threadIdx.x;
-    if (c < n) p[c] = S->it == 0 ? z[c] : z[c] + S->beta * p[c];
-}
-
-__global__ void k_spmv_pq(Level L, const float* __restrict__ p, float* __restrict__ q, double* __restrict__ part,
-                          const Scal* __restrict__ S)
-{
-    if (S->done) return;
-    const int64_t c = (int64_t)blockIdx.x * TPB + threadIdx.x;
+    const int64_t c64 = (int64_t)blockIdx.x * TPB + threadIdx.x;
+    const int n = L.nx * L.ny;
+    const int c = (int)c64;
+    const bool first = S->it == 0;
+    const float beta = S->beta;
+    const float* pold = S->cur ? p1 : p0;
+    float* pnew = S->cur ? p0 : p1;
+    auto pn = [&](int k) { return first ? z[k] : z[k] + beta * pold[k]; };
     double v = 0.0;
-    if (c < (int64_t)L.nx * L.ny) {
-        float qc = 0.0f;
-        if (L.type[c] == LIQUID) {
-            float diag;
-            qc = neg_apply(L, p, (int)(c % L.nx), (int)(c / L.nx), diag);
-        }
+    if (c64 < n) {
+        const uint8_t m = L.nbi[c];
+        const float pc = pn(c);
+        const float qc = liquid(m) ? neg_apply(m, c, L.nx, L.inv_h2, pn) : 0.0f;
+        pnew[c] = pc;
         q[c] = qc;
-        v = (double)p[c] * qc;
+        v = (double)pc * qc;
     }
-    block_partial(v, part);
-}
-
-__global__ void k_pq_final(const double* __restrict__ part, int nb, Scal* __restrict__ S)
-{
-    if (S->done) return;
-    const double pq = fixed_sum(part, nb);
-    if (threadIdx.x == 0) {
+    double pq;
+    if (block_reduce(v, part, &S->ticket, &pq) && threadIdx.x == 0) {
         S->pq = pq;
         S->alpha = pq != 0.0 ? (float)(S->rz / pq) : 0.0f;
     }
 }
 
-__global__ void k_update_xr(int64_t n, const float* __restrict__ p, const float* __restrict__ q, float* __restrict__ x,
-                            float* __restrict__ r, double* __restrict__ part, const Scal* __restrict__ S)
+// x += alpha p_new, r -= alpha q, r.r, convergence; p_new becomes p_old.
+__global__ void k_update_xr(int64_t n, const float* __restrict__ p0, const float* __restrict__ p1,
+                            const float* __restrict__ q, float* __restrict__ x, float* __restrict__ r,
+                            double* __restrict__ part, Scal* __restrict__ S)
 {
     if (S->done) return;
     const int64_t c = (int64_t)blockIdx.x * TPB + threadIdx.x;
+    const float* pnew = S->cur ? p0 : p1;
     double v = 0.0;
     if (c < n) {
         const float a = S->alpha;
-        x[c] += a * p[c];
+        x[c] += a * pnew[c];
         const float rv = r[c] - a * q[c];
         r[c] = rv;
         v = (double)rv * rv;
     }
-    block_partial(v, part);
-}
-
-__global__ void k_rr_final(const double* __restrict__ part, int nb, Scal* __restrict__ S)
-{
-    if (S->done) return;
-    const double rr = fixed_sum(part, nb);
-    if (threadIdx.x == 0) {
+    double rr;
+    if (block_reduce(v, part, &S->ticket, &rr) && threadIdx.x == 0) {
         S->rr = rr;
         S->it += 1;
+        S->cur ^= 1;
         if (rr < S->thr || S->it >= S->maxit) S->done = 1;
     }
 }
@@ -380,13 +519,16 @@ struct MgSolver
     int device = 0;
     int64_t n = 0;
     std::vector<Level> lv;
-    float *x = nullptr, *r = nullptr, *z = nullptr, *p = nullptr, *q = nullptr, *tmp = nullptr;
+    int fuse0 = 0;            // first level of the fused kernel
+    size_t fused_bytes = 0;   // its dynamic shared memory
+    float *x = nullptr, *r = nullptr, *z = nullptr, *p0 = nullptr, *p1 = nullptr, *q = nullptr;
     double* part = nullptr;
     Scal* S = nullptr;
     std::vector<void*> allocs;
-    cudaGraphExec_t chunk = nullptr;
-    const float* chunk_b = nullptr;
-    cudaStream_t chunk_stream = nullptr;
+    cudaGraphExec_t iteration = nullptr;  // one CG iteration, recorded once per stream
+    cudaStream_t iteration_stream = nullptr;
+    int64_t per_iteration = 0;            // kernels of one CG iteration
+    int expect = 8;                       // iterations to launch before the first poll
 };
 
 namespace {
@@ -398,47 +540,42 @@ cudaError_t alloc(MgSolver* m, void** p, size_t bytes)
     return e;
 }
 
-// One V-cycle from level l: lv[l].b given, lv[l].x out.
+Fused fused_levels(const MgSolver* m)
+{
+    Fused f{};
+    f.n = (int)m->lv.size() - m->fuse0;
+    for (int k = 0; k < f.n; ++k) f.lv[k] = m->lv[m->fuse0 + k];
+    return f;
+}
+
+// z = V-cycle(r), with r.z and beta (level 0's right-hand side is r, its solution z).
 void vcycle(MgSolver* m, cudaStream_t st, int64_t* launches)
 {
-    const int nl = (int)m->lv.size();
-    for (int l = 0; l < nl - 1; ++l) {
+    const int F = m->fuse0;
+    for (int l = 0; l < F; ++l) {
         Level& L = m->lv[l];
-        const unsigned nb = nblk((int64_t)L.nx * L.ny);
-        k_smooth<<<nb, TPB, 0, st>>>(L, nullptr, m->tmp, m->S);
-        k_smooth<<<nb, TPB, 0, st>>>(L, m->tmp, L.x, m->S);
-        k_residual<<<nb, TPB, 0, st>>>(L, m->S);
+        k_pre<<<nblk((int64_t)L.nx * L.ny), TPB, 0, st>>>(L, m->S);
         k_restrict<<<nblk((int64_t)m->lv[l + 1].nx * m->lv[l + 1].ny), TPB, 0, st>>>(L, m->lv[l + 1], m->S);
-        *launches += 4;
+        *launches += 2;
     }
-    k_coarse<<<1, 1024, 0, st>>>(m->lv[nl - 1], m->S);
+    k_fused<<<1, FUSED_THREADS, m->fused_bytes, st>>>(fused_levels(m), F == 0 ? m->r : nullptr, m->S);
     *launches += 1;
-    for (int l = nl - 2; l >= 0; --l) {
+    for (int l = F - 1; l >= 0; --l) {
         Level& L = m->lv[l];
         const unsigned nb = nblk((int64_t)L.nx * L.ny);
-        k_prolong<<<nb, TPB, 0, st>>>(L, m->lv[l + 1], m->S);
-        k_smooth<<<nb, TPB, 0, st>>>(L, L.x, m->tmp, m->S);
-        k_smooth<<<nb, TPB, 0, st>>>(L, m->tmp, L.x, m->S);
-        *launches += 3;
+        k_post1<<<nb, TPB, 0, st>>>(L, m->lv[l + 1], m->S);
+        k_post2<<<nb, TPB, 0, st>>>(L, l == 0 ? m->r : nullptr, m->part, m->S);
+        *launches += 2;
     }
 }
 
-// One CG iteration (z = M^-1 r first): every kernel returns once S->done.
 void cg_iteration(MgSolver* m, cudaStream_t st, int64_t* launches)
 {
-    Level& L0 = m->lv[0];
-    const int64_t n = m->n;
-    const unsigned nb = nblk(n);
-    // z = V-cycle(r): level 0's right-hand side is r, its solution z
+    const unsigned nb = nblk(m->n);
     vcycle(m, st, launches);
-    k_dot_rz<<<nb, TPB, 0, st>>>(n, m->r, m->z, m->part, m->S);
-    k_rz_final<<<1, TPB, 0, st>>>(m->part, (int)nb, m->S);
-    k_update_p<<<nb, TPB, 0, st>>>(n, m->z, m->p, m->S);
-    k_spmv_pq<<<nb, TPB, 0, st>>>(L0, m->p, m->q, m->part, m->S);
-    k_pq_final<<<1, TPB, 0, st>>>(m->part, (int)nb, m->S);
-    k_update_xr<<<nb, TPB, 0, st>>>(n, m->p, m->q, m->x, m->r, m->part, m->S);
-    k_rr_final<<<1, TPB, 0, st>>>(m->part, (int)nb, m->S);
-    *launches += 7;
+    k_p_spmv<<<nb, TPB, 0, st>>>(m->lv[0], m->z, m->p0, m->p1, m->q, m->part, m->S);
+    k_update_xr<<<nb, TPB, 0, st>>>(m->n, m->p0, m->p1, m->q, m->x, m->r, m->part, m->S);
+    *launches += 2;
 }
 
 }  // namespace
@@ -460,20 +597,30 @@ int mg_create(MgSolver** out, int nx, int ny, float dx, int device)
         L.inv_h2 = (float)(1.0 / (h * h));
         const size_t N = (size_t)lx * ly;
         if (e == cudaSuccess) e = alloc(m, (void**)&L.type, N);
+        if (e == cudaSuccess) e = alloc(m, (void**)&L.nbi, N);
         if (e == cudaSuccess) e = alloc(m, (void**)&L.x, 4 * N);
         if (e == cudaSuccess) e = alloc(m, (void**)&L.b, 4 * N);
-        if (e == cudaSuccess) e = alloc(m, (void**)&L.r, 4 * N);
+        if (e == cudaSuccess) e = alloc(m, (void**)&L.tmp, 4 * N);
         m->lv.push_back(L);
         if (std::max(lx, ly) <= COARSE) break;
         lx = (lx + 1) / 2;
         ly = (ly + 1) / 2;
         h *= 2.0;
     }
+    // the fused kernel takes every level of at most FUSE cells a side
+    m->fuse0 = (int)m->lv.size() - 1;
+    while (m->fuse0 > 0 && std::max(m->lv[m->fuse0 - 1].nx, m->lv[m->fuse0 - 1].ny) <= FUSE &&
+           (int)m->lv.size() - (m->fuse0 - 1) <= MAX_FUSED)
+        --m->fuse0;
+    for (size_t k = m->fuse0; k < m->lv.size(); ++k) m->fused_bytes += (size_t)13 * m->lv[k].nx * m->lv[k].ny;
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_fused, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)m->fused_bytes);
     const size_t N = (size_t)m->n;
-    for (float** v : {&m->x, &m->p, &m->q, &m->tmp})
+    for (float** v : {&m->x, &m->p0, &m->p1, &m->q})
         if (e == cudaSuccess) e = alloc(m, (void**)v, 4 * N);
     if (e == cudaSuccess) e = alloc(m, (void**)&m->part, 8 * (size_t)nblk(m->n));
     if (e == cudaSuccess) e = alloc(m, (void**)&m->S, sizeof(Scal));
+    if (e == cudaSuccess) e = cudaMemset(m->S, 0, sizeof(Scal));
     // level 0 of the V-cycle: right-hand side = the CG residual, solution = z
     m->r = m->lv[0].b;
     m->z = m->lv[0].x;
@@ -489,7 +636,7 @@ void mg_destroy(MgSolver* m)
 {
     if (!m) return;
     cudaSetDevice(m->device);
-    if (m->chunk) cudaGraphExecDestroy(m->chunk);
+    if (m->iteration) cudaGraphExecDestroy(m->iteration);
     for (void* p : m->allocs) cudaFree(p);
     delete m;
 }
@@ -499,43 +646,50 @@ void mg_set_labels(MgSolver* m, cudaStream_t st, const uint8_t* labels, int64_t*
     k_types0<<<nblk(m->n), TPB, 0, st>>>(m->n, labels, m->lv[0].type);
     for (size_t l = 1; l < m->lv.size(); ++l)
         k_coarsen_types<<<nblk((int64_t)m->lv[l].nx * m->lv[l].ny), TPB, 0, st>>>(m->lv[l - 1], m->lv[l]);
-    *launches += (int64_t)m->lv.size();
+    for (size_t l = 0; l < m->lv.size(); ++l)
+        k_nbi<<<nblk((int64_t)m->lv[l].nx * m->lv[l].ny), TPB, 0, st>>>(m->lv[l]);
+    *launches += 2 * (int64_t)m->lv.size();
 }
 
 cudaError_t mg_solve(MgSolver* m, cudaStream_t st, const float* b, double tol, int maxit, int64_t* launches,
                      int* iterations, double* rr, double* bb, float** x_out)
 {
-    const unsigned nb = nblk(m->n);
-    k_cg_init<<<nb, TPB, 0, st>>>(m->lv[0], b, m->x, m->r, m->part);
-    k_cg_init_final<<<1, TPB, 0, st>>>(m->part, (int)nb, m->S, tol, maxit);
-    *launches += 2;
-    // chunks of CHUNK iterations, recorded once per stream
-    if (!m->chunk || m->chunk_stream != st) {
-        if (m->chunk) cudaGraphExecDestroy(m->chunk);
-        m->chunk = nullptr;
+    k_cg_init<<<nblk(m->n), TPB, 0, st>>>(m->lv[0], b, m->x, m->r, m->part, m->S, tol, maxit);
+    *launches += 1;
+    if (!m->iteration || m->iteration_stream != st) {
+        if (m->iteration) cudaGraphExecDestroy(m->iteration);
+        m->iteration = nullptr;
         cudaGraph_t g = nullptr;
         cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
         if (e != cudaSuccess) return e;
-        int64_t dummy = 0;
-        for (int k = 0; k < CHUNK; ++k) cg_iteration(m, st, &dummy);
+        m->per_iteration = 0;
+        cg_iteration(m, st, &m->per_iteration);
         e = cudaStreamEndCapture(st, &g);
         if (e != cudaSuccess) return e;
-        e = cudaGraphInstantiate(&m->chunk, g, 0);
+        e = cudaGraphInstantiate(&m->iteration, g, 0);
         cudaGraphDestroy(g);
         if (e != cudaSuccess) return e;
-        m->chunk_stream = st;
+        m->iteration_stream = st;
     }
-    const int64_t per_iter = 7 * ((int64_t)m->lv.size() - 1) + 8;  // kernels of one cg_iteration
+    // Launch as many iterations as the last solve needed, then poll; after
+    // convergence the remaining kernels return at once.
     Scal s{};
+    int launched = 0;
+    int batch = std::max(1, std::min(m->expect, maxit));
     for (;;) {
-        cudaError_t e = cudaGraphLaunch(m->chunk, st);
-        if (e != cudaSuccess) return e;
-        *launches += per_iter * CHUNK;
-        e = cudaMemcpyAsync(&s, m->S, sizeof(Scal), cudaMemcpyDeviceToHost, st);
+        for (int k = 0; k < batch; ++k) {
+            const cudaError_t e = cudaGraphLaunch(m->iteration, st);
+            if (e != cudaSuccess) return e;
+        }
+        launched += batch;
+        *launches += m->per_iteration * batch;
+        cudaError_t e = cudaMemcpyAsync(&s, m->S, sizeof(Scal), cudaMemcpyDeviceToHost, st);
         if (e == cudaSuccess) e = cudaStreamSynchronize(st);
         if (e != cudaSuccess) return e;
-        if (s.done) break;
+        if (s.done || launched >= maxit) break;
+        batch = 2;
     }
+    m->expect = std::max(1, s.it);
     *iterations = s.it;
     *rr = s.rr;
     *bb = s.bb;
