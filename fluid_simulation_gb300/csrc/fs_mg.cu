@@ -35,6 +35,7 @@ namespace fs {
 namespace {
 
 constexpr int TPB = 256;
+constexpr int RTPB = 512;  // threads of the reducing kernels (grid-stride, two blocks per SM)
 constexpr int COARSE = 16;         // the coarsest level is at most this many cells a side
 constexpr int COARSE_SWEEPS = 64;
 constexpr int FUSE = 64;           // levels at most this many cells a side run in one CTA
@@ -74,28 +75,43 @@ struct Fused
 __device__ __forceinline__ bool liquid(uint8_t m) { return (m & 0x80u) != 0; }
 __device__ __forceinline__ int nsolid_free(uint8_t m) { return (m >> 4) & 7; }
 
+// Stencil accessors take the direction of the value they return: the cell
+// itself, or its left, right, down or up neighbour.
+enum Dir { CTR = 0, LEFT, RIGHT, DOWN, UP };
+
+// Values of an array around cell c of a level nx cells wide.
+struct Around
+{
+    const float* a;
+    int c, nx;
+    __device__ __forceinline__ float operator()(int d) const
+    {
+        return a[d == CTR ? c : d == LEFT ? c - 1 : d == RIGHT ? c + 1 : d == DOWN ? c - nx : c + nx];
+    }
+};
+
 // (-A x)_c of a LIQUID cell from its neighbour byte: (n x_c - sum of the
 // LIQUID neighbours, in the order left, right, down, up) / h^2.
 template <class X>
-__device__ __forceinline__ float neg_apply(uint8_t m, int c, int nx, float inv_h2, X xv)
+__device__ __forceinline__ float neg_apply(uint8_t m, float inv_h2, X xv)
 {
     float s = 0.0f;
-    if (m & 1u) s += xv(c - 1);
-    if (m & 2u) s += xv(c + 1);
-    if (m & 4u) s += xv(c - nx);
-    if (m & 8u) s += xv(c + nx);
-    return ((float)nsolid_free(m) * xv(c) - s) * inv_h2;
+    if (m & 1u) s += xv(LEFT);
+    if (m & 2u) s += xv(RIGHT);
+    if (m & 4u) s += xv(DOWN);
+    if (m & 8u) s += xv(UP);
+    return ((float)nsolid_free(m) * xv(CTR) - s) * inv_h2;
 }
 
-// One damped Jacobi sweep at cell c from the input values xv: 0 off LIQUID
-// cells (and where no neighbour is non-SOLID).
+// One damped Jacobi sweep at a cell from the input values xv around it: 0 off
+// LIQUID cells (and where no neighbour is non-SOLID).
 template <class X>
-__device__ __forceinline__ float sweep_at(uint8_t m, int c, int nx, float inv_h2, float bc, X xv)
+__device__ __forceinline__ float sweep_at(uint8_t m, float inv_h2, float bc, X xv)
 {
     if (!liquid(m)) return 0.0f;
     const float d = (float)nsolid_free(m) * inv_h2;
     if (!(d > 0.0f)) return 0.0f;
-    return xv(c) + OMEGA * (bc - neg_apply(m, c, nx, inv_h2, xv)) / d;
+    return xv(CTR) + OMEGA * (bc - neg_apply(m, inv_h2, xv)) / d;
 }
 
 // The first sweep from a zero guess, which is pointwise.
@@ -163,8 +179,12 @@ __global__ void k_pre(Level L, const Scal* __restrict__ S)
     if (c64 >= (int64_t)L.nx * L.ny) return;
     const int c = (int)c64;
     const uint8_t m = L.nbi[c];
-    auto x1 = [&](int k) { return first_sweep(L.nbi[k], L.inv_h2, L.b[k]); };
-    L.x[c] = sweep_at(m, c, L.nx, L.inv_h2, L.b[c], x1);
+    const Around nbi_b{L.b, c, L.nx};
+    auto x1 = [&](int d) {
+        const int k = d == CTR ? c : d == LEFT ? c - 1 : d == RIGHT ? c + 1 : d == DOWN ? c - L.nx : c + L.nx;
+        return first_sweep(L.nbi[k], L.inv_h2, nbi_b(d));
+    };
+    L.x[c] = sweep_at(m, L.inv_h2, L.b[c], x1);
 }
 
 // Coarse right-hand side: the average of the LIQUID children's residuals
@@ -179,8 +199,7 @@ __global__ void k_restrict(Level F, Level C, const Scal* __restrict__ S)
         C.b[c] = 0.0f;
         return;
     }
-    const int I = c % C.nx, J = c / C.nx;
-    auto xv = [&](int k) { return F.x[k]; };
+    const int J = c / C.nx, I = c - J * C.nx;
     float s = 0.0f;
     for (int dj = 0; dj < 2; ++dj)
         for (int di = 0; di < 2; ++di) {
@@ -188,9 +207,30 @@ __global__ void k_restrict(Level F, Level C, const Scal* __restrict__ S)
             if (i >= F.nx || j >= F.ny) continue;
             const int f = i + j * F.nx;
             const uint8_t m = F.nbi[f];
-            if (liquid(m)) s += F.b[f] - neg_apply(m, f, F.nx, F.inv_h2, xv);
+            if (liquid(m)) s += F.b[f] - neg_apply(m, F.inv_h2, Around{F.x, f, F.nx});
         }
     C.b[c] = 0.25f * s;
+}
+
+// x + the parent's coarse correction at the neighbour (di, dj) of fine cell
+// (i, j) (di, dj in {-1, 0, 1}, the neighbour inside the grid).
+__device__ __forceinline__ float prolonged(const float* __restrict__ xf, const float* __restrict__ xc, int nxf, int nxc,
+                                           int i, int j, int di, int dj)
+{
+    const int fi = i + di, fj = j + dj;
+    return xf[fi + fj * nxf] + xc[(fi >> 1) + (fj >> 1) * nxc];
+}
+
+// One sweep of x + P xc at fine cell (i, j) (the neighbours read are those
+// the neighbour byte marks LIQUID, so inside the grid).
+__device__ __forceinline__ float post1_at(uint8_t m, int i, int j, int nx, int nxc, float inv_h2, float bc,
+                                          const float* __restrict__ xf, const float* __restrict__ xc)
+{
+    auto xv = [&](int d) {
+        return prolonged(xf, xc, nx, nxc, i, j, d == LEFT ? -1 : d == RIGHT ? 1 : 0,
+                         d == DOWN ? -1 : d == UP ? 1 : 0);
+    };
+    return sweep_at(m, inv_h2, bc, xv);
 }
 
 // First post-smoothing sweep of x + (the parent's coarse correction) into tmp.
@@ -200,8 +240,8 @@ __global__ void k_post1(Level F, Level C, const Scal* __restrict__ S)
     const int64_t c64 = (int64_t)blockIdx.x * TPB + threadIdx.x;
     if (c64 >= (int64_t)F.nx * F.ny) return;
     const int c = (int)c64;
-    auto xp = [&](int k) { return F.x[k] + C.x[(k % F.nx) / 2 + ((k / F.nx) / 2) * C.nx]; };
-    F.tmp[c] = sweep_at(F.nbi[c], c, F.nx, F.inv_h2, F.b[c], xp);
+    const int j = c / F.nx, i = c - j * F.nx;
+    F.tmp[c] = post1_at(F.nbi[c], i, j, F.nx, C.nx, F.inv_h2, F.b[c], F.x, C.x);
 }
 
 // ---- reductions: a fixed tree per block, the last block sums the blocks ----
@@ -228,8 +268,11 @@ __device__ __forceinline__ bool block_reduce(double v, double* __restrict__ part
     __syncthreads();
     if (!last) return false;
     __threadfence();
-    double acc = 0.0;
-    for (int k = threadIdx.x; k < (int)gridDim.x; k += blockDim.x) acc += __ldcg(&part[k]);
+    // (grids of at most 2 * blockDim.x blocks: both loads are issued before the add)
+    const int k0 = threadIdx.x, k1 = threadIdx.x + blockDim.x;
+    const double a0 = k0 < (int)gridDim.x ? __ldcg(&part[k0]) : 0.0;
+    const double a1 = k1 < (int)gridDim.x ? __ldcg(&part[k1]) : 0.0;
+    double acc = a0 + a1;
 #pragma unroll
     for (int s = 16; s >= 1; s >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, s);
     __syncthreads();
@@ -246,22 +289,24 @@ __device__ __forceinline__ bool block_reduce(double v, double* __restrict__ part
     return true;
 }
 
+// The reducing kernels walk the cells grid-stride (cell c of thread t of
+// block b: c = b * blockDim + t + k * gridDim * blockDim), so a reduction has
+// one partial per block, and its order is fixed by the launch shape.
+
 // Last post-smoothing sweep; at level 0 (z = M^-1 r) also r.z and beta.
 __global__ void k_post2(Level L, const float* __restrict__ r0, double* __restrict__ part, Scal* __restrict__ S)
 {
     if (S->done) return;
-    const int64_t c64 = (int64_t)blockIdx.x * TPB + threadIdx.x;
     const int n = L.nx * L.ny;
-    const int c = (int)c64;
-    float z = 0.0f;
-    if (c64 < n) {
-        auto tv = [&](int k) { return L.tmp[k]; };
-        z = sweep_at(L.nbi[c], c, L.nx, L.inv_h2, L.b[c], tv);
+    double v = 0.0;
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
+        const float z = sweep_at(L.nbi[c], L.inv_h2, L.b[c], Around{L.tmp, c, L.nx});
         L.x[c] = z;
+        if (r0) v += (double)r0[c] * z;
     }
     if (!r0) return;  // uniform over the grid
     double rz;
-    if (block_reduce(c64 < n ? (double)r0[c] * z : 0.0, part, &S->ticket, &rz) && threadIdx.x == 0) {
+    if (block_reduce(v, part, &S->ticket, &rz) && threadIdx.x == 0) {
         S->beta = S->it == 0 ? 0.0f : (float)(rz / S->rz);
         S->rz = rz;
     }
@@ -309,27 +354,22 @@ __global__ void __launch_bounds__(FUSED_THREADS, 1)
         const int n = L.nx * L.ny;
         for (int c = tid; c < n; c += FUSED_THREADS) T[k][c] = first_sweep(M[k][c], L.inv_h2, B[k][c]);
         __syncthreads();
-        {
-            const float* t = T[k];
-            auto tv = [&](int q) { return t[q]; };
-            for (int c = tid; c < n; c += FUSED_THREADS) X[k][c] = sweep_at(M[k][c], c, L.nx, L.inv_h2, B[k][c], tv);
-        }
+        for (int c = tid; c < n; c += FUSED_THREADS)
+            X[k][c] = sweep_at(M[k][c], L.inv_h2, B[k][c], Around{T[k], c, L.nx});
         __syncthreads();
         const Level& C = fu.lv[k + 1];
         const int nc = C.nx * C.ny;
-        const float* x = X[k];
-        auto xv = [&](int q) { return x[q]; };
         for (int c = tid; c < nc; c += FUSED_THREADS) {
             float s = 0.0f;
             if (liquid(M[k + 1][c])) {
-                const int I = c % C.nx, J = c / C.nx;
+                const int J = c / C.nx, I = c - J * C.nx;
                 for (int dj = 0; dj < 2; ++dj)
                     for (int di = 0; di < 2; ++di) {
                         const int i = 2 * I + di, j = 2 * J + dj;
                         if (i >= L.nx || j >= L.ny) continue;
                         const int f = i + j * L.nx;
                         const uint8_t m = M[k][f];
-                        if (liquid(m)) s += B[k][f] - neg_apply(m, f, L.nx, L.inv_h2, xv);
+                        if (liquid(m)) s += B[k][f] - neg_apply(m, L.inv_h2, Around{X[k], f, L.nx});
                     }
                 s = 0.25f * s;
             }
@@ -347,8 +387,8 @@ __global__ void __launch_bounds__(FUSED_THREADS, 1)
         for (int s = 0; s < COARSE_SWEEPS; ++s) {
             const float* xin = (s & 1) ? T[k] : X[k];
             float* xout = (s & 1) ? X[k] : T[k];
-            auto xv = [&](int q) { return xin[q]; };
-            for (int c = tid; c < n; c += FUSED_THREADS) xout[c] = sweep_at(M[k][c], c, L.nx, L.inv_h2, B[k][c], xv);
+            for (int c = tid; c < n; c += FUSED_THREADS)
+                xout[c] = sweep_at(M[k][c], L.inv_h2, B[k][c], Around{xin, c, L.nx});
             __syncthreads();
         }
         static_assert((COARSE_SWEEPS & 1) == 0, "the coarse result ends in X");
@@ -361,15 +401,14 @@ __global__ void __launch_bounds__(FUSED_THREADS, 1)
         {
             const float* x = X[k];
             const float* xc = X[k + 1];
-            auto xp = [&](int q) { return x[q] + xc[(q % L.nx) / 2 + ((q / L.nx) / 2) * C.nx]; };
-            for (int c = tid; c < n; c += FUSED_THREADS) T[k][c] = sweep_at(M[k][c], c, L.nx, L.inv_h2, B[k][c], xp);
+            for (int c = tid; c < n; c += FUSED_THREADS) {
+                const int j = c / L.nx, i = c - j * L.nx;
+                T[k][c] = post1_at(M[k][c], i, j, L.nx, C.nx, L.inv_h2, B[k][c], x, xc);
+            }
         }
         __syncthreads();
-        {
-            const float* t = T[k];
-            auto tv = [&](int q) { return t[q]; };
-            for (int c = tid; c < n; c += FUSED_THREADS) X[k][c] = sweep_at(M[k][c], c, L.nx, L.inv_h2, B[k][c], tv);
-        }
+        for (int c = tid; c < n; c += FUSED_THREADS)
+            X[k][c] = sweep_at(M[k][c], L.inv_h2, B[k][c], Around{T[k], c, L.nx});
         __syncthreads();
     }
     const int n0 = fu.lv[0].nx * fu.lv[0].ny;
@@ -397,13 +436,13 @@ __global__ void __launch_bounds__(FUSED_THREADS, 1)
 __global__ void k_cg_init(Level L, const float* __restrict__ b, float* __restrict__ x, float* __restrict__ r,
                           double* __restrict__ part, Scal* __restrict__ S, double tol, int maxit)
 {
-    const int64_t c = (int64_t)blockIdx.x * TPB + threadIdx.x;
+    const int n = L.nx * L.ny;
     double v = 0.0;
-    if (c < (int64_t)L.nx * L.ny) {
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
         const float rv = L.type[c] == LIQUID ? -b[c] : 0.0f;
         x[c] = 0.0f;
         r[c] = rv;
-        v = (double)rv * rv;
+        v += (double)rv * rv;
     }
     double bb;
     if (block_reduce(v, part, &S->ticket, &bb) && threadIdx.x == 0) {
@@ -423,22 +462,21 @@ __global__ void k_p_spmv(Level L, const float* __restrict__ z, float* __restrict
                          float* __restrict__ q, double* __restrict__ part, Scal* __restrict__ S)
 {
     if (S->done) return;
-    const int64_t c64 = (int64_t)blockIdx.x * TPB + threadIdx.x;
     const int n = L.nx * L.ny;
-    const int c = (int)c64;
     const bool first = S->it == 0;
     const float beta = S->beta;
     const float* pold = S->cur ? p1 : p0;
     float* pnew = S->cur ? p0 : p1;
-    auto pn = [&](int k) { return first ? z[k] : z[k] + beta * pold[k]; };
     double v = 0.0;
-    if (c64 < n) {
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
         const uint8_t m = L.nbi[c];
-        const float pc = pn(c);
-        const float qc = liquid(m) ? neg_apply(m, c, L.nx, L.inv_h2, pn) : 0.0f;
+        const Around zs{z, c, L.nx}, ps{pold, c, L.nx};
+        auto pn = [&](int d) { return first ? zs(d) : zs(d) + beta * ps(d); };
+        const float pc = pn(CTR);
+        const float qc = liquid(m) ? neg_apply(m, L.inv_h2, pn) : 0.0f;
         pnew[c] = pc;
         q[c] = qc;
-        v = (double)pc * qc;
+        v += (double)pc * qc;
     }
     double pq;
     if (block_reduce(v, part, &S->ticket, &pq) && threadIdx.x == 0) {
@@ -453,15 +491,14 @@ __global__ void k_update_xr(int64_t n, const float* __restrict__ p0, const float
                             double* __restrict__ part, Scal* __restrict__ S)
 {
     if (S->done) return;
-    const int64_t c = (int64_t)blockIdx.x * TPB + threadIdx.x;
     const float* pnew = S->cur ? p0 : p1;
+    const float a = S->alpha;
     double v = 0.0;
-    if (c < n) {
-        const float a = S->alpha;
+    for (int64_t c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
         x[c] += a * pnew[c];
         const float rv = r[c] - a * q[c];
         r[c] = rv;
-        v = (double)rv * rv;
+        v += (double)rv * rv;
     }
     double rr;
     if (block_reduce(v, part, &S->ticket, &rr) && threadIdx.x == 0) {
@@ -528,6 +565,7 @@ struct MgSolver
     cudaGraphExec_t iteration = nullptr;  // one CG iteration, recorded once per stream
     cudaStream_t iteration_stream = nullptr;
     int64_t per_iteration = 0;            // kernels of one CG iteration
+    unsigned rgrid = 1;                   // blocks of the reducing kernels
     int expect = 8;                       // iterations to launch before the first poll
 };
 
@@ -564,17 +602,17 @@ void vcycle(MgSolver* m, cudaStream_t st, int64_t* launches)
         Level& L = m->lv[l];
         const unsigned nb = nblk((int64_t)L.nx * L.ny);
         k_post1<<<nb, TPB, 0, st>>>(L, m->lv[l + 1], m->S);
-        k_post2<<<nb, TPB, 0, st>>>(L, l == 0 ? m->r : nullptr, m->part, m->S);
+        if (l == 0) k_post2<<<m->rgrid, RTPB, 0, st>>>(L, m->r, m->part, m->S);
+        else k_post2<<<nb, TPB, 0, st>>>(L, nullptr, m->part, m->S);
         *launches += 2;
     }
 }
 
 void cg_iteration(MgSolver* m, cudaStream_t st, int64_t* launches)
 {
-    const unsigned nb = nblk(m->n);
     vcycle(m, st, launches);
-    k_p_spmv<<<nb, TPB, 0, st>>>(m->lv[0], m->z, m->p0, m->p1, m->q, m->part, m->S);
-    k_update_xr<<<nb, TPB, 0, st>>>(m->n, m->p0, m->p1, m->q, m->x, m->r, m->part, m->S);
+    k_p_spmv<<<m->rgrid, RTPB, 0, st>>>(m->lv[0], m->z, m->p0, m->p1, m->q, m->part, m->S);
+    k_update_xr<<<m->rgrid, RTPB, 0, st>>>(m->n, m->p0, m->p1, m->q, m->x, m->r, m->part, m->S);
     *launches += 2;
 }
 
@@ -618,7 +656,11 @@ int mg_create(MgSolver** out, int nx, int ny, float dx, int device)
     const size_t N = (size_t)m->n;
     for (float** v : {&m->x, &m->p0, &m->p1, &m->q})
         if (e == cudaSuccess) e = alloc(m, (void**)v, 4 * N);
-    if (e == cudaSuccess) e = alloc(m, (void**)&m->part, 8 * (size_t)nblk(m->n));
+    int sms = 0;
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    m->rgrid = (unsigned)std::max<int64_t>(1, std::min<int64_t>(2 * (int64_t)sms, (m->n + RTPB - 1) / RTPB));
+    m->rgrid = std::min(m->rgrid, (unsigned)(2 * RTPB));  // the last block loads two partials per thread
+    if (e == cudaSuccess) e = alloc(m, (void**)&m->part, 8 * (size_t)m->rgrid);
     if (e == cudaSuccess) e = alloc(m, (void**)&m->S, sizeof(Scal));
     if (e == cudaSuccess) e = cudaMemset(m->S, 0, sizeof(Scal));
     // level 0 of the V-cycle: right-hand side = the CG residual, solution = z
@@ -654,7 +696,7 @@ void mg_set_labels(MgSolver* m, cudaStream_t st, const uint8_t* labels, int64_t*
 cudaError_t mg_solve(MgSolver* m, cudaStream_t st, const float* b, double tol, int maxit, int64_t* launches,
                      int* iterations, double* rr, double* bb, float** x_out)
 {
-    k_cg_init<<<nblk(m->n), TPB, 0, st>>>(m->lv[0], b, m->x, m->r, m->part, m->S, tol, maxit);
+    k_cg_init<<<m->rgrid, RTPB, 0, st>>>(m->lv[0], b, m->x, m->r, m->part, m->S, tol, maxit);
     *launches += 1;
     if (!m->iteration || m->iteration_stream != st) {
         if (m->iteration) cudaGraphExecDestroy(m->iteration);

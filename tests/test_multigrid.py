@@ -136,3 +136,33 @@ def test_mixed_precision_with_multigrid_corrections_reaches_1e10():
     print("mixed+MG", mm, "mixed+Jacobi", mj, "error", err)
     assert mm["residual"] < 1e-10 and err < 1e-8
     assert mm["inner_iterations"] * 10 < mj["inner_iterations"]
+
+
+def test_mgpcg_on_a_narrow_grid():
+    """A 6 x 200 domain: its coarse levels are one cell wide."""
+    fsbuild.build()
+    nx, ny = 6, 200
+    rng = np.random.default_rng(5)
+    labels = np.zeros((ny, nx), np.uint8)
+    labels[:, 0] = labels[:, -1] = 2
+    labels[0, :] = 2
+    labels[-20:, 1:-1] = 1  # AIR on top
+    labels[rng.random((ny, nx)) < 0.05] = 2
+    rhs = np.where(labels == 0, rng.standard_normal(labels.shape), 0.0)
+    ps = fsg.PoissonSolver(nx, ny, float(nx), float(ny))
+    ps.set_problem(labels, rhs)
+    mg = ps.solve(fsg.POISSON_MGPCG, 1e-6, 2000)
+    x = ps.solution()
+    jac = ps.solve(fsg.POISSON_FP32, 1e-6, 20000)
+    xj = ps.solution()
+    xd, singular, comp = direct_solve(labels, rhs)
+    for c in singular:
+        for v in (x, xj):
+            m = comp == c
+            v[m] -= v[m].mean()
+    err = np.linalg.norm(x - xd) / np.linalg.norm(xd)
+    err_j = np.linalg.norm(xj - xd) / np.linalg.norm(xd)
+    print("narrow MGPCG iterations", mg["inner_iterations"], "residual", mg["residual"], "error", err,
+          "| Jacobi-PCG", jac["inner_iterations"], jac["residual"], err_j)
+    # both solve in float vectors; this thin domain is ill-conditioned (cond ~ 200^2)
+    assert err < 1e-4 and mg["residual"] < max(1e-4, 10 * jac["residual"])
