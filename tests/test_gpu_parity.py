@@ -386,3 +386,26 @@ def test_p2g_weight_threshold_edge():
     ub0 = grids[fsg.U_BACK]
     uf = g.grid(fsg.U_FRONT)  # the back buffer became the front
     assert (uf == ub0).sum() > 0 and (uf != ub0).sum() > 0
+
+
+@pytest.mark.parametrize("method", [fsg.STEP_PICFLIP, fsg.STEP_SEMI_LAGRANGIAN])
+@pytest.mark.parametrize("length", [48.0, 12.0])
+def test_particles_on_cell_corners_and_faces(method, length):
+    """Particles exactly on grid lines: cell classification truncates x / dx at
+    an integer (src/FluidDomain.cpp:150-180) and the bilinear weights of the
+    splat and the gather are exactly 0 and 1 (include/Grid.h:117-184)."""
+    n = 48
+    dx = length / n
+    ii, jj = np.meshgrid(np.arange(4, 28) * 0.5, np.arange(4, 36) * 0.5)  # corners and face centres
+    rng = np.random.default_rng(9)
+    parts = np.stack([ii.ravel() * dx, jj.ravel() * dx,
+                      rng.standard_normal(ii.size), rng.standard_normal(ii.size)], 1).astype(np.float32)
+    g = fsg.FluidSim(n, n, length, length, 1.0, 0.05, cg_tolerance=1e-6, cg_max_iterations=2000)
+    o = po.OracleSim("restatement", n, n, length, length, 1.0, 0.05)
+    o.set_cg(1e-6, 2000)
+    g.set_particles(parts)
+    o.set_particles(parts)
+    for k in range(5):
+        g.step(method, 0.005)
+        assert o.step(method, 0.005) == 0
+        assert_same(g.state(), o.state(), where="grid-line particles step %d" % k)
