@@ -161,7 +161,8 @@ def test_obstacle_and_gravity_override():
 @pytest.mark.parametrize("precision", [fsg.CG_FLOAT, fsg.CG_DOUBLE])
 def test_large_grid_one_step_bit_exact(precision):
     """512x512 dam break with an obstacle (~430k particles), one full step:
-    multi-CTA CG with grid barriers, shared-memory-resident CG state."""
+    multi-CTA CG with grid barriers, register-resident CG state (at most 4
+    chunks per CTA)."""
     sc = scenes.dam_break_large(512)
     g, o = pair(sc, precision=precision)
     g.step(fsg.STEP_PICFLIP, sc.dt)
@@ -175,7 +176,7 @@ def test_large_grid_one_step_bit_exact(precision):
 
 @pytest.mark.parametrize("precision", [fsg.CG_FLOAT, fsg.CG_DOUBLE])
 def test_streaming_cg_matches_oracle(precision):
-    """A fluid region too large for the shared-memory-resident CG (more than
+    """A fluid region too large for the register-resident CG (more than
     8 x 1024 fluid cells per CTA): the streaming variant of the same kernel."""
     n = 1280
     sc = scenes.Scene(n, n, float(n), float(n), 0.01, 0.05, 0.01,
@@ -189,6 +190,24 @@ def test_streaming_cg_matches_oracle(precision):
     assert nf > 8 * 1024 * 152
     assert (st["cg_iterations"], st["n_fluid"]) == (it, nf)
     assert_same(g.state(), o.state(), keys=["pressure", "u_front", "v_front", "labels", "particles"], where="1280")
+
+
+@pytest.mark.parametrize("precision", [fsg.CG_FLOAT, fsg.CG_DOUBLE])
+def test_eight_chunk_register_form_matches_oracle(precision):
+    """5 to 8 chunks of 1024 fluid cells per CTA: the register-resident CG
+    with r and p in shared memory and the larger halo."""
+    n = 1024
+    sc = scenes.Scene(n, n, float(n), float(n), 0.01, 0.05, 0.01,
+                      scenes.block_particles(n, n, float(n), float(n), 1, 1000, 1, 800, 1, 12),
+                      cg_tolerance=1e-3, cg_max_iterations=60)
+    g, o = pair(sc, precision=precision)
+    g.step(fsg.STEP_PICFLIP, sc.dt)
+    o.step(po.STEP_PICFLIP, sc.dt)
+    st = g.stats()
+    it, err, nf = o.cg_stats()
+    assert 4 * 1024 * 152 < nf <= 8 * 1024 * 152
+    assert (st["cg_iterations"], st["n_fluid"]) == (it, nf)
+    assert_same(g.state(), o.state(), keys=["pressure", "u_front", "v_front", "labels", "particles"], where="1024")
 
 
 def test_non_square_cells_rejected_like_reference():
