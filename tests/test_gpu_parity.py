@@ -210,6 +210,46 @@ def test_eight_chunk_register_form_matches_oracle(precision):
     assert_same(g.state(), o.state(), keys=["pressure", "u_front", "v_front", "labels", "particles"], where="1024")
 
 
+@pytest.mark.parametrize("precision", [fsg.CG_FLOAT, fsg.CG_DOUBLE])
+def test_resident_and_streaming_ctas_in_one_solve(precision):
+    """8192 cells wide: the CTAs owning the full-width rows have halos of two
+    8190-cell rows, more than the 8-chunk form holds, and stream their state,
+    while the CTAs owning the narrow column above stay register-resident; all
+    share the solve's barriers and reduction tree."""
+    nx, ny = 8192, 400
+    wide = scenes.block_particles(nx, ny, float(nx), float(ny), 1, nx - 1, 1, 60, 1, 13)
+    narrow = scenes.block_particles(nx, ny, float(nx), float(ny), 1, 1500, 60, ny - 1, 1, 14)
+    sc = scenes.Scene(nx, ny, float(nx), float(ny), 0.01, 0.05, 0.01, np.concatenate([wide, narrow]),
+                      cg_tolerance=1e-3, cg_max_iterations=60)
+    g, o = pair(sc, precision=precision)
+    g.step(fsg.STEP_PICFLIP, sc.dt)
+    o.step(po.STEP_PICFLIP, sc.dt)
+    st = g.stats()
+    it, err, nf = o.cg_stats()
+    assert 4 * 1024 * 152 < nf <= 8 * 1024 * 152
+    assert (st["cg_iterations"], st["n_fluid"]) == (it, nf)
+    assert_same(g.state(), o.state(), keys=["pressure", "u_front", "v_front", "labels", "particles"], where="mixed")
+    # the case mixes the two forms: per-CTA halo extents (152 CTAs, chunks of 1024) around the
+    # 8-chunk form's capacity of 10,237 halo cells (204,800 B of shared memory, 16 B per owned cell)
+    liquid = g.labels() == 0
+    fidx = np.full(liquid.shape, -1, np.int64)
+    fidx[liquid] = np.arange(int(liquid.sum()))  # j-major, as the fluid indexing
+    down = np.full(liquid.shape, -1, np.int64)
+    up = np.full(liquid.shape, -1, np.int64)
+    down[1:] = np.where(liquid[:-1], fidx[:-1], -1)
+    up[:-1] = np.where(liquid[1:], fidx[1:], -1)
+    dn_of, up_of = down[liquid], up[liquid]
+    nchunks = (nf + 1023) // 1024
+    halos = []
+    for cta in range(152):
+        c0, c1 = cta * nchunks // 152, (cta + 1) * nchunks // 152
+        e0, e1 = c0 * 1024, min(c1 * 1024, nf)
+        lo = min(e0, dn_of[e0:e1][dn_of[e0:e1] >= 0].min(initial=e0), e0 - 1)
+        hi = max(e1, up_of[e0:e1].max(initial=e1) + 1, e1 + 1)
+        halos.append((e0 - lo) + (hi - e1))
+    assert max(halos) > 10237 and min(halos) <= 10237, (min(halos), max(halos))
+
+
 def test_non_square_cells_rejected_like_reference():
     g = fsg.FluidSim(32, 16, 32.0, 32.0, 0.005, 0.05)
     with pytest.raises(fsg.FsError) as ei:
