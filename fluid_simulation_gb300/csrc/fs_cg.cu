@@ -234,6 +234,31 @@ __device__ __forceinline__ void reduce_all(const CgArgs& a, int buf, int nchunks
         return;
     }
     int n = (nchunks + 31) / 32;
+    if (n <= 32) {
+        // group trees into lvlB, then every warp evaluates the tree over the
+        // groups itself (lvlB is not reused before the next reduction's
+        // group trees, so no trailing barrier)
+        if (warp < n) {
+            const int e = warp * 32 + lane;
+#pragma unroll
+            for (int k = 0; k < NV; ++k) {
+                const R v = e < nchunks ? __ldcg(&src[(size_t)k * a.max_chunks + e]) : R(0);
+                const R t = warp_tree<R>(v);
+                if (lane == 0) Ar<R>::lvlB(sm, warp, k) = t;
+            }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            if (n == 1) {
+                out[k] = Ar<R>::lvlB(sm, 0, k);
+            } else {
+                const R t = warp_tree<R>(lane < n ? Ar<R>::lvlB(sm, lane, k) : R(0));
+                out[k] = __shfl_sync(0xffffffffu, t, 0);
+            }
+        }
+        return;
+    }
     for (int g = warp; g < n; g += 32) {
         const int e = g * 32 + lane;
 #pragma unroll
