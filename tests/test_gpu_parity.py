@@ -468,3 +468,28 @@ def test_particles_on_cell_corners_and_faces(method, length):
         g.step(method, 0.005)
         assert o.step(method, 0.005) == 0
         assert_same(g.state(), o.state(), where="grid-line particles step %d" % k)
+
+
+@pytest.mark.parametrize("method", [fsg.STEP_PICFLIP, fsg.STEP_SEMI_LAGRANGIAN])
+def test_particles_outside_the_domain(method):
+    """Particles beyond every wall and on the domain's edge: classification,
+    the splat and the gather clamp their cells to the grid like the reference
+    (src/FluidDomain.cpp:150-180, include/Grid.h:117-184)."""
+    n, length = 40, 40.0
+    rng = np.random.default_rng(21)
+    block = scenes.block_particles(n, n, length, length, 2, 14, 2, 20, 2, 21)
+    xs = np.array([-2.5, -0.3, -1e-3, 0.0, length, length + 1e-3, 1.7 * length, 3.25 * length], np.float32)
+    ys = np.array([-1.5, -0.01, 0.0, 7.25, length, 1.2 * length, 2.0 * length, 19.5], np.float32)
+    xx, yy = np.meshgrid(xs, ys)
+    outside = np.stack([xx.ravel(), yy.ravel(), rng.standard_normal(xx.size), rng.standard_normal(xx.size)],
+                       1).astype(np.float32)
+    parts = np.concatenate([block, outside])
+    g = fsg.FluidSim(n, n, length, length, 1.0, 0.05, cg_tolerance=1e-6, cg_max_iterations=2000)
+    o = po.OracleSim("restatement", n, n, length, length, 1.0, 0.05)
+    o.set_cg(1e-6, 2000)
+    g.set_particles(parts)
+    o.set_particles(parts)
+    for k in range(5):
+        g.step(method, 0.005)
+        assert o.step(method, 0.005) == 0
+        assert_same(g.state(), o.state(), where="outside particles step %d" % k)
