@@ -474,7 +474,9 @@ def test_particles_on_cell_corners_and_faces(method, length):
 def test_particles_outside_the_domain(method):
     """Particles beyond every wall and on the domain's edge: classification,
     the splat and the gather clamp their cells to the grid like the reference
-    (src/FluidDomain.cpp:150-180, include/Grid.h:117-184)."""
+    (src/FluidDomain.cpp:150-180, include/Grid.h:117-184); the per-cell
+    particle count, which the reference does not clamp (src/FluidSolver.cpp:
+    353-360, undefined there), skips them here and in the oracle alike."""
     n, length = 40, 40.0
     rng = np.random.default_rng(21)
     block = scenes.block_particles(n, n, length, length, 2, 14, 2, 20, 2, 21)
