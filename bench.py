@@ -62,6 +62,10 @@ def parse():
     ap.add_argument("--no-forms", action="store_true", help="skip the batched and mixed-precision forms")
     ap.add_argument("--batch", type=int, default=512, help="members of the batched form")
     ap.add_argument("--projection-size", type=int, default=4096, help="grid side of the mixed-precision form")
+    ap.add_argument("--projection-methods", default="mixed_multigrid,mixed_f32_dots,mixed_f64_dots,fp64",
+                    help="solves of the mixed-precision form, in order (also fp32: the step's Jacobi CG alone)")
+    ap.add_argument("--projection-max-iterations", type=int, default=200000,
+                    help="CG iteration cap of each projection solve (a small cap makes a short profiling case)")
     ap.add_argument("--batch-plan", type=int, choices=[1, 2, 4, 8], default=None,
                     help="batched form: CG chunks per CTA instead of the autotuner's choice")
     ap.add_argument("--only-form", choices=["batched", "mixed_precision", "multigrid"], default=None,
@@ -326,17 +330,23 @@ def measure_projection(args, local_rank):
     ps.set_problem(labels, rhs)
     out = {"workload": "%dx%d projection, 5%% solids, N(0,1) rhs, relative residual 1e-10" % (n, n),
            "fluid_cells": int((labels == 0).sum())}
-    for name, method, inner in (("mixed_multigrid", fsg.POISSON_MIXED_MG, fsg.CG_FLOAT),
-                                ("mixed_f32_dots", fsg.POISSON_MIXED, fsg.CG_FLOAT),
-                                ("mixed_f64_dots", fsg.POISSON_MIXED, fsg.CG_DOUBLE),
-                                ("fp64", fsg.POISSON_FP64, fsg.CG_FLOAT)):
-        st = ps.solve(method, 1e-10, 200000, inner_tol=1e-3, inner_precision=inner)
+    methods = {"mixed_multigrid": (fsg.POISSON_MIXED_MG, fsg.CG_FLOAT),
+               "mixed_f32_dots": (fsg.POISSON_MIXED, fsg.CG_FLOAT),
+               "mixed_f64_dots": (fsg.POISSON_MIXED, fsg.CG_DOUBLE),
+               "fp64": (fsg.POISSON_FP64, fsg.CG_FLOAT),
+               "fp32": (fsg.POISSON_FP32, fsg.CG_FLOAT)}
+    for name in args.projection_methods.split(","):
+        method, inner = methods[name]
+        st = ps.solve(method, 1e-10, args.projection_max_iterations, inner_tol=1e-3, inner_precision=inner)
         out[name] = {"ms": st["ms"], "residual": st["residual"], "outer_iterations": st["outer_iterations"],
                      "inner_iterations": st["inner_iterations"],
                      "cell_solves_per_s": n * n / (st["ms"] / 1000.0)}
-    out["speedup_mixed_vs_fp64"] = out["fp64"]["ms"] / out["mixed_f32_dots"]["ms"]
-    out["speedup_mixed_multigrid_vs_fp64"] = out["fp64"]["ms"] / out["mixed_multigrid"]["ms"]
-    out["speedup_mixed_f64_dots_vs_fp64"] = out["fp64"]["ms"] / out["mixed_f64_dots"]["ms"]
+    if "fp64" in out:
+        for name, key in (("mixed_f32_dots", "speedup_mixed_vs_fp64"),
+                          ("mixed_multigrid", "speedup_mixed_multigrid_vs_fp64"),
+                          ("mixed_f64_dots", "speedup_mixed_f64_dots_vs_fp64")):
+            if name in out:
+                out[key] = out["fp64"]["ms"] / out[name]["ms"]
     ps.close()
     return out
 
