@@ -174,6 +174,22 @@ def test_large_grid_one_step_bit_exact(precision):
     assert st["cg_residual"] < sc.cg_tolerance
 
 
+def test_benchmark_workload_three_steps_bit_exact():
+    """The benchmark's own workload (1024x1024 dam break, disc obstacle,
+    1,716,100 particles, CG to 1e-5, stepPICFLIP): three steps, every array
+    bit-identical to the oracle after each, with the same CG iteration counts."""
+    sc = scenes.dam_break_large(1024)
+    g, o = pair(sc)
+    for k in range(3):
+        g.step(fsg.STEP_PICFLIP, sc.dt)
+        assert o.step(po.STEP_PICFLIP, sc.dt) == 0
+        st = g.stats()
+        it, err, nf = o.cg_stats()
+        assert (st["cg_iterations"], st["n_fluid"]) == (it, nf), k
+        assert st["cg_iterations"] > 1000 and st["cg_residual"] < sc.cg_tolerance
+        assert_same(g.state(), o.state(), where="1024 step %d" % k)
+
+
 @pytest.mark.parametrize("precision", [fsg.CG_FLOAT, fsg.CG_DOUBLE])
 def test_streaming_cg_matches_oracle(precision):
     """A fluid region too large for the register-resident CG (more than
