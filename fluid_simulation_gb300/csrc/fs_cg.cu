@@ -133,11 +133,11 @@ __device__ __forceinline__ R warp_tree(R v)
 // acquired view to the other threads, which read shared data with ld.cg.
 // Returns false if this CTA gave up waiting (after a.wait_ns); a CTA that
 // gives up returns, so every other CTA also gives up at its next barrier.
-__device__ __forceinline__ bool cta_barrier(const CgArgs& a, bool grid, unsigned& target, Smem& sm)
+__device__ __forceinline__ bool cta_barrier(const CgArgs& a, bool grid, unsigned arrivals, unsigned& target, Smem& sm)
 {
     // (callers come straight from level2, whose closing bar.sync orders the CTA's writes)
     if (grid && threadIdx.x == 0) {
-        target += gridDim.x;
+        target += arrivals;
         unsigned old;
         asm volatile("atom.add.acq_rel.gpu.global.u32 %0, [%1], 1;" : "=r"(old) : "l"(a.barrier) : "memory");
         int ok = 1;
@@ -164,9 +164,10 @@ struct GridSync
 {
     bool grid;
     unsigned target;
+    int active;  // CTAs taking part: the fewest that keep the most chunks per CTA unchanged
     __device__ int rank() const { return grid ? (int)blockIdx.x : 0; }
-    __device__ int size() const { return grid ? (int)gridDim.x : 1; }
-    __device__ bool barrier(const CgArgs& a, Smem& sm) { return cta_barrier(a, grid, target, sm); }
+    __device__ int size() const { return grid ? active : 1; }
+    __device__ bool barrier(const CgArgs& a, Smem& sm) { return cta_barrier(a, grid, (unsigned)active, target, sm); }
 };
 
 // ... or the CTAs of one thread-block cluster, which the hardware schedules
@@ -762,7 +763,10 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(CgArgs a)
     if (!grid && blockIdx.x != 0) return;
     const int per_cta = grid ? (nchunks + gridDim.x - 1) / gridDim.x : nchunks;
     const bool resident = per_cta <= KREG;
-    GridSync sync{grid, 0u};
+    // the CTAs beyond ceil(nchunks / per_cta) would only add arrivals to every barrier
+    const int active = grid ? (nchunks + per_cta - 1) / per_cta : 1;
+    if (grid && (int)blockIdx.x >= active) return;
+    GridSync sync{grid, 0u, active};
     const bool ran = resident && (per_cta <= 4 ? cg_lean<4, R>(a, sm, dyn, nf, nchunks, sync)
                                                : cg_lean<KREG, R>(a, sm, dyn, nf, nchunks, sync));
     if (!ran) cg_stream<R>(a, sm, nf, nchunks, sync);
