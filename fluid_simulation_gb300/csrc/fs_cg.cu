@@ -44,7 +44,7 @@ namespace {
 constexpr int CG_THREADS = 1024;
 constexpr int CHUNK = CG_THREADS;
 constexpr int KREG = 8;                   // most chunks per CTA in the register-resident form
-constexpr size_t DYN_BYTES = 204800;      // dynamic shared memory of k_cg: 12 B per resident cell + halo
+constexpr size_t DYN_BYTES = 204800;      // dynamic shared memory of k_cg: 12 B (16 B above 4 chunks) per cell + halo
 constexpr int SINGLE_CTA_CHUNKS = 16;       // systems this small run in one CTA
 constexpr int MAX_CHUNKS = 32 * 1024;       // all-read reduction limit (33.5M cells)
 constexpr uint64_t WAIT_LIMIT_NS = 2000000000ull;
