@@ -81,7 +81,7 @@ size_t fluid_index_batch_tmp_ints(const Domain& d);
 void fluid_index_batch(const Launch& L, const Domain& d, const uint8_t* labels, int32_t* fidx, int32_t* cell_of,
                        int32_t* nfluid, int32_t* tmp);
 
-// ---- stable radix sort + ordered splat (fs_splat.cu) ---------------------
+// ---- counting-sort binning + ordered splat (fs_splat.cu) -----------------
 struct SplatWork
 {
     uint32_t* keys = nullptr;      // bin of each item
