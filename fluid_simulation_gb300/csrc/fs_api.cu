@@ -364,7 +364,7 @@ void destroy_all(fs_handle* h)
                     h->counts8, h->acc[0], h->acc[1], h->acc[2], h->acc[3], h->grid_tmp, h->sl[0], h->sl[1],
                     h->sl[2], h->sl[3], h->sl[4], h->sl[5], h->sl_ok[0], h->sl_ok[1], h->px, h->py, h->pvx,
                     h->pvy, h->yu, h->xv, h->staging, h->cg.x, h->cg.r, h->cg.z,
-                    h->cg.p, h->cg.q, h->cg.partials, h->cg.barrier, h->cg.result, h->cg_b, h->cg_down, h->cg_up,
+                    h->cg.p, h->cg.q, h->cg.partials, h->cg.barrier, h->cg.result, h->cg.route, h->cg_b, h->cg_down, h->cg_up,
                     h->cg_flags, h->d_nfluid, h->d_status, h->d_warn, h->scan_tmp};
     for (void* p : ptrs) cudaFree(p);
     splat_free(h->sw);
@@ -387,10 +387,8 @@ int device_status(fs_handle* h)
     if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
     if (e != cudaSuccess) return cuda_fail(h, e, "synchronize");
     if (st & ST_TIMEOUT) {
-        // The aborted solve did not advance the tag sequence; clear its tagged
-        // partials so that none of them can match a later solve's tags.
-        const int64_t max_chunks = (h->ncell + 1023) / 1024;
-        cudaMemsetAsync(h->cg.partials, 0, sizeof(double) * 8 * (size_t)max_chunks, h->stream);
+        // Every solve clears the barrier counter before it starts and writes
+        // its partials before reading them, so only the status word is reset.
         cudaMemsetAsync(h->d_status, 0, sizeof(unsigned), h->stream);
         cudaStreamSynchronize(h->stream);
         return fail(h, FS_ERR_TIMEOUT, "a device-side wait of the CG kernel timed out");
@@ -540,18 +538,22 @@ int fs_create(const fs_config* cfg, fs_handle** out)
     A(dalloc(&h->counts8, N));
     for (int k = 0; k < 4; ++k) A(dalloc(&h->acc[k], N));
     A(dalloc(&h->grid_tmp, N));
-    A(dalloc(&h->cg.x, N));
-    A(dalloc(&h->cg.r, N));
-    A(dalloc(&h->cg.z, N));
-    A(dalloc(&h->cg.p, N));
-    A(dalloc(&h->cg.q, N));
+    // The CG kernel copies whole 1024-element chunks of its system arrays, so
+    // they are allocated to the last chunk's end.
+    const size_t NP = (size_t)max_chunks * 1024;
+    A(dalloc(&h->cg.x, NP));
+    A(dalloc(&h->cg.r, NP));
+    A(dalloc(&h->cg.z, NP));
+    A(dalloc(&h->cg.p, NP));
+    A(dalloc(&h->cg.q, NP));
     A(dalloc(&h->cg.partials, (size_t)8 * max_chunks));
     A(dalloc(&h->cg.barrier, 1));
     A(dalloc(&h->cg.result, 1));
+    A(dalloc(&h->cg.route, 2));
     A(dalloc(&h->cg_b, N));
-    A(dalloc(&h->cg_down, N));
-    A(dalloc(&h->cg_up, N));
-    A(dalloc(&h->cg_flags, N));
+    A(dalloc(&h->cg_down, NP));
+    A(dalloc(&h->cg_up, NP));
+    A(dalloc(&h->cg_flags, NP));
     A(dalloc(&h->d_nfluid, 1));
     A(dalloc(&h->d_status, 1));
     A(dalloc(&h->d_warn, 1));

@@ -31,9 +31,12 @@
 // with the same float operations.  A CTA that owns at most KREG chunks of 1024
 // cells keeps their state in registers and shared memory and stages the p_new
 // values its rows read from other CTAs into a shared-memory halo once per
-// iteration; larger systems stream the state from global memory.  Waits are
-// bounded: a CTA that waits longer than about two seconds sets ST_TIMEOUT and
-// every CTA returns.
+// iteration; larger systems stream the state from global memory: in k_cg,
+// or, from PIPE_MIN_CHUNKS chunks per CTA with float dot products, in
+// k_cg_pipe, which copies each slot's operands into shared memory with
+// cp.async several slots ahead of their use (k_cg_route picks one of the two
+// on the device).  Waits are bounded: a CTA that waits longer than about two
+// seconds sets ST_TIMEOUT and every CTA returns.
 #include <type_traits>
 
 #include "fs_internal.h"
@@ -142,9 +145,9 @@ __device__ __forceinline__ bool cta_barrier(const CgArgs& a, bool grid, unsigned
         asm volatile("atom.add.acq_rel.gpu.global.u32 %0, [%1], 1;" : "=r"(old) : "l"(a.barrier) : "memory");
         int ok = 1;
         const unsigned want = target + a.missing;
-        if (old + 1u < want && ld_acquire_u32(a.barrier) < want) {
+        if (!count_reached(old + 1u, want) && !count_reached(ld_acquire_u32(a.barrier), want)) {
             const uint64_t t0 = globaltimer_ns();
-            while (ld_acquire_u32(a.barrier) < want) {
+            while (!count_reached(ld_acquire_u32(a.barrier), want)) {
                 if (globaltimer_ns() - t0 > a.wait_ns) {
                     atomicOr(a.status, ST_TIMEOUT);
                     ok = 0;
@@ -472,6 +475,340 @@ __device__ __forceinline__ void cg_stream(const CgArgs& a, Smem& sm, int nf, int
     }
 }
 
+// ---- asynchronous copies into shared memory (cp.async: generic proxy, the
+// copying thread waits for its own groups).  Shared destinations are
+// shared-window addresses, global sources global-window addresses.
+__device__ __forceinline__ unsigned long long gaddr(const void* p)
+{
+    return (unsigned long long)__cvta_generic_to_global(p);
+}
+__device__ __forceinline__ void cp_async16(unsigned dst, unsigned long long src)
+{
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async4(unsigned dst, unsigned long long src)
+{
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(dst), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+// Until at most N of this thread's most recent groups are pending.
+template <int N>
+__device__ __forceinline__ void cp_wait()
+{
+    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+template <int N>
+using IntC = std::integral_constant<int, N>;
+
+// Shared-memory layout of the pipelined streaming form.  Every warp owns a
+// private 6400-byte region and copies only the 32 cells it computes (plus
+// the 4-cell pieces around them that its edge lanes read), so no copy ever
+// needs a CTA barrier.  Phase A keeps PA_STAGES slots of stage 1 (z, p, down,
+// up: 128 bytes each; flags: 32; the z and p of the 4 cells before and after
+// the warp's cells: 64) and PG_STAGES slots of stage 2 (z and p of each
+// cell's down and up neighbours, gathered once its indices have arrived);
+// phase B keeps PB_STAGES slots of z, p, x, r, q and flags.  The two phases
+// use the same bytes: each starts after the other's copies have all landed.
+constexpr int PIPE_MIN_CHUNKS = 20;  // chunks per CTA from which k_cg_pipe takes the solve
+constexpr int PIPE_WARP_BYTES = (int)(DYN_BYTES / 32);
+constexpr int PA_ENTRY = 4 * 128 + 32 + 64;
+constexpr int PA_STAGES = 6;
+constexpr int PA_AHEAD = PA_STAGES - 1;
+constexpr int PG_ENTRY = 4 * 128;
+constexpr int PG_STAGES = 3;
+constexpr int PG_AHEAD = PG_STAGES - 1;
+constexpr int PB_ENTRY = 5 * 128 + 32;
+constexpr int PB_STAGES = 9;
+constexpr int PB_AHEAD = PB_STAGES - 1;
+static_assert(PA_STAGES * PA_ENTRY + PG_STAGES * PG_ENTRY <= PIPE_WARP_BYTES, "phase A stages");
+static_assert(PB_STAGES * PB_ENTRY <= PIPE_WARP_BYTES, "phase B stages");
+static_assert(PIPE_WARP_BYTES % 16 == 0 && PA_ENTRY % 16 == 0 && PB_ENTRY % 16 == 0, "16-byte copies");
+// k_cg_pipe's CTAs own at least PIPE_MIN_CHUNKS - 1 slots
+static_assert(PIPE_MIN_CHUNKS - 1 > PA_AHEAD, "a CTA's last slot is copied after the barrier");
+
+// Phase A's copy groups, in commit order: G1(0..PA_AHEAD-1) (stage 1 of the
+// first slots, before the barrier), G2(0..PG_AHEAD-1) (their gathers), then
+// per slot k: G2(k + PG_AHEAD), G1(k + PA_AHEAD).  Groups committed after
+// G1(k + PG_AHEAD) when slot k starts, and after G2(k) once slot k's own
+// groups are committed:
+__host__ __device__ constexpr int pa_wait1(int k)
+{
+    return k + PG_AHEAD <= PA_AHEAD - 1 ? PA_AHEAD - 1 + k : 2 * (PA_AHEAD - PG_AHEAD - 1);
+}
+__host__ __device__ constexpr int pa_wait2(int k) { return k < PG_AHEAD ? PG_AHEAD + 1 + k : 2 * PG_AHEAD + 1; }
+constexpr int PA_PEEL = 3;  // slots before both counts settle
+static_assert(PA_PEEL >= PA_AHEAD - PG_AHEAD && PA_PEEL >= PG_AHEAD, "steady waits from slot PA_PEEL on");
+static_assert(PIPE_MIN_CHUNKS - 1 > PA_PEEL, "the peeled slots exist");
+
+// The streaming solve (state in global memory) with the cells' operands
+// copied into shared memory several slots ahead of their use.  The
+// arithmetic, the reduction tree and the exchanges are those of cg_stream;
+// only where each operand is read from differs.  Used by grid launches only
+// (every chunk partial goes through global memory).  The system arrays are
+// read in whole 1024-cell chunks, so they must be allocated to the last
+// chunk's end.
+template <typename R, class Sync>
+__device__ __forceinline__ void cg_pipe(const CgArgs& a, Smem& sm, unsigned char* dyn, int nf, int nchunks,
+                                        Sync& sync)
+{
+    const int tid = threadIdx.x;
+    const int lane = tid & 31, warp = tid >> 5;
+    const int ncta = sync.size();
+    const int cta = sync.rank();
+    const int c0 = (int)(((int64_t)cta * nchunks) / ncta);
+    const int c1 = (int)(((int64_t)(cta + 1) * nchunks) / ncta);
+    const int kb = c1 - c0;
+    const int e0 = c0 * CHUNK;
+    const int e_end = c1 * CHUNK;  // first element of the next CTA's chunks
+    const int NONE = 0x7fffffff;   // slot base of a slot past the CTA's last
+    const float* dtab = sm.dtab;
+    const float* itab = sm.itab;
+    const float off = a.off;
+    unsigned char* const wb = dyn + (size_t)warp * PIPE_WARP_BYTES;
+    const unsigned swb = (unsigned)__cvta_generic_to_shared(wb);
+    unsigned char* const gring = wb + PA_STAGES * PA_ENTRY;
+    const unsigned sgring = swb + PA_STAGES * PA_ENTRY;
+    bool first = true;
+    float beta = 0.0f;
+    auto slot_base = [&](int k) { return k < kb ? (c0 + k) * CHUNK + warp * 32 : NONE; };
+
+    // This lane's copies, fixed for the solve: source = base + slot base x
+    // scale, destination = entry + offset.  Phase A: 16 bytes of z, p, down or
+    // up (lane / 8, piece lane % 8), then lanes 0-1 the flags, 2-3 z and p of
+    // the 4 cells before the warp's, 4-5 z and p of the 4 after them.  Phase
+    // B: 16 bytes of z, p, x or r, then lanes 0-7 q and 8-9 the flags.
+    const int arr = lane >> 3, piece = lane & 7;
+    const unsigned long long gz = gaddr(a.z), gp = gaddr(a.p), gfl = gaddr(a.flags);
+    const unsigned long long a1_src =
+        (arr == 0 ? gz : arr == 1 ? gp : arr == 2 ? gaddr(a.down) : gaddr(a.up)) + piece * 16;
+    const int a2_kind = lane < 2 ? 0 : lane < 4 ? 1 : lane < 6 ? 2 : 3;  // flags, before, after, none
+    const unsigned long long a2_src = a2_kind == 0   ? gfl + lane * 16
+                                      : a2_kind == 1 ? (lane == 2 ? gz : gp) - 16
+                                                     : (lane == 4 ? gz : gp) + 128;
+    const unsigned a2_scale = a2_kind == 0 ? 1u : 4u;
+    const unsigned a2_dst = a2_kind == 0 ? 512 + lane * 16 : 544 + (lane - 2) * 16;
+    const unsigned long long b1_src =
+        (arr == 0 ? gz : arr == 1 ? gp : arr == 2 ? gaddr(a.x) : gaddr(a.r)) + piece * 16;
+    const bool b2_on = lane < 10;
+    const unsigned long long b2_src = lane < 8 ? gaddr(a.q) + lane * 16 : gfl + (lane - 8) * 16;
+    const unsigned b2_scale = lane < 8 ? 4u : 1u;
+
+    // Stage 1 of phase A for the slot at element base eb into the entry at
+    // shared address dst.  Before the barrier that publishes the other CTAs'
+    // z and p (post == false), the piece before the CTA's first cell is left
+    // out; fix_edge copies it after the barrier.
+    auto issue_a1 = [&](int eb, unsigned dst, bool post) {
+        if (eb >= nf) return;
+        cp_async16(dst + lane * 16, a1_src + (unsigned)eb * 4u);
+        const bool on = a2_kind == 0 || (a2_kind == 1 && eb > 0 && (post || eb != e0)) ||
+                        (a2_kind == 2 && eb + 32 < nf && (post || eb + 32 != e_end));
+        if (on) cp_async16(dst + a2_dst, a2_src + (unsigned long long)((unsigned)eb * a2_scale));
+    };
+    auto fix_edge = [&]() {
+        if (warp == 0 && (lane == 2 || lane == 3) && e0 > 0)
+            cp_async16(swb + a2_dst, a2_src + (unsigned long long)((unsigned)e0 * 4u));
+    };
+    // Stage 2 of phase A for the slot at element base eb (indices in its
+    // stage-1 entry en): z and p of the down and up neighbours into the gather
+    // entry at dst.
+    auto issue_gather = [&](int eb, const unsigned char* en, unsigned dst) {
+        if (eb >= nf || eb + lane >= nf) return;
+        const int dn = reinterpret_cast<const int*>(en + 256)[lane];
+        const int up = reinterpret_cast<const int*>(en + 384)[lane];
+        if (dn >= 0) {
+            cp_async4(dst + lane * 4, gz + (unsigned)dn * 4u);
+            if (!first) cp_async4(dst + 128 + lane * 4, gp + (unsigned)dn * 4u);
+        }
+        if (up >= 0) {
+            cp_async4(dst + 256 + lane * 4, gz + (unsigned)up * 4u);
+            if (!first) cp_async4(dst + 384 + lane * 4, gp + (unsigned)up * 4u);
+        }
+    };
+    auto issue_b = [&](int eb, unsigned dst) {
+        if (eb >= nf) return;
+        cp_async16(dst + lane * 16, b1_src + (unsigned)eb * 4u);
+        if (b2_on) cp_async16(dst + 512 + lane * 16, b2_src + (unsigned long long)((unsigned)eb * b2_scale));
+    };
+    auto prologue_a = [&]() {
+        for (int k = 0; k < PA_AHEAD; ++k) {
+            issue_a1(slot_base(k), swb + k * PA_ENTRY, false);
+            cp_commit();
+        }
+    };
+    auto prologue_b = [&]() {
+        for (int k = 0; k < PB_AHEAD; ++k) {
+            issue_b(slot_base(k), swb + k * PB_ENTRY);
+            cp_commit();
+        }
+    };
+    auto pnew = [&](float z, float p) { return first ? z : fadd(z, fmul(beta, p)); };
+    auto wrap = [](int o, int stride, int end) { return o + stride == end ? 0 : o + stride; };
+
+    // ---- initialisation: x = 0, r = b, z = M^-1 r; bb = r.r, rz = r.z
+    for (int base = 0; base < kb; base += 32) {
+        const int nslot = min(32, kb - base);
+        for (int sl = 0; sl < nslot; ++sl) {
+            const int e = (c0 + base + sl) * CHUNK + tid;
+            R v[2] = {R(0), R(0)};
+            if (e < nf) {
+                const float r = a.b[e];
+                const uint8_t fl = a.flags[e];
+                const float z = fmul(itab[fl >> 2], r);
+                __stcg(&a.z[e], z);
+                v[0] = Ar<R>::prod(r, r);
+                v[1] = Ar<R>::prod(r, z);
+                __stcg(&a.x[e], 0.0f);
+                __stcg(&a.r[e], r);
+            }
+            level1<R, 2>(v, sl, sm);
+        }
+        level2<R, 2>(a, 0, c0 + base, nslot, sm);
+    }
+    prologue_a();
+    R red2[2];
+    if (!sync.barrier(a, sm)) {
+        cp_wait_all();
+        return;
+    }
+    reduce_all<R, 2>(a, 0, nchunks, sm, red2);
+    const R bb = red2[0];
+    R rz = red2[1];
+    R rr = bb;
+    int iters = 0;
+    bool done = bb == R(0);
+    const R tolr = (R)a.tol;
+    R thr = Ar<R>::mul(Ar<R>::mul(tolr, tolr), bb);
+    if (thr < Ar<R>::tiny()) thr = Ar<R>::tiny();
+    if (!done && rr < thr) done = true;
+
+    constexpr int A_END = PA_STAGES * PA_ENTRY, G_END = PG_STAGES * PG_ENTRY, B_END = PB_STAGES * PB_ENTRY;
+    for (int it = 1; !done && it <= a.maxit; ++it) {
+        // ---- phase A: p_new = z + beta p, q = A p_new, partial p.q
+        // Ring offsets: oa / og of slot k's entries, oa_g of slot
+        // k + PG_AHEAD's stage-1 entry; slot k + PA_AHEAD reuses slot k - 1's
+        // stage-1 entry (oa_prev), and slot k + PG_AHEAD slot k - 1's gather
+        // entry (og_prev).
+        fix_edge();
+        for (int j = 0; j < PG_AHEAD; ++j) {
+            cp_wait<PA_AHEAD - 1>();  // G1(j)
+            __syncwarp();
+            issue_gather(slot_base(j), wb + j * PA_ENTRY, sgring + j * PG_ENTRY);
+            cp_commit();
+        }
+        int oa = 0, oa_prev = A_END - PA_ENTRY, oa_g = PG_AHEAD * PA_ENTRY, og = 0, og_prev = G_END - PG_ENTRY;
+        auto step_a = [&](int k, auto w1, auto w2) {
+            cp_wait<decltype(w1)::value>();  // G1(k + PG_AHEAD)
+            __syncwarp();
+            issue_gather(slot_base(k + PG_AHEAD), wb + oa_g, sgring + og_prev);
+            cp_commit();
+            issue_a1(slot_base(k + PA_AHEAD), swb + oa_prev, true);
+            cp_commit();
+            cp_wait<decltype(w2)::value>();  // G2(k)
+            __syncwarp();
+            const unsigned char* en = wb + oa;
+            const float* ez = reinterpret_cast<const float*>(en);
+            const float* edge = reinterpret_cast<const float*>(en + 544);
+            const float* g = reinterpret_cast<const float*>(gring + og);
+            const int e = (c0 + k) * CHUNK + warp * 32 + lane;
+            float pe = 0.0f;
+            if (e < nf) pe = pnew(ez[lane], ez[32 + lane]);
+            float pl = __shfl_up_sync(0xffffffffu, pe, 1);
+            float pr = __shfl_down_sync(0xffffffffu, pe, 1);
+            R v[1] = {R(0)};
+            if (e < nf) {
+                const unsigned fl = en[512 + lane];
+                const int dn = reinterpret_cast<const int*>(en + 256)[lane];
+                const int up = reinterpret_cast<const int*>(en + 384)[lane];
+                if (lane == 0 && (fl & 1u)) pl = pnew(edge[3], edge[7]);
+                if (lane == 31 && (fl & 2u)) pr = pnew(edge[8], edge[12]);
+                float acc = 0.0f;
+                if (dn >= 0) acc = fadd(acc, fmul(off, pnew(g[lane], g[32 + lane])));
+                if (fl & 1u) acc = fadd(acc, fmul(off, pl));
+                acc = fadd(acc, fmul(dtab[fl >> 2], pe));
+                if (fl & 2u) acc = fadd(acc, fmul(off, pr));
+                if (up >= 0) acc = fadd(acc, fmul(off, pnew(g[64 + lane], g[96 + lane])));
+                v[0] = Ar<R>::prod(pe, acc);
+                __stcg(&a.q[e], acc);
+            }
+            level1<R, 1>(v, k & 31, sm);
+            if ((k & 31) == 31 || k == kb - 1) level2<R, 1>(a, 1, c0 + (k & ~31), (k & 31) + 1, sm);
+            oa_prev = oa;
+            oa = wrap(oa, PA_ENTRY, A_END);
+            oa_g = wrap(oa_g, PA_ENTRY, A_END);
+            og_prev = og;
+            og = wrap(og, PG_ENTRY, G_END);
+        };
+        step_a(0, IntC<pa_wait1(0)>{}, IntC<pa_wait2(0)>{});
+        step_a(1, IntC<pa_wait1(1)>{}, IntC<pa_wait2(1)>{});
+        step_a(2, IntC<pa_wait1(2)>{}, IntC<pa_wait2(2)>{});
+        static_assert(PA_PEEL == 3, "three peeled slots above");
+        for (int k = PA_PEEL; k < kb; ++k) step_a(k, IntC<pa_wait1(PA_PEEL)>{}, IntC<pa_wait2(PA_PEEL)>{});
+        prologue_b();
+        R red1[1];
+        if (!sync.barrier(a, sm)) {
+            cp_wait_all();
+            return;
+        }
+        reduce_all<R, 1>(a, 1, nchunks, sm, red1);
+        const float alpha = Ar<R>::ratio(rz, red1[0]);
+
+        // ---- phase B: x += alpha p, r -= alpha q, z = M^-1 r; publish z, p; partial r.r, r.z
+        // Groups: GB(0..PB_AHEAD-1) before the barrier, then GB(k + PB_AHEAD)
+        // per slot k, into slot k - 1's entry.
+        int ob = 0, ob_prev = B_END - PB_ENTRY;
+        for (int k = 0; k < kb; ++k) {
+            issue_b(slot_base(k + PB_AHEAD), swb + ob_prev);
+            cp_commit();
+            cp_wait<PB_AHEAD>();  // GB(k)
+            __syncwarp();
+            const float* en = reinterpret_cast<const float*>(wb + ob);
+            const unsigned char* efl = wb + ob + 640;
+            const int e = (c0 + k) * CHUNK + warp * 32 + lane;
+            R v[2] = {R(0), R(0)};
+            if (e < nf) {
+                const float pn = pnew(en[lane], en[32 + lane]);
+                float x = en[64 + lane];
+                float r = en[96 + lane];
+                const float q = en[128 + lane];
+                const unsigned fl = efl[lane];
+                x = fadd(x, fmul(alpha, pn));
+                r = fsub(r, fmul(alpha, q));
+                const float z = fmul(itab[fl >> 2], r);
+                __stcg(&a.x[e], x);
+                __stcg(&a.r[e], r);
+                __stcg(&a.z[e], z);
+                __stcg(&a.p[e], pn);
+                v[0] = Ar<R>::prod(r, r);
+                v[1] = Ar<R>::prod(r, z);
+            }
+            level1<R, 2>(v, k & 31, sm);
+            if ((k & 31) == 31 || k == kb - 1) level2<R, 2>(a, 0, c0 + (k & ~31), (k & 31) + 1, sm);
+            ob_prev = ob;
+            ob = wrap(ob, PB_ENTRY, B_END);
+        }
+        prologue_a();
+        if (!sync.barrier(a, sm)) {
+            cp_wait_all();
+            return;
+        }
+        reduce_all<R, 2>(a, 0, nchunks, sm, red2);
+        rr = red2[0];
+        iters = it;
+        if (rr < thr) break;
+        beta = Ar<R>::ratio(red2[1], rz);
+        rz = red2[1];
+        first = false;
+    }
+    cp_wait_all();
+    if (cta == 0 && tid == 0) {
+        a.result->iterations = iters;
+        a.result->rr = (double)rr;
+        a.result->bb = (double)bb;
+        a.result->status = 0;
+    }
+}
+
 // Register-resident form of the solve, for CTAs that own at most K chunks.
 // The owned cells' z (q between the SpMV and the update) live in registers,
 // and r and p too for K <= 4 (slot s of thread t is element
@@ -734,6 +1071,40 @@ __device__ __forceinline__ bool cg_lean(const CgArgs& a, Smem& sm, unsigned char
     return true;
 }
 
+// Splits a solve between k_cg and k_cg_pipe: route[0] = the fluid cells k_cg
+// solves, route[1] = those k_cg_pipe solves; one of the two is 0.  k_cg_pipe
+// takes the large systems with enough chunks per CTA (and that k_cg accepts).
+__global__ void k_cg_route(const int32_t* __restrict__ nfluid, int max_chunks, int grid, int32_t* __restrict__ route)
+{
+    const int nf = *nfluid;
+    const int nchunks = (nf + CHUNK - 1) / CHUNK;
+    const bool pipe = nchunks <= max_chunks && nchunks <= MAX_CHUNKS && nchunks > SINGLE_CTA_CHUNKS &&
+                      (nchunks + grid - 1) / grid >= PIPE_MIN_CHUNKS;
+    route[0] = pipe ? 0 : nf;
+    route[1] = pipe ? nf : 0;
+}
+
+// Large systems with FP32 dot products: the pipelined streaming form, on the
+// system k_cg_route gave it (none: return without a result; k_cg wrote it).
+__global__ void __launch_bounds__(CG_THREADS, 1) k_cg_pipe(CgArgs a)
+{
+    __shared__ Smem sm;
+    extern __shared__ __align__(16) unsigned char dyn[];
+    const int nf = *a.nfluid;
+    if (nf == 0) return;
+    const int nchunks = (nf + CHUNK - 1) / CHUNK;
+    const int per_cta = (nchunks + gridDim.x - 1) / gridDim.x;
+    const int active = (nchunks + per_cta - 1) / per_cta;
+    if ((int)blockIdx.x >= active) return;
+    if (threadIdx.x < 5) {
+        sm.dtab[threadIdx.x] = a.dtab[threadIdx.x];
+        sm.itab[threadIdx.x] = a.itab[threadIdx.x];
+    }
+    __syncthreads();
+    GridSync sync{true, 0u, active};
+    cg_pipe<float>(a, sm, dyn, nf, nchunks, sync);
+}
+
 template <typename R>
 __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(CgArgs a)
 {
@@ -841,7 +1212,9 @@ int cg_prepare(CgWork& w, int device)
         cudaFuncSetAttribute(k_cg<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)DYN_BYTES) !=
             cudaSuccess)
         return -1;
-    for (const void* f : {(const void*)k_cg<float>, (const void*)k_cg<double>}) {
+    if (cudaFuncSetAttribute(k_cg_pipe, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)DYN_BYTES) != cudaSuccess)
+        return -1;
+    for (const void* f : {(const void*)k_cg<float>, (const void*)k_cg<double>, (const void*)k_cg_pipe}) {
         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, f, CG_THREADS, DYN_BYTES) != cudaSuccess)
             return -1;
         if (per_sm < 1) return -1;
@@ -884,8 +1257,22 @@ void cg_solve(const Launch& L, CgWork& w, const int32_t* nfluid, const float* b,
     cudaMemsetAsync(w.barrier, 0, sizeof(unsigned), L.stream);
     void* args[] = {&a};
     const void* kernel = fp64 ? (const void*)k_cg<double> : (const void*)k_cg<float>;
+    // Arrays with room for PIPE_MIN_CHUNKS chunks per CTA: k_cg_route decides
+    // on the device which of k_cg and k_cg_pipe solves.
+    const bool pipe = !fp64 && w.route && (a.max_chunks + w.grid - 1) / w.grid >= PIPE_MIN_CHUNKS;
+    if (pipe) {
+        k_cg_route<<<1, 1, 0, L.stream>>>(nfluid, a.max_chunks, w.grid, w.route);
+        L.count();
+        a.nfluid = w.route;
+    }
     cudaLaunchCooperativeKernel(kernel, dim3(w.grid), dim3(CG_THREADS), args, DYN_BYTES, L.stream);
     L.count();
+    if (pipe) {
+        a.nfluid = w.route + 1;
+        cudaLaunchCooperativeKernel((const void*)k_cg_pipe, dim3(w.grid), dim3(CG_THREADS), args, DYN_BYTES,
+                                    L.stream);
+        L.count();
+    }
 }
 
 namespace {

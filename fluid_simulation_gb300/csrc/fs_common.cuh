@@ -226,4 +226,11 @@ __device__ __forceinline__ void red_release_add_u32(unsigned* p, unsigned v)
     asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
+// Whether an arrival counter has reached target.  Both advance by the grid's
+// arrivals per barrier and wrap modulo 2^32 together (after about 14 million
+// CG iterations of a 152-CTA grid), and a waiting CTA's counter is never more
+// than a few hundred arrivals from its target, so their signed difference
+// decides.
+__device__ __forceinline__ bool count_reached(unsigned count, unsigned target) { return (int)(count - target) >= 0; }
+
 }  // namespace fs

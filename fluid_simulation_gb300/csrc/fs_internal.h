@@ -185,9 +185,10 @@ struct CgResult
 struct CgWork
 {
     float *x, *r, *z, *p, *q;
-    double* partials;   // tagged partial words, 8 per chunk (zeroed once at allocation)
-    unsigned* barrier;  // reduction sequence number; persists across launches (zeroed at allocation)
+    double* partials;   // chunk partials of the reductions, [2 buffers][2 values][max chunks]
+    unsigned* barrier;  // arrival counter of the grid barrier, cleared before every solve
     CgResult* result;
+    int32_t* route = nullptr;  // 2 ints: the fluid cells k_cg and the pipelined kernel take (large systems)
     int64_t max_cells;
     int grid;           // co-resident CTAs of the cooperative launch
     unsigned missing_arrivals = 0;       // test hook: barrier waits for CTAs that do not exist

@@ -220,9 +220,9 @@ __device__ bool exchange64(const Cg64Args& a, int buf, int nchunks, unsigned& ta
         int ok = 1;
         target += gridDim.x;
         red_release_add_u32(a.barrier, 1u);
-        if (ld_acquire_u32(a.barrier) < target) {
+        if (!count_reached(ld_acquire_u32(a.barrier), target)) {
             const uint64_t t0 = globaltimer_ns();
-            while (ld_acquire_u32(a.barrier) < target) {
+            while (!count_reached(ld_acquire_u32(a.barrier), target)) {
                 if (globaltimer_ns() - t0 > WAIT_LIMIT_NS) {
                     atomicOr(a.status, ST_TIMEOUT);
                     ok = 0;
@@ -456,7 +456,7 @@ void destroy(fs_poisson* p)
     void* ptrs[] = {p->labels, p->fidx, p->cell_of, p->down, p->up, p->scan_tmp, p->nfluid, p->flags, p->rhs, p->b,
                     p->x, p->r, p->part, p->scal, p->cx, p->cr, p->cz, p->cp, p->cq, p->cpart, p->b32, p->status,
                     p->barrier64, p->result64, p->cg.x, p->cg.r, p->cg.z, p->cg.p, p->cg.q, p->cg.partials,
-                    p->cg.barrier, p->cg.result};
+                    p->cg.barrier, p->cg.result, p->cg.route};
     for (void* q : ptrs) cudaFree(q);
     for (auto& e : p->ev)
         if (e) cudaEventDestroy(e);
@@ -660,11 +660,14 @@ FS_API int fs_poisson_create(int size_x, int size_y, float length_x, float lengt
     A((void**)&p->labels, N);
     A((void**)&p->fidx, 4 * N);
     A((void**)&p->cell_of, 4 * N);
-    A((void**)&p->down, 4 * N);
-    A((void**)&p->up, 4 * N);
+    // The FP32 CG kernel copies whole 1024-element chunks of its system
+    // arrays, so they are allocated to the last chunk's end.
+    const size_t NP = (size_t)max_chunks * T;
+    A((void**)&p->down, 4 * NP);
+    A((void**)&p->up, 4 * NP);
     A((void**)&p->scan_tmp, 4 * scan_tmp_ints(n + 2));
     A((void**)&p->nfluid, 4);
-    A((void**)&p->flags, N);
+    A((void**)&p->flags, NP);
     for (double** d : {&p->rhs, &p->b, &p->x, &p->r, &p->cx, &p->cr, &p->cz, &p->cp, &p->cq}) A((void**)d, 8 * N);
     A((void**)&p->part, 8 * max_chunks);
     A((void**)&p->scal, 8 * 4);
@@ -673,10 +676,11 @@ FS_API int fs_poisson_create(int size_x, int size_y, float length_x, float lengt
     A((void**)&p->status, 4);
     A((void**)&p->barrier64, 4);
     A((void**)&p->result64, sizeof(CgResult));
-    for (float** f : {&p->cg.x, &p->cg.r, &p->cg.z, &p->cg.p, &p->cg.q}) A((void**)f, 4 * N);
+    for (float** f : {&p->cg.x, &p->cg.r, &p->cg.z, &p->cg.p, &p->cg.q}) A((void**)f, 4 * NP);
     A((void**)&p->cg.partials, 8 * 4 * max_chunks);
     A((void**)&p->cg.barrier, 4);
     A((void**)&p->cg.result, sizeof(CgResult));
+    A((void**)&p->cg.route, 8);
     for (auto& ev : p->ev)
         if (e == cudaSuccess) e = cudaEventCreate(&ev);
     if (e == cudaSuccess) e = cudaMemsetAsync(p->status, 0, 4, p->stream);

@@ -90,6 +90,32 @@ def test_gpu_matches_restatement_bit_exact(shape, method, inner_precision):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("tol,maxit", [(1e-30, 48), (0.1, 400)])
+def test_gpu_pipelined_streaming_form_matches_restatement(tol, maxit):
+    """A 2048x2048 system (3,976,387 fluid cells: 3884 chunks of 1024, 26 per
+    CTA) is solved by the pipelined streaming kernel (k_cg_pipe), which copies
+    each slot's operands into shared memory ahead of use.  Iterations, the
+    residual and every bit of the solution equal the restatement's, for a solve
+    cut off at maxit and for one that stops on the tolerance (37 iterations)."""
+    import fluid_simulation_gb300 as fsg
+    from fluid_simulation_gb300 import build as fsbuild
+
+    fsbuild.build()
+    n = 2048
+    labels, rhs = scenes.projection_problem(n, seed=13)
+    ps = fsg.PoissonSolver(n, n, float(n), float(n))
+    ps.set_problem(labels, rhs)
+    st = ps.solve(0, tol, maxit)
+    x = ps.solution()
+    ps.close()
+    xo, so = po.poisson_solve(labels, rhs, float(n), float(n), 0, tol, maxit)
+    assert so["n_fluid"] == 3976387
+    assert st["inner_iterations"] == so["inner_iterations"] == (48 if maxit == 48 else 37)
+    assert st["residual"] == so["residual"]
+    assert np.array_equal(x.view(np.uint64), xo.view(np.uint64))
+
+
+@pytest.mark.gpu
 def test_gpu_methods_error_against_fp64_direct_solve():
     """Error of each method against an FP64 direct solve (pinned to zero mean
     per component, where the solution is unique)."""
