@@ -6,12 +6,12 @@
 // fewer iterations than the Jacobi-preconditioned CG (the reference's, kept
 // bit-exact elsewhere) and gives a different, equally converged, solution.
 //
-// Levels halve the grid until it is at most 16 cells a side.  A coarse cell
+// Levels halve the grid until it is at most 8 cells a side.  A coarse cell
 // is AIR if any of its (up to four) children is AIR, else LIQUID if any child
 // is LIQUID, else SOLID; the operator is re-discretised with twice the
 // spacing.  Smoothing is damped Jacobi (omega = 2/3; two sweeps before and
 // after), restriction averages the children's residuals, prolongation copies
-// the coarse correction to the children, and the coarsest level takes 64
+// the coarse correction to the children, and the coarsest level takes 16
 // Jacobi sweeps, so the V-cycle is a fixed symmetric linear operator.  The CG
 // runs on -A (positive) with dot products accumulated in double along a fixed
 // order; its scalars stay on the device and every kernel of an iteration
@@ -36,8 +36,8 @@ namespace {
 
 constexpr int TPB = 256;
 constexpr int RTPB = 512;  // threads of the reducing kernels (grid-stride, two blocks per SM)
-constexpr int COARSE = 16;         // the coarsest level is at most this many cells a side
-constexpr int COARSE_SWEEPS = 64;
+constexpr int COARSE = 8;          // the coarsest level is at most this many cells a side
+constexpr int COARSE_SWEEPS = 16;
 constexpr int FUSE = 64;           // levels at most this many cells a side run in one CTA
 constexpr int FUSED_THREADS = 1024;
 constexpr int MAX_FUSED = 8;
