@@ -32,10 +32,11 @@
 // cells keeps their state in registers and shared memory and stages the p_new
 // values its rows read from other CTAs into a shared-memory halo once per
 // iteration; larger systems stream the state from global memory: in k_cg,
-// or, from PIPE_MIN_CHUNKS chunks per CTA with float dot products, in
-// k_cg_pipe, which copies each slot's operands into shared memory with
-// cp.async several slots ahead of their use (k_cg_route picks one of the two
-// on the device).  Waits are bounded: a CTA that waits longer than about two
+// or, with float dot products, in k_cg_large: from KREG + 1 to KBIG chunks per
+// CTA in the register-resident form with 4-byte rows, from PIPE_MIN_CHUNKS
+// on in a form that copies each slot's operands into shared memory with
+// cp.async several slots ahead of their use (k_cg_route picks k_cg or
+// k_cg_large on the device).  Waits are bounded: a CTA that waits longer than about two
 // seconds sets ST_TIMEOUT and every CTA returns.
 #include <type_traits>
 
@@ -48,6 +49,10 @@ constexpr int CG_THREADS = 1024;
 constexpr int CHUNK = CG_THREADS;
 constexpr int KREG = 8;                   // most chunks per CTA in the register-resident form
 constexpr size_t DYN_BYTES = 204800;      // dynamic shared memory of k_cg: 12 B (16 B above 4 chunks) per cell + halo
+constexpr int KBIG = 12;                  // most chunks per CTA in k_cg_large's register-resident form
+// Dynamic shared memory of k_cg_large: 227 KB per CTA less the static Smem; 12
+// B per resident cell + halo, or the pipeline's stages.
+constexpr size_t LARGE_DYN_BYTES = 215040;
 constexpr int SINGLE_CTA_CHUNKS = 16;       // systems this small run in one CTA
 constexpr int MAX_CHUNKS = 32 * 1024;       // all-read reduction limit (33.5M cells)
 constexpr uint64_t WAIT_LIMIT_NS = 2000000000ull;
@@ -510,7 +515,7 @@ using IntC = std::integral_constant<int, N>;
 // cell's down and up neighbours, gathered once its indices have arrived);
 // phase B keeps PB_STAGES slots of z, p, x, r, q and flags.  The two phases
 // use the same bytes: each starts after the other's copies have all landed.
-constexpr int PIPE_MIN_CHUNKS = 20;  // chunks per CTA from which k_cg_pipe takes the solve
+constexpr int PIPE_MIN_CHUNKS = 20;  // chunks per CTA from which k_cg_large streams through the pipeline
 constexpr int PIPE_WARP_BYTES = (int)(DYN_BYTES / 32);
 constexpr int PA_ENTRY = 4 * 128 + 32 + 64;
 constexpr int PA_STAGES = 6;
@@ -524,7 +529,7 @@ constexpr int PB_AHEAD = PB_STAGES - 1;
 static_assert(PA_STAGES * PA_ENTRY + PG_STAGES * PG_ENTRY <= PIPE_WARP_BYTES, "phase A stages");
 static_assert(PB_STAGES * PB_ENTRY <= PIPE_WARP_BYTES, "phase B stages");
 static_assert(PIPE_WARP_BYTES % 16 == 0 && PA_ENTRY % 16 == 0 && PB_ENTRY % 16 == 0, "16-byte copies");
-// k_cg_pipe's CTAs own at least PIPE_MIN_CHUNKS - 1 slots
+// the pipeline's CTAs own at least PIPE_MIN_CHUNKS - 1 slots
 static_assert(PIPE_MIN_CHUNKS - 1 > PA_AHEAD, "a CTA's last slot is copied after the barrier");
 
 // Phase A's copy groups, in commit order: G1(0..PA_AHEAD-1) (stage 1 of the
@@ -829,8 +834,9 @@ __device__ __forceinline__ void cg_pipe(const CgArgs& a, Smem& sm, unsigned char
 __device__ __forceinline__ int lean_halo_cap(int K, int dyn_bytes)
 {
     const int cells = K * CHUNK;
-    const int cap = (dyn_bytes - (K <= 4 ? 12 : 16) * cells - 8) / 4 - cells - 1;
-    return min(cap, 65535 - cells);
+    const int per_cell = K <= 4 ? 12 : K <= 8 ? 16 : 12;  // nb (8 or 4 bytes), x, r above 4 chunks
+    const int cap = (dyn_bytes - per_cell * cells - 8) / 4 - cells - 1;
+    return min(cap, (K > 8 ? 32767 : 65535) - cells);
 }
 
 template <int K, typename R, class Sync>
@@ -848,10 +854,17 @@ __device__ __forceinline__ bool cg_lean(const CgArgs& a, Smem& sm, unsigned char
     const bool local = ncta == 1 && nchunks <= 32;
     const bool publish = !local;
     constexpr int OWN = K * CHUNK;
+    // Above 8 chunks a row is one 32-bit word: the down and up indices (15
+    // bits each), bit 15 left and bit 31 right neighbour liquid.  Those two
+    // are the adjacent cells of the fluid order: the adjacent entries of pv,
+    // or at the ends of the CTA's range the nearest halo cells.
+    constexpr bool NB4 = K > 8;
     const int hcap = lean_halo_cap(K, a.dyn_bytes);
     float* pv = reinterpret_cast<float*>(dyn);
-    uint2* nb = reinterpret_cast<uint2*>(dyn + (((size_t)(OWN + hcap + 1) * 4 + 7) & ~(size_t)7));
-    float* xs = reinterpret_cast<float*>(nb + OWN);
+    unsigned char* const nbp = dyn + (((size_t)(OWN + hcap + 1) * 4 + 7) & ~(size_t)7);
+    uint2* nb = reinterpret_cast<uint2*>(nbp);
+    unsigned* nb4 = reinterpret_cast<unsigned*>(nbp);
+    float* xs = reinterpret_cast<float*>(nbp + (size_t)OWN * (NB4 ? 4 : 8));
     float* rsm = xs + OWN;
     constexpr bool PREG = K <= 4;  // p of the owned cells in registers (else read back from pv)
     const float* dtab = sm.dtab;
@@ -896,7 +909,8 @@ __device__ __forceinline__ bool cg_lean(const CgArgs& a, Smem& sm, unsigned char
 
     // ---- initialisation: x = 0, r = b, z = M^-1 r; bb = r.r, rz = r.z
     float rreg[PREG ? K : 1], zq[K], pn[PREG ? K : 1];
-    unsigned cnts = 0;  // non-solid neighbour count of slot s in bits 4s..4s+2
+    using Cnt = std::conditional_t<(K > 8), unsigned long long, unsigned>;
+    Cnt cnts = 0;  // non-solid neighbour count of slot s in bits 4s..4s+2
     if (tid == 0) pv[zero_i] = 0.0f;
 #pragma unroll
     for (int s = 0; s < K; ++s) {
@@ -918,12 +932,16 @@ __device__ __forceinline__ bool cg_lean(const CgArgs& a, Smem& sm, unsigned char
                 zq[s] = z;
                 xs[s * CHUNK + tid] = 0.0f;
                 if constexpr (!PREG) pv[s * CHUNK + tid] = 0.0f;
-                cnts |= (fl >> 2) << (4 * s);
+                cnts |= (Cnt)(fl >> 2) << (4 * s);
                 const unsigned i_dn = slot_of(a.down[e]);
-                const unsigned i_l = (fl & 1u) ? slot_of(e - 1) : zero_i;
-                const unsigned i_r = (fl & 2u) ? slot_of(e + 1) : zero_i;
                 const unsigned i_up = slot_of(a.up[e]);
-                nb[s * CHUNK + tid] = make_uint2(i_dn | (i_l << 16), i_r | (i_up << 16));
+                if constexpr (NB4) {
+                    nb4[s * CHUNK + tid] = i_dn | (i_up << 16) | ((fl & 1u) << 15) | ((fl & 2u) << 30);
+                } else {
+                    const unsigned i_l = (fl & 1u) ? slot_of(e - 1) : zero_i;
+                    const unsigned i_r = (fl & 2u) ? slot_of(e + 1) : zero_i;
+                    nb[s * CHUNK + tid] = make_uint2(i_dn | (i_l << 16), i_r | (i_up << 16));
+                }
             }
             level1<R, 2>(v, s, sm);
         }
@@ -993,14 +1011,30 @@ __device__ __forceinline__ bool cg_lean(const CgArgs& a, Smem& sm, unsigned char
             if (s < kb) {
                 R v[1] = {R(0)};
                 if ((c0 + s) * CHUNK + tid < nf) {
-                    const uint2 w = nb[s * CHUNK + tid];
                     const float ps = PREG ? pn[s] : pv[s * CHUNK + tid];
                     float acc = 0.0f;
-                    acc = fadd(acc, fmul(off, pv[w.x & 0xffffu]));
-                    acc = fadd(acc, fmul(off, pv[w.x >> 16]));
-                    acc = fadd(acc, fmul(dtab[(cnts >> (4 * s)) & 7u], ps));
-                    acc = fadd(acc, fmul(off, pv[w.y & 0xffffu]));
-                    acc = fadd(acc, fmul(off, pv[w.y >> 16]));
+                    if constexpr (NB4) {
+                        const unsigned w = nb4[s * CHUNK + tid];
+                        const int l = s * CHUNK + tid;  // = e - e0
+                        const unsigned il = !(w & 0x8000u) ? zero_i
+                                            : l > 0        ? (unsigned)(l - 1)
+                                                           : (unsigned)(OWN + nbelow - 1);
+                        const unsigned ir = !(w & 0x80000000u) ? zero_i
+                                            : l + 1 < e1 - e0  ? (unsigned)(l + 1)
+                                                               : (unsigned)(OWN + nbelow);
+                        acc = fadd(acc, fmul(off, pv[w & 0x7fffu]));
+                        acc = fadd(acc, fmul(off, pv[il]));
+                        acc = fadd(acc, fmul(dtab[(unsigned)(cnts >> (4 * s)) & 7u], ps));
+                        acc = fadd(acc, fmul(off, pv[ir]));
+                        acc = fadd(acc, fmul(off, pv[(w >> 16) & 0x7fffu]));
+                    } else {
+                        const uint2 w = nb[s * CHUNK + tid];
+                        acc = fadd(acc, fmul(off, pv[w.x & 0xffffu]));
+                        acc = fadd(acc, fmul(off, pv[w.x >> 16]));
+                        acc = fadd(acc, fmul(dtab[(cnts >> (4 * s)) & 7u], ps));
+                        acc = fadd(acc, fmul(off, pv[w.y & 0xffffu]));
+                        acc = fadd(acc, fmul(off, pv[w.y >> 16]));
+                    }
                     v[0] = Ar<R>::prod(ps, acc);
                     zq[s] = acc;
                 }
@@ -1030,7 +1064,7 @@ __device__ __forceinline__ bool cg_lean(const CgArgs& a, Smem& sm, unsigned char
                     float& rr_ = PREG ? rreg[s] : rsm[l];
                     const float rn = fsub(rr_, fmul(alpha, zq[s]));
                     rr_ = rn;
-                    const float z = fmul(itab[(cnts >> (4 * s)) & 7u], rn);
+                    const float z = fmul(itab[(unsigned)(cnts >> (4 * s)) & 7u], rn);
                     zq[s] = z;
                     if (publish) {
                         __stcg(&a.z[e], z);
@@ -1071,22 +1105,32 @@ __device__ __forceinline__ bool cg_lean(const CgArgs& a, Smem& sm, unsigned char
     return true;
 }
 
-// Splits a solve between k_cg and k_cg_pipe: route[0] = the fluid cells k_cg
-// solves, route[1] = those k_cg_pipe solves; one of the two is 0.  k_cg_pipe
-// takes the large systems with enough chunks per CTA (and that k_cg accepts).
+// Whether k_cg_large solves a system of nchunks chunks on `grid` CTAs: from
+// KREG + 1 to KBIG chunks per CTA (the register-resident form with 4-byte
+// rows) and from PIPE_MIN_CHUNKS on (the pipelined streaming form).
+__device__ __forceinline__ bool large_takes(int nchunks, int grid)
+{
+    const int per_cta = (nchunks + grid - 1) / grid;
+    return nchunks > SINGLE_CTA_CHUNKS && ((per_cta > KREG && per_cta <= KBIG) || per_cta >= PIPE_MIN_CHUNKS);
+}
+
+// Splits a solve between k_cg and k_cg_large: route[0] = the fluid cells k_cg
+// solves, route[1] = those k_cg_large solves; one of the two is 0 (k_cg keeps
+// the systems it rejects, to report them).
 __global__ void k_cg_route(const int32_t* __restrict__ nfluid, int max_chunks, int grid, int32_t* __restrict__ route)
 {
     const int nf = *nfluid;
     const int nchunks = (nf + CHUNK - 1) / CHUNK;
-    const bool pipe = nchunks <= max_chunks && nchunks <= MAX_CHUNKS && nchunks > SINGLE_CTA_CHUNKS &&
-                      (nchunks + grid - 1) / grid >= PIPE_MIN_CHUNKS;
-    route[0] = pipe ? 0 : nf;
-    route[1] = pipe ? nf : 0;
+    const bool large = nchunks <= max_chunks && nchunks <= MAX_CHUNKS && large_takes(nchunks, grid);
+    route[0] = large ? 0 : nf;
+    route[1] = large ? nf : 0;
 }
 
-// Large systems with FP32 dot products: the pipelined streaming form, on the
-// system k_cg_route gave it (none: return without a result; k_cg wrote it).
-__global__ void __launch_bounds__(CG_THREADS, 1) k_cg_pipe(CgArgs a)
+// Large systems with FP32 dot products, on the system k_cg_route gave it
+// (none: return without a result; k_cg wrote it): up to KBIG chunks per CTA
+// in registers and shared memory, from PIPE_MIN_CHUNKS on streamed through
+// the cp.async pipeline.
+__global__ void __launch_bounds__(CG_THREADS, 1) k_cg_large(CgArgs a)
 {
     __shared__ Smem sm;
     extern __shared__ __align__(16) unsigned char dyn[];
@@ -1102,7 +1146,11 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg_pipe(CgArgs a)
     }
     __syncthreads();
     GridSync sync{true, 0u, active};
-    cg_pipe<float>(a, sm, dyn, nf, nchunks, sync);
+    if (per_cta <= KBIG) {
+        if (!cg_lean<KBIG, float>(a, sm, dyn, nf, nchunks, sync)) cg_stream<float>(a, sm, nf, nchunks, sync);
+    } else {
+        cg_pipe<float>(a, sm, dyn, nf, nchunks, sync);
+    }
 }
 
 template <typename R>
@@ -1212,13 +1260,18 @@ int cg_prepare(CgWork& w, int device)
         cudaFuncSetAttribute(k_cg<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)DYN_BYTES) !=
             cudaSuccess)
         return -1;
-    if (cudaFuncSetAttribute(k_cg_pipe, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)DYN_BYTES) != cudaSuccess)
+    if (cudaFuncSetAttribute(k_cg_large, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)LARGE_DYN_BYTES) !=
+        cudaSuccess)
         return -1;
-    for (const void* f : {(const void*)k_cg<float>, (const void*)k_cg<double>, (const void*)k_cg_pipe}) {
+    for (const void* f : {(const void*)k_cg<float>, (const void*)k_cg<double>}) {
         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, f, CG_THREADS, DYN_BYTES) != cudaSuccess)
             return -1;
         if (per_sm < 1) return -1;
     }
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cg_large, CG_THREADS, LARGE_DYN_BYTES) !=
+            cudaSuccess ||
+        per_sm < 1)
+        return -1;
     w.grid = sms;  // one CTA per SM: fewer barrier arrivals
     return 0;
 }
@@ -1257,20 +1310,21 @@ void cg_solve(const Launch& L, CgWork& w, const int32_t* nfluid, const float* b,
     cudaMemsetAsync(w.barrier, 0, sizeof(unsigned), L.stream);
     void* args[] = {&a};
     const void* kernel = fp64 ? (const void*)k_cg<double> : (const void*)k_cg<float>;
-    // Arrays with room for PIPE_MIN_CHUNKS chunks per CTA: k_cg_route decides
-    // on the device which of k_cg and k_cg_pipe solves.
-    const bool pipe = !fp64 && w.route && (a.max_chunks + w.grid - 1) / w.grid >= PIPE_MIN_CHUNKS;
-    if (pipe) {
+    // Arrays with room for more than KREG chunks per CTA: k_cg_route decides
+    // on the device which of k_cg and k_cg_large solves.
+    const bool large = !fp64 && w.route && (a.max_chunks + w.grid - 1) / w.grid > KREG;
+    if (large) {
         k_cg_route<<<1, 1, 0, L.stream>>>(nfluid, a.max_chunks, w.grid, w.route);
         L.count();
         a.nfluid = w.route;
     }
     cudaLaunchCooperativeKernel(kernel, dim3(w.grid), dim3(CG_THREADS), args, DYN_BYTES, L.stream);
     L.count();
-    if (pipe) {
+    if (large) {
         a.nfluid = w.route + 1;
-        cudaLaunchCooperativeKernel((const void*)k_cg_pipe, dim3(w.grid), dim3(CG_THREADS), args, DYN_BYTES,
-                                    L.stream);
+        a.dyn_bytes = (int)LARGE_DYN_BYTES;
+        cudaLaunchCooperativeKernel((const void*)k_cg_large, dim3(w.grid), dim3(CG_THREADS), args,
+                                    LARGE_DYN_BYTES, L.stream);
         L.count();
     }
 }

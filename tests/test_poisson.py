@@ -89,28 +89,60 @@ def test_gpu_matches_restatement_bit_exact(shape, method, inner_precision):
     assert np.array_equal(x.view(np.uint64), xo.view(np.uint64))
 
 
+def _narrow_then_wide(nx=5000, ny=500, narrow_rows=200, narrow_width=1000, seed=23):
+    """A closed box whose lower rows are narrow_width cells wide and whose
+    upper rows span nx, 2% random solids, zero-mean right-hand side."""
+    rng = np.random.default_rng(seed)
+    labels = np.zeros((ny, nx), np.uint8)
+    labels[:, 0] = labels[:, -1] = 2
+    labels[0, :] = labels[-1, :] = 2
+    labels[1:narrow_rows, narrow_width:] = 2
+    labels[rng.random((ny, nx)) < 0.02] = 2
+    rhs = np.where(labels == 0, rng.standard_normal(labels.shape), 0.0)
+    rhs[labels == 0] -= rhs[labels == 0].mean()
+    return labels, rhs
+
+
+# (case, problem, fluid cells, chunks of 1024 per CTA on 152 SMs, tol, maxit, iterations)
+_LARGE_CASES = [
+    # 10 chunks per CTA: every CTA keeps its cells in registers and shared memory (12-chunk form)
+    ("resident12", lambda: scenes.projection_problem(1280, seed=17), 1552248, 10, 1e-30, 48, 48),
+    # 11 chunks per CTA: the CTAs of the 1000-wide rows are resident; those of the 5000-wide rows
+    # read halos larger than their shared memory and stream instead, in the same solve
+    ("resident12_and_streaming", _narrow_then_wide, 1659364, 11, 1e-30, 48, 48),
+    # 26 chunks per CTA: the pipelined streaming form, cut off at maxit and stopping on the tolerance
+    ("pipelined", lambda: scenes.projection_problem(2048, seed=13), 3976387, 26, 1e-30, 48, 48),
+    ("pipelined_tolerance", lambda: scenes.projection_problem(2048, seed=13), 3976387, 26, 0.1, 400, 37),
+]
+
+
 @pytest.mark.gpu
-@pytest.mark.parametrize("tol,maxit", [(1e-30, 48), (0.1, 400)])
-def test_gpu_pipelined_streaming_form_matches_restatement(tol, maxit):
-    """A 2048x2048 system (3,976,387 fluid cells: 3884 chunks of 1024, 26 per
-    CTA) is solved by the pipelined streaming kernel (k_cg_pipe), which copies
-    each slot's operands into shared memory ahead of use.  Iterations, the
-    residual and every bit of the solution equal the restatement's, for a solve
-    cut off at maxit and for one that stops on the tolerance (37 iterations)."""
+@pytest.mark.parametrize("case,make,n_fluid,per_cta,tol,maxit,iters", _LARGE_CASES, ids=[c[0] for c in _LARGE_CASES])
+def test_gpu_large_system_forms_match_restatement(case, make, n_fluid, per_cta, tol, maxit, iters):
+    """Systems of more than 8 chunks of 1024 cells per CTA with float dot
+    products are solved by k_cg_large: up to 12 chunks per CTA in the
+    register-resident form with 4-byte rows (a CTA whose halo does not fit
+    streams instead), from 20 on through the cp.async pipeline.  Iterations,
+    the residual and every bit of the solution equal the restatement's."""
+    import torch
+
     import fluid_simulation_gb300 as fsg
     from fluid_simulation_gb300 import build as fsbuild
 
     fsbuild.build()
-    n = 2048
-    labels, rhs = scenes.projection_problem(n, seed=13)
-    ps = fsg.PoissonSolver(n, n, float(n), float(n))
+    labels, rhs = make()
+    ny, nx = labels.shape
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    assert int((labels == 0).sum()) == n_fluid
+    if sms == 152:
+        assert (-(-n_fluid // 1024) + sms - 1) // sms == per_cta
+    ps = fsg.PoissonSolver(nx, ny, float(nx), float(ny))
     ps.set_problem(labels, rhs)
     st = ps.solve(0, tol, maxit)
     x = ps.solution()
     ps.close()
-    xo, so = po.poisson_solve(labels, rhs, float(n), float(n), 0, tol, maxit)
-    assert so["n_fluid"] == 3976387
-    assert st["inner_iterations"] == so["inner_iterations"] == (48 if maxit == 48 else 37)
+    xo, so = po.poisson_solve(labels, rhs, float(nx), float(ny), 0, tol, maxit)
+    assert st["inner_iterations"] == so["inner_iterations"] == iters
     assert st["residual"] == so["residual"]
     assert np.array_equal(x.view(np.uint64), xo.view(np.uint64))
 
