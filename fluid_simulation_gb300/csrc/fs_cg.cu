@@ -31,13 +31,14 @@
 // with the same float operations.  A CTA that owns at most KREG chunks of 1024
 // cells keeps their state in registers and shared memory and stages the p_new
 // values its rows read from other CTAs into a shared-memory halo once per
-// iteration; larger systems stream the state from global memory: in k_cg,
-// or, with float dot products, in k_cg_large: from KREG + 1 to KBIG chunks per
-// CTA in the register-resident form with 4-byte rows, from PIPE_MIN_CHUNKS
-// on in a form that copies each slot's operands into shared memory with
-// cp.async several slots ahead of their use (k_cg_route picks k_cg or
-// k_cg_large on the device).  Waits are bounded: a CTA that waits longer than about two
-// seconds sets ST_TIMEOUT and every CTA returns.
+// iteration; larger systems stream the state from global memory.  With float
+// dot products, systems of more than KREG chunks per CTA run in k_cg_large
+// instead (k_cg_route picks the kernel on the device): up to KBIG chunks per
+// CTA in the register-resident form with 4-byte rows, from PIPE_MIN_CHUNKS on
+// in a streaming form that copies each slot's operands into shared memory
+// with cp.async several slots ahead of their use, in between streaming as in
+// k_cg.  Waits are bounded: a CTA that waits longer than about two seconds
+// sets ST_TIMEOUT and every CTA returns.
 #include <type_traits>
 
 #include "fs_internal.h"
@@ -50,8 +51,8 @@ constexpr int CHUNK = CG_THREADS;
 constexpr int KREG = 8;                   // most chunks per CTA in the register-resident form
 constexpr size_t DYN_BYTES = 204800;      // dynamic shared memory of k_cg: 12 B (16 B above 4 chunks) per cell + halo
 constexpr int KBIG = 12;                  // most chunks per CTA in k_cg_large's register-resident form
-// Dynamic shared memory of k_cg_large: 227 KB per CTA less the static Smem; 12
-// B per resident cell + halo, or the pipeline's stages.
+// Dynamic shared memory of k_cg_large: 227 KB per CTA less the static Smem;
+// 16 B per resident cell (p, row, x, r) + halo, or the pipeline's stages.
 constexpr size_t LARGE_DYN_BYTES = 215040;
 constexpr int SINGLE_CTA_CHUNKS = 16;       // systems this small run in one CTA
 constexpr int MAX_CHUNKS = 32 * 1024;       // all-read reduction limit (33.5M cells)
