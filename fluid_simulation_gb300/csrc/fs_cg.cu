@@ -42,6 +42,7 @@
 #include <type_traits>
 
 #include "fs_internal.h"
+#include "fs_pipeline.h"
 
 namespace fs {
 namespace {
@@ -507,45 +508,22 @@ __device__ __forceinline__ void cp_wait()
 template <int N>
 using IntC = std::integral_constant<int, N>;
 
-// Shared-memory layout of the pipelined streaming form.  Every warp owns a
-// private 6400-byte region and copies only the 32 cells it computes (plus
-// the 4-cell pieces around them that its edge lanes read), so no copy ever
-// needs a CTA barrier.  Phase A keeps PA_STAGES slots of stage 1 (z, p, down,
-// up: 128 bytes each; flags: 32; the z and p of the 4 cells before and after
-// the warp's cells: 64) and PG_STAGES slots of stage 2 (z and p of each
-// cell's down and up neighbours, gathered once its indices have arrived);
-// phase B keeps PB_STAGES slots of z, p, x, r, q and flags.  The two phases
-// use the same bytes: each starts after the other's copies have all landed.
-constexpr int PIPE_MIN_CHUNKS = 20;  // chunks per CTA from which k_cg_large streams through the pipeline
-constexpr int PIPE_WARP_BYTES = (int)(DYN_BYTES / 32);
-constexpr int PA_ENTRY = 4 * 128 + 32 + 64;
-constexpr int PA_STAGES = 6;
-constexpr int PA_AHEAD = PA_STAGES - 1;
-constexpr int PG_ENTRY = 4 * 128;
-constexpr int PG_STAGES = 3;
-constexpr int PG_AHEAD = PG_STAGES - 1;
-constexpr int PB_ENTRY = 5 * 128 + 32;
-constexpr int PB_STAGES = 9;
-constexpr int PB_AHEAD = PB_STAGES - 1;
-static_assert(PA_STAGES * PA_ENTRY + PG_STAGES * PG_ENTRY <= PIPE_WARP_BYTES, "phase A stages");
-static_assert(PB_STAGES * PB_ENTRY <= PIPE_WARP_BYTES, "phase B stages");
-static_assert(PIPE_WARP_BYTES % 16 == 0 && PA_ENTRY % 16 == 0 && PB_ENTRY % 16 == 0, "16-byte copies");
-// the pipeline's CTAs own at least PIPE_MIN_CHUNKS - 1 slots
-static_assert(PIPE_MIN_CHUNKS - 1 > PA_AHEAD, "a CTA's last slot is copied after the barrier");
-
-// Phase A's copy groups, in commit order: G1(0..PA_AHEAD-1) (stage 1 of the
-// first slots, before the barrier), G2(0..PG_AHEAD-1) (their gathers), then
-// per slot k: G2(k + PG_AHEAD), G1(k + PA_AHEAD).  Groups committed after
-// G1(k + PG_AHEAD) when slot k starts, and after G2(k) once slot k's own
-// groups are committed:
-__host__ __device__ constexpr int pa_wait1(int k)
-{
-    return k + PG_AHEAD <= PA_AHEAD - 1 ? PA_AHEAD - 1 + k : 2 * (PA_AHEAD - PG_AHEAD - 1);
-}
-__host__ __device__ constexpr int pa_wait2(int k) { return k < PG_AHEAD ? PG_AHEAD + 1 + k : 2 * PG_AHEAD + 1; }
-constexpr int PA_PEEL = 3;  // slots before both counts settle
-static_assert(PA_PEEL >= PA_AHEAD - PG_AHEAD && PA_PEEL >= PG_AHEAD, "steady waits from slot PA_PEEL on");
-static_assert(PIPE_MIN_CHUNKS - 1 > PA_PEEL, "the peeled slots exist");
+// The pipelined streaming form's copy schedule (fs_pipeline.h).
+constexpr int PIPE_MIN_CHUNKS = pipe::MIN_CHUNKS;
+constexpr int PIPE_WARP_BYTES = pipe::WARP_BYTES;
+using pipe::PA_AHEAD;
+using pipe::PA_ENTRY;
+using pipe::PA_PEEL;
+using pipe::PA_STAGES;
+using pipe::PB_AHEAD;
+using pipe::PB_ENTRY;
+using pipe::PB_STAGES;
+using pipe::PG_AHEAD;
+using pipe::PG_ENTRY;
+using pipe::PG_STAGES;
+using pipe::pa_wait1;
+using pipe::pa_wait2;
+static_assert(32 * PIPE_WARP_BYTES <= (int)LARGE_DYN_BYTES, "the warps' regions fit k_cg_large's shared memory");
 
 // The streaming solve (state in global memory) with the cells' operands
 // copied into shared memory several slots ahead of their use.  The
@@ -697,7 +675,7 @@ __device__ __forceinline__ void cg_pipe(const CgArgs& a, Smem& sm, unsigned char
         // entry (og_prev).
         fix_edge();
         for (int j = 0; j < PG_AHEAD; ++j) {
-            cp_wait<PA_AHEAD - 1>();  // G1(j)
+            cp_wait<pipe::PA_WAIT_PROLOGUE>();  // G1(j)
             __syncwarp();
             issue_gather(slot_base(j), wb + j * PA_ENTRY, sgring + j * PG_ENTRY);
             cp_commit();
@@ -766,7 +744,7 @@ __device__ __forceinline__ void cg_pipe(const CgArgs& a, Smem& sm, unsigned char
         for (int k = 0; k < kb; ++k) {
             issue_b(slot_base(k + PB_AHEAD), swb + ob_prev);
             cp_commit();
-            cp_wait<PB_AHEAD>();  // GB(k)
+            cp_wait<pipe::PB_WAIT>();  // GB(k)
             __syncwarp();
             const float* en = reinterpret_cast<const float*>(wb + ob);
             const unsigned char* efl = wb + ob + 640;
