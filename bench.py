@@ -25,7 +25,8 @@ multigrid form (the same 1024^2 workload with a multigrid-preconditioned
 pressure solve, not the reference's solver) and the mixed-precision form (the
 4096^2 pressure projection to relative residual 1e-10 by FP64 iterative
 refinement around float multigrid or Jacobi CG corrections, against an
-FP64-only CG).
+FP64-only CG), and the large step (the plain step on the dam break at twice
+the side, whose pressure system the CG keeps on chip in its 12-chunk form).
 --no-forms skips them; --only-form measures one of them alone.
 """
 from __future__ import annotations
@@ -68,7 +69,7 @@ def parse():
                     help="CG iteration cap of each projection solve (a small cap makes a short profiling case)")
     ap.add_argument("--batch-plan", type=int, choices=[1, 2, 4, 8], default=None,
                     help="batched form: CG chunks per CTA instead of the autotuner's choice")
-    ap.add_argument("--only-form", choices=["batched", "mixed_precision", "multigrid"], default=None,
+    ap.add_argument("--only-form", choices=["batched", "mixed_precision", "multigrid", "large_step"], default=None,
                     help="measure one form alone (profiling runs) and print its JSON object")
     return ap.parse_args()
 
@@ -385,6 +386,44 @@ def measure_multigrid(args, local_rank, plain_value, flush):
             "cg_iterations_mean": float(np.mean(its))}
 
 
+def measure_large_step(args, local_rank, flush):
+    """The plain step (the reference's algorithm, bit-exact) on the dam break
+    at twice the side, 2048^2: about 1.72M fluid cells, 12 chunks of 1024
+    cells per CTA, a system the CG keeps on chip in k_cg_large.  Device time
+    per step, and the CG's share from the library's per-phase events."""
+    import torch
+
+    import fluid_simulation_gb300 as fsg
+
+    sc = workload(2 * args.size)
+    sim = fsg.FluidSim.from_scene(sc, device=local_rank)
+    for _ in range(2):
+        sim.step(fsg.STEP_PICFLIP, sc.dt)
+    sim.synchronize()
+    sim.set_timing(True)
+    stream = torch.cuda.ExternalStream(sim.stream(), device=local_rank)
+    ms, cg_ms, its, nf = [], [], [], 0
+    for _ in range(3):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+        sim.step(fsg.STEP_PICFLIP, sc.dt)
+        e1.record(stream)
+        st = sim.stats()
+        ms.append(e0.elapsed_time(e1))
+        cg_ms.append(st["ms_phase"]["cg"])
+        its.append(st["cg_iterations"])
+        nf = st["n_fluid"]
+    sim.set_timing(False)
+    t = sum(ms) / 1000.0
+    return {"workload": "dam break %dx%d (the plain workload at twice the side), stepPICFLIP, Jacobi-PCG 1e-5"
+            % (sc.size_x, sc.size_y), "value": sc.cells * len(ms) / t, "unit": UNIT,
+            "ms_per_step": 1000.0 * t / len(ms), "fluid_cells": int(nf), "cg_iterations_mean": float(np.mean(its)),
+            "cg_us_per_iteration": 1000.0 * sum(cg_ms) / sum(its)}
+
+
 def run_gpu(args, rank, world, local_rank):
     import torch
 
@@ -405,6 +444,8 @@ def run_gpu(args, rank, world, local_rank):
                 out = measure_batched(args, local_rank, float("nan"), flush)
             elif args.only_form == "multigrid":
                 out = measure_multigrid(args, local_rank, float("nan"), flush)
+            elif args.only_form == "large_step":
+                out = measure_large_step(args, local_rank, flush)
             else:
                 out = measure_projection(args, local_rank)
             print(json.dumps({"form": args.only_form, **out}), flush=True)
@@ -483,6 +524,7 @@ def run_gpu(args, rank, world, local_rank):
     if world == 1 and not args.no_forms:
         forms = {"batched": measure_batched(args, local_rank, value, flush),
                  "multigrid": measure_multigrid(args, local_rank, value, flush),
+                 "large_step": measure_large_step(args, local_rank, flush),
                  "mixed_precision": measure_projection(args, local_rank)}
     # roofline of the dominant kernel (the CG)
     peak, peak_kind = peaks()
