@@ -400,6 +400,41 @@ def test_cg_barrier_timeout_is_reported_and_the_handle_recovers():
         assert_same(g.state(), o.state(), where="after recovery, step %d" % k)
 
 
+def test_large_system_cg_barrier_timeout_recovers():
+    """The same failure path in the large-system kernel: a 1280^2 box of fluid
+    (about 1.6M fluid cells, 11 chunks of 1024 per CTA on 152 SMs) solves in
+    k_cg_large's 12-chunk form.  With the barrier waiting for a CTA that does
+    not exist every CTA gives up after 50 ms (and waits for its own copies in
+    flight), the host reads FS_ERR_TIMEOUT, and the handle, restored from a
+    snapshot, steps bit-exact with a handle that never failed."""
+    import torch
+
+    n = 1280
+    parts = scenes.block_particles(n, n, float(n), float(n), 1, n - 1, 1, n - 20, 4, 11)
+    sims = []
+    for _ in range(2):
+        s = fsg.FluidSim(n, n, float(n), float(n), 0.005, 0.05, cg_tolerance=1e-5, cg_max_iterations=60)
+        s.set_particles(parts)
+        s.step(fsg.STEP_PICFLIP, 0.005)
+        sims.append(s)
+    g, ref = sims
+    nf = g.stats()["n_fluid"]
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    assert 8 * sms * 1024 < nf <= 12 * sms * 1024  # the 12-chunk form of k_cg_large
+    snap = g.snapshot()
+    assert g.lib.fs_debug_set_cg_barrier_fault(g.h, 1, 0.05) == 0
+    g.step(fsg.STEP_PICFLIP, 0.005)
+    with pytest.raises(fsg.FsError) as e:
+        g.synchronize()
+    assert e.value.code == 4
+    assert g.lib.fs_debug_set_cg_barrier_fault(g.h, 0, 2.0) == 0
+    g.restore(snap)
+    for k in range(2):
+        g.step(fsg.STEP_PICFLIP, 0.005)
+        ref.step(fsg.STEP_PICFLIP, 0.005)
+        assert_same(g.state(), ref.state(), where="after recovery, step %d" % k)
+
+
 @pytest.mark.parametrize("shape", [(64, 64), (40, 64)])
 def test_level_set_path_matches_oracle(shape):
     """FluidDomain::advectLevelSet and classifyCells(LevelSet&) on the device,
