@@ -193,8 +193,9 @@ def test_benchmark_workload_three_steps_bit_exact():
 
 @pytest.mark.parametrize("precision", [fsg.CG_FLOAT, fsg.CG_DOUBLE])
 def test_streaming_cg_matches_oracle(precision):
-    """A fluid region too large for the register-resident CG (more than
-    8 x 1024 fluid cells per CTA): the streaming variant of the same kernel."""
+    """A fluid region too large for k_cg's register-resident CG (11 chunks of
+    1024 fluid cells per CTA): with float dot products k_cg_large's 12-chunk
+    form, with double dot products k_cg's streaming form."""
     n = 1280
     sc = scenes.Scene(n, n, float(n), float(n), 0.01, 0.05, 0.01,
                       scenes.block_particles(n, n, float(n), float(n), 1, n - 1, 1, n - 1, 1, 11),
