@@ -395,6 +395,9 @@ def measure_large_step(args, local_rank, flush):
 
     import fluid_simulation_gb300 as fsg
 
+    if 2 * args.size > 4096:
+        return {"skipped": "a handle holds at most 4096x4096 cells; --size %d doubles to %d" % (args.size,
+                                                                                               2 * args.size)}
     sc = workload(2 * args.size)
     sim = fsg.FluidSim.from_scene(sc, device=local_rank)
     for _ in range(2):
