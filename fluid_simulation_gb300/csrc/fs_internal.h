@@ -68,8 +68,10 @@ struct Domain
 
 // ---- scan (fs_scan.cu) ----------------------------------------------------
 // Exclusive prefix sum of n int32 values into out[0..n]; out[n] = total.
-// tmp must hold scan_tmp_ints(n) ints.
-size_t scan_tmp_ints(int64_t n);
+// tmp must hold scan_tmp_ints(n) ints: one partial sum per tile of
+// SCAN_TILE_ITEMS items, plus one.
+constexpr int64_t SCAN_TILE_ITEMS = 4096;
+constexpr size_t scan_tmp_ints(int64_t n) { return (size_t)((n + SCAN_TILE_ITEMS - 1) / SCAN_TILE_ITEMS) + 1; }
 void scan_exclusive_i32(const Launch& L, const int32_t* in, int32_t* out, int64_t n, int32_t* tmp);
 // Fluid indexing (FluidSolver.cpp:329-346): fidx[c] = running index of LIQUID
 // cells in j-major order or -1; cell_of[k] = c; *nfluid = count.

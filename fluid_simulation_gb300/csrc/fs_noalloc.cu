@@ -15,10 +15,16 @@
 // holds until the process exits.  Host code cannot use the array's name as
 // a device address, so the first call on each device looks the address up
 // with cudaGetSymbolAddress (with that device current) and caches it; make
-// that first call before any stream capture.  Every call shares the array
-// and finds the previous call's contents in it: the parts that must start at
-// zero are cleared by each call, and calls whose work overlaps on the GPU
-// (different streams, different threads) race on the array.
+// that first call before any stream capture.  The cached address belongs to
+// the device's context at that time: after cudaDeviceReset the process must
+// not call this entry point on that device again.  Every call shares the
+// array and finds the previous call's contents in it: the parts that must
+// start at zero are cleared by each call, and calls whose work overlaps on
+// the GPU (different streams, different threads) race on the array.
+//
+// Every call synchronises its stream and reads the device status word before
+// it returns, so a device-side failure is reported by the call that met it
+// and never left for a later call to clear.
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -53,7 +59,8 @@ constexpr size_t OFF_P = OFF_Z + up_to(4 * N);
 constexpr size_t OFF_Q = OFF_P + up_to(4 * N);
 constexpr size_t OFF_PARTIALS = OFF_Q + up_to(4 * N);
 constexpr size_t OFF_SCAN = OFF_PARTIALS + up_to(8 * 8 * (size_t)NOALLOC_MAX_CHUNKS);
-constexpr size_t SCAN_INTS = 64;  // >= scan_tmp_ints(NOALLOC_MAX_CELLS + 2)
+constexpr size_t SCAN_INTS = 64;
+static_assert(scan_tmp_ints(NOALLOC_MAX_CELLS + 2) <= SCAN_INTS, "the scan's tile sums fit their scratch");
 constexpr size_t OFF_NFLUID = OFF_SCAN + up_to(4 * SCAN_INTS);
 constexpr size_t OFF_STATUS = OFF_NFLUID + ALIGN;
 constexpr size_t OFF_WARN = OFF_STATUS + ALIGN;
@@ -173,17 +180,17 @@ extern "C" FS_API int fs_pressure_solve_noalloc(int size_x, int size_y, float le
     pressure_to_grid(L, d, fidx, nfluid, w.x, pressure);
     e = cudaGetLastError();
     if (e != cudaSuccess) return fail(FS_ERR_CUDA, std::string("launch: ") + cudaGetErrorString(e));
-    if (cg_iterations || cg_residual) {
-        CgResult res{};
-        unsigned st = 0;
-        cudaMemcpyAsync(&res, w.result, sizeof(res), cudaMemcpyDeviceToHost, L.stream);
-        cudaMemcpyAsync(&st, status, sizeof(st), cudaMemcpyDeviceToHost, L.stream);
-        e = cudaStreamSynchronize(L.stream);
-        if (e != cudaSuccess) return fail(FS_ERR_CUDA, std::string("synchronize: ") + cudaGetErrorString(e));
-        if (st & ST_TIMEOUT) return fail(FS_ERR_TIMEOUT, "a device-side wait of the CG kernel timed out");
-        if (st & ST_TOO_LARGE) return fail(FS_ERR_TOO_LARGE, "too many fluid cells");
-        if (cg_iterations) *cg_iterations = res.iterations;
-        if (cg_residual) *cg_residual = res.bb > 0 ? std::sqrt(res.rr / res.bb) : 0.0;
-    }
+    // The status is read on every call: the next call clears it.
+    CgResult res{};
+    unsigned st = 0;
+    cudaMemcpyAsync(&res, w.result, sizeof(res), cudaMemcpyDeviceToHost, L.stream);
+    cudaMemcpyAsync(&st, status, sizeof(st), cudaMemcpyDeviceToHost, L.stream);
+    e = cudaStreamSynchronize(L.stream);
+    if (e != cudaSuccess) return fail(FS_ERR_CUDA, std::string("synchronize: ") + cudaGetErrorString(e));
+    if (st & ST_TIMEOUT) return fail(FS_ERR_TIMEOUT, "a device-side wait of the CG kernel timed out");
+    if (st & ST_TOO_LARGE) return fail(FS_ERR_TOO_LARGE, "too many fluid cells");
+    if (st) return fail(FS_ERR_INTERNAL, "internal consistency check failed on the device");
+    if (cg_iterations) *cg_iterations = res.iterations;
+    if (cg_residual) *cg_residual = res.bb > 0 ? std::sqrt(res.rr / res.bb) : 0.0;
     return FS_OK;
 }

@@ -8,6 +8,7 @@ namespace {
 constexpr int SCAN_THREADS = 1024;
 constexpr int SCAN_ITEMS = 4;
 constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
+static_assert(SCAN_TILE == SCAN_TILE_ITEMS, "scan_tmp_ints sizes the tiles of this file");
 
 __device__ __forceinline__ int warp_inclusive(int v)
 {
@@ -178,8 +179,6 @@ __global__ void __launch_bounds__(DOMAIN_TPB) k_block_fluid_index(const Seg* __r
 }
 
 }  // namespace
-
-size_t scan_tmp_ints(int64_t n) { return (size_t)((n + SCAN_TILE - 1) / SCAN_TILE) + 1; }
 
 void scan_exclusive_i32(const Launch& L, const int32_t* in, int32_t* out, int64_t n, int32_t* tmp)
 {

@@ -1,7 +1,8 @@
 // Drop-in for the reference's include/FluidDomain.h.  A FluidDomain owns one
 // fsgpu handle: its MacGrid and MarkerParticleSet are mirrors of the grid
-// and particles that live on the GPU.  Fluid sources spawn on the host and
-// their new particles are appended to the device set before the next step.
+// and particles that live on the GPU.  Fluid sources are registered with the
+// handle and spawn their particles on the device (fs_update), appended to the
+// device set in the reference's order.
 #ifndef FLUID_DOMAIN_H
 #define FLUID_DOMAIN_H
 

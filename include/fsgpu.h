@@ -452,15 +452,19 @@ FS_API int64_t fs_smoke_kernel_launches(const fs_smoke* s);
  * the front velocities u, v; the output is the pressure of every cell
  * (0 outside fluid), as fs_get_pressure reports after FS_PH_PRESSURE.  The
  * velocity update is left to the caller.  Work is queued on `stream`
- * (cudaStream_t, NULL = default stream); when cg_iterations or cg_residual
- * is non-NULL the call synchronises the stream to report them.
+ * (cudaStream_t, NULL = default stream) and the call synchronises that
+ * stream before it returns, so that its return code reports a failure on
+ * the device (FS_ERR_TIMEOUT, FS_ERR_TOO_LARGE) as well as on the host;
+ * cg_iterations and cg_residual may be NULL.
  *
  * Limit: size_x * size_y <= 16384 cells (e.g. 128 x 128); larger grids
  * return FS_ERR_TOO_LARGE.  All scratch lives in one static device array of
  * about 0.75 MB that every GPU loading this library holds until exit.  The
  * first call on a device looks up that array's address (cudaGetSymbolAddress)
- * and must come before any stream capture.  Calls share the array: calls
- * whose work overlaps on the GPU race.  Messages go to fs_last_error(NULL). */
+ * and must come before any stream capture; the address is kept for the life
+ * of the process, so a device reset (cudaDeviceReset) ends the use of this
+ * entry point on that device.  Calls share the array: calls whose work
+ * overlaps on the GPU race.  Messages go to fs_last_error(NULL). */
 FS_API int fs_pressure_solve_noalloc(int size_x, int size_y, float length_x, float length_y,
                                      const uint8_t* labels, const float* u, const float* v,
                                      double cg_tolerance, int cg_max_iterations, int cg_precision,

@@ -5,7 +5,8 @@
 * ``oracle/_ref/libfsref.so`` -- the reference's own sources
   ``src/{FluidSolver,FluidDomain,MacGrid,MarkerParticleSet,LevelSet,Canvas,Renderer}.cpp``,
   compiled where they lie under the reference checkout (``$FS_REFERENCE_DIR``,
-  default ``/root/reference``) against the project's Eigen-subset stand-in
+  else a checkout named ``reference`` beside this repository's root) against
+  the project's Eigen-subset stand-in
   ``oracle/eigen_shim`` plus ``oracle/ref_harness.cpp``.  Built only when the
   reference checkout exists; nothing is copied out of it.
 
@@ -31,7 +32,10 @@ FLAGS = ["-O3", "-DNDEBUG", "-ffp-contract=off", "-fPIC", "-fno-fast-math"]
 
 
 def reference_dir() -> str:
-    return os.environ.get("FS_REFERENCE_DIR", "/root/reference")
+    env = os.environ.get("FS_REFERENCE_DIR")
+    if env:
+        return env
+    return os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference")
 
 
 def _newer(target: str, sources: list[str]) -> bool:

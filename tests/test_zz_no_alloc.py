@@ -69,6 +69,51 @@ def test_noalloc_pressure_matches_handle_path_two_calls(precision):
         assert res.value == st["cg_residual"]
 
 
+def _noalloc_vs_handle(lib, torch, nx, ny, steps, with_outputs=True):
+    """One allocation-free solve of a disc-obstacle dam break of nx x ny after
+    `steps` steps, and the handle path's pressure of the same state."""
+    solid = scenes.disc_mask(nx, ny, 0.75 * nx, 0.25 * ny, 0.1 * min(nx, ny))
+    parts = scenes.block_particles(nx, ny, float(nx), float(ny), 1, int(0.4 * nx), 1, int(0.6 * ny), 4, nx + ny,
+                                   solid)
+    tol, maxit, dt = 1e-5, 5000, 0.005
+    sim = fsg.FluidSim(nx, ny, float(nx), float(ny), dt, 0.05, cg_tolerance=tol, cg_max_iterations=maxit)
+    sim.set_solid_mask(solid)
+    sim.set_particles(parts)
+    for _ in range(steps):
+        sim.step(fsg.STEP_PICFLIP, dt)
+    labels, u, v = _state_before_pressure(sim, dt)
+    d_lab = torch.from_numpy(labels).cuda()
+    d_u = torch.from_numpy(u).cuda()
+    d_v = torch.from_numpy(v).cuda()
+    d_p = torch.full((ny, nx), float("nan"), dtype=torch.float32, device="cuda")
+    it, res = C.c_int(-1), C.c_double(-1.0)
+    rc = lib.fs_pressure_solve_noalloc(nx, ny, float(nx), float(ny), d_lab.data_ptr(), d_u.data_ptr(),
+                                       d_v.data_ptr(), tol, maxit, fsg.CG_FLOAT, d_p.data_ptr(),
+                                       C.byref(it) if with_outputs else None,
+                                       C.byref(res) if with_outputs else None,
+                                       torch.cuda.current_stream().cuda_stream)
+    assert rc == 0, lib.fs_last_error(None)
+    torch.cuda.synchronize()
+    sim.phase(fsg.PH_PRESSURE, dt)
+    assert sim.stats()["n_fluid"] > 100
+    return d_p.cpu().numpy(), sim.pressure(), (it.value if with_outputs else None), sim.stats()
+
+
+def test_noalloc_smaller_grid_after_larger_one():
+    """The shared array still holds a 128 x 128 call's values past a smaller
+    grid's cells; the 64 x 48 call after it must not see them.  Calls without
+    the optional outputs return the same pressure."""
+    torch = pytest.importorskip("torch")
+    fsbuild.build()
+    lib = fsg.load_library()
+    for nx, ny, steps, with_outputs in ((128, 128, 6, True), (64, 48, 4, False), (128, 128, 2, False),
+                                        (40, 72, 5, True)):
+        p_noalloc, p_ref, it, st = _noalloc_vs_handle(lib, torch, nx, ny, steps, with_outputs=with_outputs)
+        assert np.array_equal(p_noalloc.view(np.uint32), p_ref.view(np.uint32)), (nx, ny)
+        if with_outputs:
+            assert it == st["cg_iterations"]
+
+
 def test_noalloc_rejects_grids_beyond_its_limit():
     torch = pytest.importorskip("torch")
     fsbuild.build()
