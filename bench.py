@@ -26,8 +26,19 @@ pressure solve, not the reference's solver) and the mixed-precision form (the
 4096^2 pressure projection to relative residual 1e-10 by FP64 iterative
 refinement around float multigrid or Jacobi CG corrections, against an
 FP64-only CG), and the large step (the plain step on the dam break at twice
-the side, whose pressure system the CG keeps on chip in its 12-chunk form).
---no-forms skips them; --only-form measures one of them alone.
+the side, whose pressure system the CG keeps on chip in its 12-chunk form),
+the 500-step trajectory of the workload from its initial state with
+per-phase times (the configuration as it is stated), and the per-phase
+roofline rows of the dam break at 4096^2.  The batched form also steps the
+same members as plain handles one after another (`vs_handles`), and the
+mixed-precision form states every method's error against FP64 on the host:
+the residual recomputed from the returned solution at 4096^2, and the
+distance to an FP64 direct solve at 512^2.  --no-forms skips them;
+--only-form measures one of them alone.
+
+Both arms time steps W+1..W+K of the workload (the GPU arm's last warm-up
+step records the timed CUDA graph) and carry the same `config`; what
+differs between them is under `measurement`.
 """
 from __future__ import annotations
 
@@ -51,6 +62,104 @@ CG_BYTES_PER_CELL_ITER = 42  # fused Jacobi-PCG: 17 B (SpMV pass) + 25 B (update
 L2_FLUSH_BYTES = 256 << 20
 
 
+def phase_bytes(n_cells, n_particles, n_fluid, cg_iterations):
+    """Algorithmic bytes of each timed phase of one stepPICFLIP: every array
+    the phase must read or write, counted once (float grids and particle
+    fields 4 B, labels and masks 1 B).  N cells, P particles, F fluid cells,
+    I CG iterations; the phases are those of src/FluidSolver.cpp:211-251."""
+    N, P, F, I = n_cells, n_particles, n_fluid, cg_iterations
+    return {"classify": 8 * P + 2 * N,            # positions in; solid mask in, labels out
+            "p2g": 16 * P + 16 * N,               # particles in; u, v and their previous copies out
+            "forces": 17 * N,                     # labels in; u, v in and out (gravity, walls, extension)
+            "assembly": 8 * P + 13 * N + 13 * F,  # positions in (counts); labels, u, v in; fluid index out;
+                                                  # right-hand side, down/up rows, flags out
+            "cg": CG_BYTES_PER_CELL_ITER * F * I,
+            "project": 37 * N,                    # pressure, labels, u, v in; u, v out; walls; diff out
+            "g2p": 32 * P}                        # particles in and out (grid samples hit in cache)
+
+
+PHASE_MODEL = ("algorithmic bytes per step: classify 8P+2N, p2g 16P+16N, forces 17N, assembly 8P+13N+13F, "
+               "cg 42FI, project 37N, g2p 32P")
+
+
+def per_phase_rows(bytes_sum, ms_sum, steps, peak):
+    """{phase: algorithmic bytes and ms per step, GB/s, fraction of peak}."""
+    rows = {}
+    for k, b in bytes_sum.items():
+        ms = ms_sum.get(k, 0.0)
+        gbs = b / (ms / 1000.0) / 1e9 if ms > 0 else None
+        rows[k] = {"bytes_per_step": int(b / steps), "ms_per_step": ms / steps, "gbs": gbs,
+                   "frac": gbs / peak if gbs else None}
+    return rows
+
+
+def fp64_residual(labels, rhs, x):
+    """||b - A x|| / ||b|| over the fluid cells in float64, A the reference's
+    pressure matrix on unit cells (src/FluidSolver.cpp:363-416: +1 per liquid
+    neighbour, minus the count of non-solid neighbours on the diagonal),
+    evaluated matrix-free from the label grid."""
+    L = np.pad(labels, 1, constant_values=2)
+    X = np.pad(np.asarray(x, np.float64), 1)
+    fl = labels == 0
+    ax = np.zeros(labels.shape)
+    cnt = np.zeros(labels.shape)
+    ny, nx = labels.shape
+    for dj, di in ((0, -1), (0, 1), (-1, 0), (1, 0)):
+        nl = L[1 + dj:1 + dj + ny, 1 + di:1 + di + nx]
+        xn = X[1 + dj:1 + dj + ny, 1 + di:1 + di + nx]
+        ax += np.where(nl == 0, xn, 0.0)
+        cnt += nl != 2
+    ax -= cnt * x
+    b = np.asarray(rhs, np.float64)[fl]
+    return float(np.linalg.norm(b - ax[fl]) / np.linalg.norm(b))
+
+
+def fp64_direct_solution(labels, rhs):
+    """FP64 direct solve (scipy spsolve) of the same system: one unknown of
+    each connected fluid component pinned, then every component shifted to
+    zero mean, where the solution is unique."""
+    import scipy.sparse as sp
+    import scipy.sparse.linalg as spla
+    from scipy import ndimage
+
+    fl = labels == 0
+    idx = -np.ones(labels.shape, np.int64)
+    idx[fl] = np.arange(int(fl.sum()))
+    jj, ii = np.nonzero(fl)
+    k = idx[jj, ii]
+    rows, cols = [k], [k]
+    diag = np.zeros(k.size)
+    vals = []
+    L = np.pad(labels, 1, constant_values=2)
+    I = np.pad(idx, 1, constant_values=-1)
+    for dj, di in ((0, -1), (0, 1), (-1, 0), (1, 0)):
+        nl = L[jj + 1 + dj, ii + 1 + di]
+        diag -= nl != 2
+        liq = nl == 0
+        rows.append(k[liq])
+        cols.append(I[jj[liq] + 1 + dj, ii[liq] + 1 + di])
+        vals.append(np.ones(int(liq.sum())))
+    vals.insert(0, diag)
+    n = k.size
+    A = sp.csr_matrix((np.concatenate(vals), (np.concatenate(rows), np.concatenate(cols))), shape=(n, n))
+    b = np.asarray(rhs, np.float64)[fl]
+    comp, nc = ndimage.label(fl, structure=[[0, 1, 0], [1, 1, 1], [0, 1, 0]])
+    cidx = comp[fl]
+    _, pins = np.unique(cidx, return_index=True)
+    keep = np.ones(n, bool)
+    keep[pins] = False
+    xd = np.zeros(n)
+    xd[keep] = spla.spsolve(A[keep][:, keep].tocsc(), b[keep])
+    return demean_components(xd, cidx, nc), cidx, nc
+
+
+def demean_components(v, cidx, nc):
+    from scipy import ndimage
+
+    means = ndimage.mean(v, cidx, index=np.arange(1, nc + 1))
+    return v - means[cidx - 1]
+
+
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -69,7 +178,13 @@ def parse():
                     help="CG iteration cap of each projection solve (a small cap makes a short profiling case)")
     ap.add_argument("--batch-plan", type=int, choices=[1, 2, 4, 8], default=None,
                     help="batched form: CG chunks per CTA instead of the autotuner's choice")
-    ap.add_argument("--only-form", choices=["batched", "mixed_precision", "multigrid", "large_step"], default=None,
+    ap.add_argument("--handles-steps", type=int, default=5,
+                    help="batched form: steps of the same members as plain handles, one after another (0: skip)")
+    ap.add_argument("--trajectory-steps", type=int, default=500,
+                    help="trajectory form: steps of the workload from its initial state (0: skip)")
+    ap.add_argument("--phases-size", type=int, default=4096, help="grid side of the per-phase roofline form (0: skip)")
+    ap.add_argument("--only-form", choices=["batched", "mixed_precision", "multigrid", "large_step", "trajectory",
+                                            "phases"], default=None,
                     help="measure one form alone (profiling runs) and print its JSON object")
     return ap.parse_args()
 
@@ -219,9 +334,11 @@ def run_reference(args, rank):
             "steps": len(times), "warmup": warm, "ms_per_step": 1000 * total / len(times),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded SplitMix64 dam break)",
-            "config": config_of(sc, {"implementation": "reference C++ sources + Eigen-subset stand-in"
-                                     if kind == "reference" else "C restatement of the reference (port)"}),
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1,
+            "config": config_of(sc),
+            "measurement": {"implementation": "reference C++ sources + Eigen-subset stand-in"
+                            if kind == "reference" else "C restatement of the reference (port)",
+                            "timed_steps": "steps %d..%d of the workload" % (warm + 1, warm + len(times))},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1, "host_cores": os.cpu_count(),
                              "kind": "reference" if kind == "reference" else "port", "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -308,12 +425,58 @@ def measure_batched(args, local_rank, plain_value, flush):
         itmax = max(itmax, st["cg_iterations"])
     t = sum(ms) / 1000.0
     value = cells * args.steps / t
-    return {"workload": "%d simulations, sides U{32..256} (seed 0xC3), %d cells, %d particles, "
-                        "stepPICFLIP, CG 1e-5" % (len(sc), cells, sum(len(s.particles) for s in sc)),
-            "value": value, "unit": UNIT, "ms_per_step": 1000.0 * t / args.steps, "vs_plain": value / plain_value,
-            "cg_plan_chunks_per_cta": tuned["chunks_per_cta"], "tuner_ms_per_step": tuned["ms_per_step"],
-            "cg_iterations_max_last_step": itmax, "sum_F_I_last_step": fi,
-            "gpu_launches": int(b.kernel_launches() - l0)}
+    launches = int(b.kernel_launches() - l0)
+    b.close()
+    out = {"workload": "%d simulations, sides U{32..256} (seed 0xC3), %d cells, %d particles, "
+                       "stepPICFLIP, CG 1e-5" % (len(sc), cells, sum(len(s.particles) for s in sc)),
+           "value": value, "unit": UNIT, "ms_per_step": 1000.0 * t / args.steps, "vs_plain": value / plain_value,
+           "cg_plan_chunks_per_cta": tuned["chunks_per_cta"], "tuner_ms_per_step": tuned["ms_per_step"],
+           "cg_iterations_max_last_step": itmax, "sum_F_I_last_step": fi, "gpu_launches": launches}
+    if args.handles_steps > 0:
+        nh = min(args.handles_steps, args.steps)
+        h = measure_handles(sc, 1 + args.warmup, nh, local_rank, flush)
+        batch_ms = float(np.mean(ms[:nh]))
+        out["vs_handles"] = {"workload": "the same members, each a plain FluidSim handle stepped one after "
+                                         "another (each handle's step is its own CUDA graph)",
+                             "steps": nh, "handles_device_ms_per_step": h["device_ms"],
+                             "handles_wall_ms_per_step": h["wall_ms"], "batch_ms_per_step_same_steps": batch_ms,
+                             "speedup_device": h["device_ms"] / batch_ms, "speedup_wall": h["wall_ms"] / batch_ms}
+    return out
+
+
+def measure_handles(scs, pre_steps, steps, local_rank, flush):
+    """The batch's members as independent FluidSim handles, stepped one after
+    another: pre_steps untimed steps each (the batch's first step and
+    warm-up), then `steps` timed steps; per step the sum over members of
+    each member's device time (events on its own stream, the member
+    synchronised before the next starts) and the wall time of the loop."""
+    import torch
+
+    import fluid_simulation_gb300 as fsg
+
+    sims = [fsg.FluidSim.from_scene(sc, device=local_rank) for sc in scs]
+    for sim in sims:
+        for _ in range(pre_steps):
+            sim.step(fsg.STEP_PICFLIP, 0.005)
+    torch.cuda.synchronize()
+    dev, wall = 0.0, 0.0
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in sims]
+    streams = [torch.cuda.ExternalStream(sim.stream(), device=local_rank) for sim in sims]
+    for _ in range(steps):
+        with torch.cuda.stream(streams[0]):
+            flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for sim, (e0, e1), st in zip(sims, evs, streams):
+            e0.record(st)
+            sim.step(fsg.STEP_PICFLIP, 0.005)
+            e1.record(st)
+            e1.synchronize()
+        wall += time.perf_counter() - t0
+        dev += sum(e0.elapsed_time(e1) for e0, e1 in evs)
+    for sim in sims:
+        sim.close()
+    return {"device_ms": dev / steps, "wall_ms": 1000.0 * wall / steps}
 
 
 def measure_projection(args, local_rank):
@@ -339,15 +502,47 @@ def measure_projection(args, local_rank):
     for name in args.projection_methods.split(","):
         method, inner = methods[name]
         st = ps.solve(method, 1e-10, args.projection_max_iterations, inner_tol=1e-3, inner_precision=inner)
-        out[name] = {"ms": st["ms"], "residual": st["residual"], "outer_iterations": st["outer_iterations"],
-                     "inner_iterations": st["inner_iterations"],
+        out[name] = {"ms": st["ms"], "residual": st["residual"],
+                     "residual_fp64_host": fp64_residual(labels, rhs, ps.solution()),
+                     "outer_iterations": st["outer_iterations"], "inner_iterations": st["inner_iterations"],
                      "cell_solves_per_s": n * n / (st["ms"] / 1000.0)}
+    out["residual_fp64_host"] = ("||b - A x|| / ||b|| recomputed in float64 on the host from the returned x "
+                                 "(numpy, matrix-free), beside the library's own residual")
     if "fp64" in out:
         for name, key in (("mixed_f32_dots", "speedup_mixed_vs_fp64"),
                           ("mixed_multigrid", "speedup_mixed_multigrid_vs_fp64"),
                           ("mixed_f64_dots", "speedup_mixed_f64_dots_vs_fp64")):
             if name in out:
                 out[key] = out["fp64"]["ms"] / out[name]["ms"]
+    ps.close()
+    out["fp64_direct_512"] = projection_vs_direct(512, methods, args, local_rank)
+    return out
+
+
+def projection_vs_direct(n, methods, args, local_rank):
+    """Every projection method on the n x n problem against an FP64 direct
+    solve on the host (both shifted to zero mean per fluid component, where
+    the solution is unique): max |x - x_FP64| / max |x_FP64| and the relative
+    L2 error."""
+    import fluid_simulation_gb300 as fsg
+    from fluid_simulation_gb300 import scenes
+
+    labels, rhs = scenes.projection_problem(n)
+    t0 = time.perf_counter()
+    xd, cidx, nc = fp64_direct_solution(labels, rhs)
+    out = {"workload": "%dx%d projection (same generator), relative residual 1e-10 (fp32: 1e-5)" % (n, n),
+           "direct_solve_s": time.perf_counter() - t0}
+    fl = labels == 0
+    ps = fsg.PoissonSolver(n, n, float(n), float(n), device=local_rank)
+    ps.set_problem(labels, rhs)
+    for name in args.projection_methods.split(","):
+        method, inner = methods[name]
+        tol = 1e-5 if method == fsg.POISSON_FP32 else 1e-10
+        st = ps.solve(method, tol, args.projection_max_iterations, inner_tol=1e-3, inner_precision=inner)
+        x = demean_components(ps.solution()[fl], cidx, nc)
+        out[name] = {"max_rel_err": float(np.abs(x - xd).max() / np.abs(xd).max()),
+                     "l2_rel_err": float(np.linalg.norm(x - xd) / np.linalg.norm(xd)),
+                     "residual": st["residual"]}
     ps.close()
     return out
 
@@ -386,6 +581,89 @@ def measure_multigrid(args, local_rank, plain_value, flush):
             "cg_iterations_mean": float(np.mean(its))}
 
 
+def _timed_steps(sim, sc, stream, flush, steps):
+    """`steps` stepPICFLIP steps, each timed with CUDA events (an L2-flushing
+    write before each, outside the events), with the library's per-phase
+    times and the per-phase algorithmic bytes."""
+    import torch
+
+    import fluid_simulation_gb300 as fsg
+
+    ms, its = [], []
+    phases = {k: 0.0 for k in fsg.TIMED_PHASES}
+    bsum = {k: 0 for k in fsg.TIMED_PHASES}
+    for _ in range(steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+        sim.step(fsg.STEP_PICFLIP, sc.dt)
+        e1.record(stream)
+        st = sim.stats()
+        ms.append(e0.elapsed_time(e1))
+        its.append(st["cg_iterations"])
+        for k, v in st["ms_phase"].items():
+            phases[k] += v
+        for k, v in phase_bytes(sc.cells, sim.num_particles(), st["n_fluid"], st["cg_iterations"]).items():
+            bsum[k] += v
+    return ms, its, phases, bsum
+
+
+def measure_trajectory(args, local_rank, flush, peak):
+    """The workload as its configuration states it: --trajectory-steps (500)
+    stepPICFLIP steps from the initial state on a fresh handle, per-step
+    device time, per-phase times and the CG iterations of every step."""
+    import torch
+
+    import fluid_simulation_gb300 as fsg
+
+    sc = workload(args.size)
+    sim = fsg.FluidSim.from_scene(sc, device=local_rank)
+    sim.set_timing(True)
+    stream = torch.cuda.ExternalStream(sim.stream(), device=local_rank)
+    n = args.trajectory_steps
+    t0 = time.perf_counter()
+    ms, its, phases, bsum = _timed_steps(sim, sc, stream, flush, n)
+    wall = time.perf_counter() - t0
+    sim.close()
+    t = sum(ms) / 1000.0
+    return {"workload": "the plain workload, steps 1..%d from its initial state (the configuration's trajectory)"
+                        % n, "steps": n, "value": sc.cells * n / t, "unit": UNIT, "ms_per_step": 1000.0 * t / n,
+            "ms_per_step_after_first": float(np.mean(ms[1:])) if n > 1 else None,
+            "wall_s": wall, "phases_ms_per_step": {k: v / n for k, v in phases.items()},
+            "cg_iterations_mean": float(np.mean(its)), "cg_iterations_max": int(np.max(its)),
+            "per_phase_roofline": per_phase_rows(bsum, phases, n, peak), "per_phase_model": PHASE_MODEL}
+
+
+def measure_phases(args, local_rank, flush, peak):
+    """Per-phase roofline rows of the plain step on the dam break at
+    --phases-size (4096^2: about 6.9M fluid cells and 27M particles): 2
+    warm-up steps, then 2 steps timed with the library's phase events."""
+    import torch
+
+    import fluid_simulation_gb300 as fsg
+
+    sc = workload(args.phases_size)
+    try:
+        sim = fsg.FluidSim.from_scene(sc, device=local_rank)
+    except fsg.FsError as e:
+        if e.code != 5:  # FS_ERR_TOO_LARGE: the library's own size limit
+            raise
+        return {"skipped": "the library refused the %dx%d grid: %s" % (sc.size_x, sc.size_y, e)}
+    for _ in range(2):
+        sim.step(fsg.STEP_PICFLIP, sc.dt)
+    sim.set_timing(True)
+    stream = torch.cuda.ExternalStream(sim.stream(), device=local_rank)
+    ms, its, phases, bsum = _timed_steps(sim, sc, stream, flush, 2)
+    nf = sim.stats()["n_fluid"]
+    sim.close()
+    return {"workload": "dam break %dx%d (the plain workload scaled), %d particles, stepPICFLIP, Jacobi-PCG 1e-5"
+                        % (sc.size_x, sc.size_y, sc.particles.shape[0]), "fluid_cells": nf,
+            "ms_per_step": float(np.mean(ms)), "cg_iterations": its,
+            "per_phase_roofline": per_phase_rows(bsum, phases, 2, peak), "per_phase_model": PHASE_MODEL}
+
+
 def measure_large_step(args, local_rank, flush):
     """The plain step (the reference's algorithm, bit-exact) on the dam break
     at twice the side, 2048^2: about 1.72M fluid cells, 12 chunks of 1024
@@ -395,11 +673,13 @@ def measure_large_step(args, local_rank, flush):
 
     import fluid_simulation_gb300 as fsg
 
-    if 2 * args.size > 4096:
-        return {"skipped": "a handle holds at most 4096x4096 cells; --size %d doubles to %d" % (args.size,
-                                                                                               2 * args.size)}
     sc = workload(2 * args.size)
-    sim = fsg.FluidSim.from_scene(sc, device=local_rank)
+    try:
+        sim = fsg.FluidSim.from_scene(sc, device=local_rank)
+    except fsg.FsError as e:
+        if e.code != 5:  # FS_ERR_TOO_LARGE: the library's own size limit
+            raise
+        return {"skipped": "the library refused the %dx%d grid: %s" % (sc.size_x, sc.size_y, e)}
     for _ in range(2):
         sim.step(fsg.STEP_PICFLIP, sc.dt)
     sim.synchronize()
@@ -449,6 +729,10 @@ def run_gpu(args, rank, world, local_rank):
                 out = measure_multigrid(args, local_rank, float("nan"), flush)
             elif args.only_form == "large_step":
                 out = measure_large_step(args, local_rank, flush)
+            elif args.only_form == "trajectory":
+                out = measure_trajectory(args, local_rank, flush, peaks()[0])
+            elif args.only_form == "phases":
+                out = measure_phases(args, local_rank, flush, peaks()[0])
             else:
                 out = measure_projection(args, local_rank)
             print(json.dumps({"form": args.only_form, **out}), flush=True)
@@ -458,16 +742,18 @@ def run_gpu(args, rank, world, local_rank):
     stream = torch.cuda.ExternalStream(sim.stream(), device=local_rank)
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda:%d" % local_rank)
 
-    for _ in range(args.warmup):
+    # W untimed warm-up steps, the last of which records the timed graph
+    # variant (per-phase events): the timed steps are W+1..W+K, as in the
+    # reference arm
+    for _ in range(max(args.warmup - 1, 0)):
+        sim.step(fsg.STEP_PICFLIP, sc.dt)
+    sim.set_timing(True)
+    if args.warmup > 0:
         sim.step(fsg.STEP_PICFLIP, sc.dt)
     sim.synchronize()
     # state at the start of the timed region, for the CPU baseline sample
     grids0 = [sim.grid(w) for w in range(8)] if rank == 0 else None
     parts0 = sim.particles() if rank == 0 else None
-
-    sim.set_timing(True)
-    sim.step(fsg.STEP_PICFLIP, sc.dt)  # records the timed graph variant; not counted
-    sim.synchronize()
     start = sim.snapshot()  # the end-to-end run below replays the timed steps from here
     if world > 1:
         import torch.distributed as dist
@@ -475,6 +761,7 @@ def run_gpu(args, rank, world, local_rank):
         dist.barrier()
     torch.cuda.synchronize()
     step_ms, cg_ms, fi, iters, phases = [], [], 0, [], {k: 0.0 for k in fsg.TIMED_PHASES}
+    bsum = {k: 0 for k in fsg.TIMED_PHASES}
     launches0 = sim.kernel_launches()
     with ClockSampler(local_rank) as clk:
         for _ in range(args.steps):
@@ -492,6 +779,8 @@ def run_gpu(args, rank, world, local_rank):
                 phases[k] += v
             fi += st["n_fluid"] * st["cg_iterations"]
             iters.append(st["cg_iterations"])
+            for k, v in phase_bytes(sc.cells, sim.num_particles(), st["n_fluid"], st["cg_iterations"]).items():
+                bsum[k] += v
     launches = sim.kernel_launches() - launches0
     torch.cuda.synchronize()
     t_dev = max_over_ranks(sum(step_ms) / 1000.0, "cuda:%d" % local_rank)
@@ -523,14 +812,19 @@ def run_gpu(args, rank, world, local_rank):
 
     if rank != 0:
         return
+    sim.close()
+    peak, peak_kind = peaks()
     forms = None
     if world == 1 and not args.no_forms:
         forms = {"batched": measure_batched(args, local_rank, value, flush),
                  "multigrid": measure_multigrid(args, local_rank, value, flush),
                  "large_step": measure_large_step(args, local_rank, flush),
                  "mixed_precision": measure_projection(args, local_rank)}
+        if args.trajectory_steps > 0:
+            forms["trajectory_500"] = measure_trajectory(args, local_rank, flush, peak)
+        if args.phases_size > 0:
+            forms["phases_4096"] = measure_phases(args, local_rank, flush, peak)
     # roofline of the dominant kernel (the CG)
-    peak, peak_kind = peaks()
     cg_s = sum(cg_ms) / 1000.0
     achieved = CG_BYTES_PER_CELL_ITER * fi / cg_s / 1e9 if cg_s > 0 else None
     traffic = read_traffic()
@@ -548,9 +842,12 @@ def run_gpu(args, rank, world, local_rank):
         "warmup": args.warmup, "ms_per_step": 1000.0 * t_dev / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded SplitMix64 dam break)",
-        "config": config_of(sc, {"parallelism": "replicas" if world > 1 else "single GPU",
-                                 "l2": "256 MiB written before every timed step; the step's CUDA events exclude it",
-                                 "cg_iterations_mean": float(np.mean(iters)), "cg_iterations": iters}),
+        "config": config_of(sc),
+        "measurement": {"parallelism": "replicas" if world > 1 else "single GPU",
+                        "l2": "256 MiB written before every timed step; the step's CUDA events exclude it",
+                        "timed_steps": "steps %d..%d of the workload (W warm-up steps first, the last of them "
+                                       "recording the timed graph)" % (args.warmup + 1, args.warmup + args.steps),
+                        "cg_iterations_mean": float(np.mean(iters)), "cg_iterations": iters},
         "phases_ms_per_step": {k: v / args.steps for k, v in phases.items()},
         "gpu_launches": int(launches),
         "e2e": {"value": e2e_value, "unit": UNIT, "steps": e2e_steps,
@@ -561,8 +858,9 @@ def run_gpu(args, rank, world, local_rank):
                      "frac": (achieved / peak) if achieved else None, "traffic": traffic,
                      "algorithmic_bytes": "%d B per fluid cell per CG iteration x sum(F x I) = %d B"
                                           % (CG_BYTES_PER_CELL_ITER, CG_BYTES_PER_CELL_ITER * fi),
-                     "cg_ms_per_step": 1000.0 * cg_s / args.steps},
-        "cpu_baseline": {"value": cpu_value, "unit": UNIT, "cores": 1,
+                     "cg_ms_per_step": 1000.0 * cg_s / args.steps,
+                     "per_phase": per_phase_rows(bsum, phases, args.steps, peak), "per_phase_model": PHASE_MODEL},
+        "cpu_baseline": {"value": cpu_value, "unit": UNIT, "cores": 1, "host_cores": os.cpu_count(),
                          "kind": "reference" if kind == "reference" else "port",
                          "sample": "1 stepPICFLIP of the same workload from the GPU state at the start of "
                                    "the timed region (%.1f s), single thread" % sum(ctimes)},
