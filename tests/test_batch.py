@@ -191,3 +191,56 @@ def test_batch_member_outgrowing_its_cluster_plan_stays_exact():
             o.step(po.STEP_PICFLIP, 0.005)
             assert_same(b.state(s), o.state(), "grown step %d sim %d" % (k, s))
     assert b.stats(0)["n_fluid"] > 4 * 1024 * 5 // 4
+
+
+def _launch_class(n_fluid, interior, target):
+    """(chunks per CTA footprint, CTAs per cluster) of a member planned from
+    n_fluid fluid cells for the tuner's target chunks per CTA (the planning
+    rule of fs_batch: current fluid cells plus 25%, at most the interior,
+    in 1024-cell chunks; the smallest power-of-two cluster up to 8 that keeps
+    the chunks per CTA at or under the target)."""
+    ch = max(1, min((n_fluid * 5 // 4 + 1023) // 1024, max(1, (interior + 1023) // 1024)))
+    c = 1
+    while c < 8 and -(-ch // c) > target:
+        c *= 2
+    return (4 if -(-ch // c) <= 4 else 8, c)
+
+
+@pytest.mark.gpu
+def test_full_batch_workload_members_bit_exact_after_tuning():
+    """The benchmark's batched workload itself -- 512 members of sides
+    U{32..256} (seed 0xC3), 12.9M cells -- tuned as the benchmark tunes it,
+    then stepped: after each of three steps, at least 32 members are
+    bit-identical to the restatement stepping each alone, among them every
+    member of side 248 or more, members with three discs, and the first
+    member of every CG launch class of the tuned plan."""
+    fsbuild.build()
+    sc = scenes.batch_scenes(512)
+    b = fsg.FluidBatch.from_scenes(sc)
+    b.step(fsg.STEP_PICFLIP, 0.005)
+    nf = [b.stats(s)["n_fluid"] for s in range(len(sc))]
+    t = b.tune(fsg.STEP_PICFLIP, 0.005, steps=2)
+    target = t["chunks_per_cta"]
+    classes = {}
+    for s, x in enumerate(sc):
+        classes.setdefault(_launch_class(nf[s], (x.size_x - 2) * (x.size_y - 2), target), []).append(s)
+    pick = {v[0] for v in classes.values()}
+    pick |= {s for s, x in enumerate(sc) if x.size_x >= 248}
+    pick |= set([s for s, x in enumerate(sc) if x.meta["discs"] == 3][:8])
+    pick |= set(range(0, 512, 32))
+    pick = sorted(pick)
+    assert len(pick) >= 32 and len(classes) >= 3, (len(pick), sorted(classes))
+    os_ = {s: oracle_for(sc[s]) for s in pick}
+    for o in os_.values():
+        assert o.step(po.STEP_PICFLIP, 0.005) == 0
+    for k in range(3):
+        b.step(fsg.STEP_PICFLIP, 0.005)
+        for s in pick:
+            o = os_[s]
+            assert o.step(po.STEP_PICFLIP, 0.005) == 0
+            assert_same(b.state(s), o.state(), "tuned 512-member batch, step %d, sim %d (%dx%d)"
+                        % (k + 2, s, sc[s].size_x, sc[s].size_y))
+            it, res, n = o.cg_stats()
+            st = b.stats(s)
+            assert (st["cg_iterations"], st["n_fluid"]) == (it, n), (k, s)
+    assert max(sc[s].size_x for s in pick) >= 250

@@ -190,6 +190,58 @@ def test_gpu_methods_error_against_fp64_direct_solve():
     assert errs["fp32"] < 1e-2, errs
 
 
+@pytest.mark.gpu
+def test_gpu_methods_against_fp64_direct_solve_512():
+    """The 4096^2 workload's generator at 512^2, where an FP64 direct solve on
+    the host is affordable: every method's solution (shifted to zero mean per
+    fluid component, where it is unique) against the direct solve, and the
+    residual recomputed in float64 from the returned solution.  The FP64,
+    mixed and mixed-multigrid methods stay within 1e-8 relative."""
+    import scipy.sparse.linalg as spla
+    from scipy import ndimage
+
+    import fluid_simulation_gb300 as fsg
+    from fluid_simulation_gb300 import build as fsbuild
+
+    fsbuild.build()
+    n = 512
+    labels, rhs = scenes.projection_problem(n)
+    A, b, fluid = _system(labels, rhs)
+    comp, nc = ndimage.label(fluid, structure=[[0, 1, 0], [1, 1, 1], [0, 1, 0]])
+    cidx = comp[fluid]
+    _, pins = np.unique(cidx, return_index=True)
+    keep = np.ones(b.size, bool)
+    keep[pins] = False
+    xd = np.zeros(b.size)
+    xd[keep] = spla.spsolve(A[keep][:, keep].tocsc(), b[keep])
+
+    def demean(v):
+        m = ndimage.mean(v, cidx, index=np.arange(1, nc + 1))
+        return v - m[cidx - 1]
+
+    xd = demean(xd)
+    ps = fsg.PoissonSolver(n, n, float(n), float(n))
+    ps.set_problem(labels, rhs)
+    errs = {}
+    for name, method, inner, tol in (("fp32", fsg.POISSON_FP32, fsg.CG_FLOAT, 1e-5),
+                                     ("fp64", fsg.POISSON_FP64, fsg.CG_FLOAT, 1e-10),
+                                     ("mixed_f32_dots", fsg.POISSON_MIXED, fsg.CG_FLOAT, 1e-10),
+                                     ("mixed_f64_dots", fsg.POISSON_MIXED, fsg.CG_DOUBLE, 1e-10),
+                                     ("mixed_multigrid", fsg.POISSON_MIXED_MG, fsg.CG_FLOAT, 1e-10)):
+        st = ps.solve(method, tol, 200000, inner_tol=1e-3, inner_precision=inner)
+        xf = ps.solution()[fluid]
+        x = demean(xf)
+        true_res = np.linalg.norm(b - A @ xf) / np.linalg.norm(b)
+        errs[name] = (float(np.abs(x - xd).max() / np.abs(xd).max()),
+                      float(np.linalg.norm(x - xd) / np.linalg.norm(xd)), float(true_res))
+        if method != fsg.POISSON_FP32:
+            assert true_res < 2e-10, (name, true_res)  # FP64 CG stops on its recursive residual
+            assert errs[name][0] < 1e-8 and errs[name][1] < 1e-8, (name, errs[name])
+    ps.close()
+    print("max / L2 relative error vs FP64 direct solve, FP64 residual:", errs)
+    assert errs["fp32"][1] < 1e-2, errs
+
+
 def test_restated_float_cg_against_scipy_cg():
     """The restatement's Jacobi-preconditioned float CG (the reference's
     solver) against scipy.sparse.linalg.cg and an FP64 direct solve of the
