@@ -31,7 +31,7 @@ CG_FLOAT, CG_DOUBLE = 0, 1
 POISSON_FP32, POISSON_FP64, POISSON_MIXED, POISSON_MGPCG, POISSON_MIXED_MG = 0, 1, 2, 3, 4
 SOLVER_JACOBI_PCG, SOLVER_MGPCG = 0, 1
 INTEGRATOR_EULER, INTEGRATOR_RK2, INTEGRATOR_RK3 = 0, 1, 2
-SMOKE_FP32, SMOKE_FP64 = 0, 1
+SMOKE_FP32, SMOKE_FP64, SMOKE_FP32_TRACE64 = 0, 1, 2
 RENDER_CLEAR, RENDER_CELLS, RENDER_VELOCITIES, RENDER_PARTICLES, RENDER_METABALLS, RENDER_LEVEL_SET = range(6)
 TIMED_PHASES = ("classify", "p2g", "forces", "assembly", "cg", "project", "g2p")
 

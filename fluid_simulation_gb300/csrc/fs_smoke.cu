@@ -20,11 +20,14 @@
 //
 // The projection composed with the wall condition is symmetric (B - B D^T
 // A^-1 D B with the wall mask B and the divergence D), so its adjoint is the
-// same operation on the adjoint velocity.  The adjoint of advection scatters
-// each sample's adjoint through the transposed bilinear weights (double
-// atomics) and carries the adjoint of the traced position back through the
-// integrator stages.  Fields and advection run in the handle's precision
-// (float or double); adjoints accumulate in double.
+// same operation on the adjoint velocity.  The adjoint of advection sends
+// each sample's adjoint through the transposed bilinear weights and carries
+// the adjoint of the traced position back through the integrator stages.
+// The transpose is a gather, so that gradients repeat to the bit: every
+// contribution becomes an item keyed by the node it adds to, the counting
+// sort of the ordered splat (group_by_key) groups the items by node in item
+// order, and each node adds its items in that order.  Fields and advection
+// run in the handle's precision (float or double); adjoints are double.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -69,19 +72,20 @@ __device__ __forceinline__ Foot<T> footprint(int nx, int ny, T h, T x, T y)
     return F;
 }
 
-template <typename T>
-__device__ __forceinline__ T interp(const T* __restrict__ f, int nx, const Foot<T>& F)
+// Field values stored as S, sampled in the arithmetic A of the footprint.
+template <typename S, typename A>
+__device__ __forceinline__ A interp(const S* __restrict__ f, int nx, const Foot<A>& F)
 {
-    const T v00 = f[F.i + F.j * nx], v10 = f[F.i1 + F.j * nx];
-    const T v01 = f[F.i + F.j1 * nx], v11 = f[F.i1 + F.j1 * nx];
-    const T a = (T(1) - F.fi) * v00 + F.fi * v10;
-    const T b = (T(1) - F.fi) * v01 + F.fi * v11;
-    return (T(1) - F.fj) * a + F.fj * b;
+    const A v00 = (A)f[F.i + F.j * nx], v10 = (A)f[F.i1 + F.j * nx];
+    const A v01 = (A)f[F.i + F.j1 * nx], v11 = (A)f[F.i1 + F.j1 * nx];
+    const A a = (A(1) - F.fi) * v00 + F.fi * v10;
+    const A b = (A(1) - F.fi) * v01 + F.fi * v11;
+    return (A(1) - F.fj) * a + F.fj * b;
 }
 
 // d interp / d(x, y), in double.
-template <typename T>
-__device__ __forceinline__ void interp_grad(const T* __restrict__ f, int nx, const Foot<T>& F, double h, double& gx,
+template <typename S, typename A>
+__device__ __forceinline__ void interp_grad(const S* __restrict__ f, int nx, const Foot<A>& F, double h, double& gx,
                                             double& gy)
 {
     const double v00 = f[F.i + F.j * nx], v10 = f[F.i1 + F.j * nx];
@@ -91,31 +95,59 @@ __device__ __forceinline__ void interp_grad(const T* __restrict__ f, int nx, con
     gy = ((1.0 - fi) * (v01 - v00) + fi * (v11 - v10)) / h;
 }
 
-// acc += w * (the bilinear weights of F): the transpose of interp.
-template <typename T>
-__device__ __forceinline__ void scatter(double* __restrict__ acc, int nx, const Foot<T>& F, double w)
+// Contribution items of one adjoint step: item q * n + c is contribution
+// slot q of cell c; key = field * n + node (field 0 u, 1 v, 2 density), or
+// 3 n for an empty slot; val = the value added there.
+struct Items
 {
-    if (w == 0.0) return;
+    uint32_t* key;
+    double* val;
+    int64_t n;
+};
+
+// Slots of a sample's contributions: its final footprint (4 corners), then 8
+// per integrator stage (4 u corners, 4 v corners).
+__host__ __device__ constexpr int stage_count(int integrator)
+{
+    return integrator == FS_INTEGRATOR_EULER ? 1 : integrator == FS_INTEGRATOR_RK2 ? 2 : 3;
+}
+__host__ __device__ constexpr int sample_slots(int integrator) { return 4 + 8 * stage_count(integrator); }
+
+// w * (the bilinear weights of F) into field `field`: the transpose of
+// interp, as four items from slot q of cell c.
+template <typename T>
+__device__ __forceinline__ void scatter(const Items& it, int64_t c, int q, int field, int nx, const Foot<T>& F,
+                                        double w)
+{
+    const uint32_t none = (uint32_t)(3 * it.n);
+    const int64_t base = (int64_t)field * it.n;
     const double fi = F.fi, fj = F.fj;
-    atomicAdd(&acc[F.i + F.j * nx], (1.0 - fi) * (1.0 - fj) * w);
-    atomicAdd(&acc[F.i1 + F.j * nx], fi * (1.0 - fj) * w);
-    atomicAdd(&acc[F.i + F.j1 * nx], (1.0 - fi) * fj * w);
-    atomicAdd(&acc[F.i1 + F.j1 * nx], fi * fj * w);
+    const int64_t node[4] = {F.i + (int64_t)F.j * nx, F.i1 + (int64_t)F.j * nx, F.i + (int64_t)F.j1 * nx,
+                             F.i1 + (int64_t)F.j1 * nx};
+    const double wt[4] = {(1.0 - fi) * (1.0 - fj) * w, fi * (1.0 - fj) * w, (1.0 - fi) * fj * w, fi * fj * w};
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const int64_t item = (int64_t)(q + k) * it.n + c;
+        it.key[item] = w == 0.0 ? none : (uint32_t)(base + node[k]);
+        it.val[item] = wt[k];
+    }
 }
 
-template <typename T>
+// Fields stored as S; back-trace positions, footprints and samples in the
+// arithmetic A (S, or double for float fields traced in double).
+template <typename S, typename A = S>
 struct Fields
 {
-    const T *u, *v, *d;
+    const S *u, *v, *d;
     int nx, ny;
-    T h;
-    __device__ Foot<T> foot_u(T x, T y) const { return footprint<T>(nx, ny, h, x, y - h / T(2)); }
-    __device__ Foot<T> foot_v(T x, T y) const { return footprint<T>(nx, ny, h, x - h / T(2), y); }
-    __device__ Foot<T> foot_d(T x, T y) const { return footprint<T>(nx, ny, h, x - h / T(2), y - h / T(2)); }
-    __device__ void vel(T x, T y, T& vx, T& vy) const
+    A h;
+    __device__ Foot<A> foot_u(A x, A y) const { return footprint<A>(nx, ny, h, x, y - h / A(2)); }
+    __device__ Foot<A> foot_v(A x, A y) const { return footprint<A>(nx, ny, h, x - h / A(2), y); }
+    __device__ Foot<A> foot_d(A x, A y) const { return footprint<A>(nx, ny, h, x - h / A(2), y - h / A(2)); }
+    __device__ void vel(A x, A y, A& vx, A& vy) const
     {
-        vx = interp(u, nx, foot_u(x, y));
-        vy = interp(v, nx, foot_v(x, y));
+        vx = interp<S, A>(u, nx, foot_u(x, y));
+        vy = interp<S, A>(v, nx, foot_v(x, y));
     }
 };
 
@@ -128,8 +160,8 @@ struct Trace
     T ox, oy;      // the traced position
 };
 
-template <typename T>
-__device__ __forceinline__ void trace(const Fields<T>& F, int integrator, T ht, T x, T y, Trace<T>& tr)
+template <typename S, typename T>
+__device__ __forceinline__ void trace(const Fields<S, T>& F, int integrator, T ht, T x, T y, Trace<T>& tr)
 {
     tr.x[0] = x;
     tr.y[0] = y;
@@ -170,9 +202,9 @@ __device__ __forceinline__ bool v_open(const uint8_t* lab, int nx, int i, int j)
 
 // One advection: every u face, v face and cell centre gathers from the old
 // fields at its traced position; closed faces get 0.
-template <typename T>
-__global__ void k_advect(Fields<T> F, const uint8_t* __restrict__ lab, int integrator, T dt, T* __restrict__ un,
-                         T* __restrict__ vn, T* __restrict__ dn)
+template <typename S, typename T>
+__global__ void k_advect(Fields<S, T> F, const uint8_t* __restrict__ lab, int integrator, T dt, S* __restrict__ un,
+                         S* __restrict__ vn, S* __restrict__ dn)
 {
     const int64_t c = (int64_t)blockIdx.x * TPB + threadIdx.x;
     if (c >= (int64_t)F.nx * F.ny) return;
@@ -181,18 +213,18 @@ __global__ void k_advect(Fields<T> F, const uint8_t* __restrict__ lab, int integ
     Trace<T> tr;
     if (u_open(lab, F.nx, i, j)) {
         trace(F, integrator, ht, T(i) * h, (T(j) + T(0.5)) * h, tr);
-        un[c] = interp(F.u, F.nx, F.foot_u(tr.ox, tr.oy));
+        un[c] = (S)interp<S, T>(F.u, F.nx, F.foot_u(tr.ox, tr.oy));
     } else {
-        un[c] = T(0);
+        un[c] = S(0);
     }
     if (v_open(lab, F.nx, i, j)) {
         trace(F, integrator, ht, (T(i) + T(0.5)) * h, T(j) * h, tr);
-        vn[c] = interp(F.v, F.nx, F.foot_v(tr.ox, tr.oy));
+        vn[c] = (S)interp<S, T>(F.v, F.nx, F.foot_v(tr.ox, tr.oy));
     } else {
-        vn[c] = T(0);
+        vn[c] = S(0);
     }
     trace(F, integrator, ht, (T(i) + T(0.5)) * h, (T(j) + T(0.5)) * h, tr);
-    dn[c] = interp(F.d, F.nx, F.foot_d(tr.ox, tr.oy));
+    dn[c] = (S)interp<S, T>(F.d, F.nx, F.foot_d(tr.ox, tr.oy));
 }
 
 // rhs = divergence on fluid cells (double), 0 elsewhere.
@@ -223,21 +255,22 @@ __global__ void k_subtract_gradient(int nx, int ny, double h, const uint8_t* __r
     if (here && j > 0 && lab[c - nx] == FS_LIQUID) v[c] = (T)((double)v[c] - (p[c] - p[c - nx]) / h);
 }
 
-// The adjoint of one advection.  lu, lv, ld: adjoints of the advected fields
-// (already through the projection's adjoint); au, av, ad: adjoints of the old
-// fields, accumulated.
-template <typename T>
-__global__ void k_advect_adjoint(Fields<T> F, const uint8_t* __restrict__ lab, int integrator, T dt,
+// The adjoint of one advection as contribution items (Items).  lu, lv, ld:
+// adjoints of the advected fields (already through the projection's
+// adjoint); the items add up to the adjoints of the old fields.
+template <typename S, typename T>
+__global__ void k_advect_adjoint(Fields<S, T> F, const uint8_t* __restrict__ lab, int integrator, T dt,
                                  const double* __restrict__ lu, const double* __restrict__ lv,
-                                 const double* __restrict__ ld, double* __restrict__ au, double* __restrict__ av,
-                                 double* __restrict__ ad)
+                                 const double* __restrict__ ld, Items items)
 {
     const int64_t c = (int64_t)blockIdx.x * TPB + threadIdx.x;
     if (c >= (int64_t)F.nx * F.ny) return;
     const int i = (int)(c % F.nx), j = (int)(c / F.nx);
     const T h = F.h, ht = -dt;
     const double hd = (double)h, htd = (double)ht;
+    const int per = sample_slots(integrator);
     for (int s = 0; s < 3; ++s) {
+        const int q0 = s * per;
         double lam;
         T x0, y0;
         if (s == 0) {
@@ -253,32 +286,38 @@ __global__ void k_advect_adjoint(Fields<T> F, const uint8_t* __restrict__ lab, i
             x0 = (T(i) + T(0.5)) * h;
             y0 = (T(j) + T(0.5)) * h;
         }
-        if (lam == 0.0) continue;
+        if (lam == 0.0) {
+            for (int q = 0; q < per; ++q) items.key[(int64_t)(q0 + q) * items.n + c] = (uint32_t)(3 * items.n);
+            continue;
+        }
         Trace<T> tr;
         trace(F, integrator, ht, x0, y0, tr);
         // the sampled field at the traced position
         double gx, gy;
         if (s == 0) {
             const Foot<T> fo = F.foot_u(tr.ox, tr.oy);
-            scatter(au, F.nx, fo, lam);
+            scatter(items, c, q0, 0, F.nx, fo, lam);
             interp_grad(F.u, F.nx, fo, hd, gx, gy);
         } else if (s == 1) {
             const Foot<T> fo = F.foot_v(tr.ox, tr.oy);
-            scatter(av, F.nx, fo, lam);
+            scatter(items, c, q0, 1, F.nx, fo, lam);
             interp_grad(F.v, F.nx, fo, hd, gx, gy);
         } else {
             const Foot<T> fo = F.foot_d(tr.ox, tr.oy);
-            scatter(ad, F.nx, fo, lam);
+            scatter(items, c, q0, 2, F.nx, fo, lam);
             interp_grad(F.d, F.nx, fo, hd, gx, gy);
         }
         const double lx = lam * gx, ly = lam * gy;  // adjoint of the traced position
         // back through the stages: adjoint of the velocity sample k at stage
-        // position q adds to the fields there and to q's adjoint
+        // position q adds to the fields there and to q's adjoint (the t-th
+        // stage visited fills slots 4 + 8 t .. 11 + 8 t of the sample)
+        int t = 0;
         auto stage = [&](int q, double kxa, double kya, double& pxa, double& pya) {
             const Foot<T> fu = F.foot_u(tr.x[q], tr.y[q]);
             const Foot<T> fv = F.foot_v(tr.x[q], tr.y[q]);
-            scatter(au, F.nx, fu, kxa);
-            scatter(av, F.nx, fv, kya);
+            scatter(items, c, q0 + 4 + 8 * t, 0, F.nx, fu, kxa);
+            scatter(items, c, q0 + 8 + 8 * t, 1, F.nx, fv, kya);
+            ++t;
             double ux, uy, vx, vy;
             interp_grad(F.u, F.nx, fu, hd, ux, uy);
             interp_grad(F.v, F.nx, fv, hd, vx, vy);
@@ -304,6 +343,20 @@ __global__ void k_advect_adjoint(Fields<T> F, const uint8_t* __restrict__ lab, i
             stage(0, k1x, k1y, px, py);
         }
     }
+}
+
+// acc[field][node] = the sum of the items grouped at bin field * n + node, in
+// item order (bin_start / sorted from group_by_key).
+__global__ void k_adjoint_gather(int64_t n, const int32_t* __restrict__ bin_start, const int32_t* __restrict__ sorted,
+                                 const double* __restrict__ val, double* __restrict__ au, double* __restrict__ av,
+                                 double* __restrict__ ad)
+{
+    const int64_t b = (int64_t)blockIdx.x * TPB + threadIdx.x;
+    if (b >= 3 * n) return;
+    double acc = 0.0;
+    for (int k = bin_start[b]; k < bin_start[b + 1]; ++k) acc += val[sorted[k]];
+    double* out = b < n ? au : b < 2 * n ? av : ad;
+    out[b % n] = acc;
 }
 
 // Adjoint of the wall condition: closed faces pass nothing back.
@@ -389,6 +442,7 @@ struct fs_smoke
     int64_t n = 0;
     double h = 1.0;
     bool fp64 = false;
+    bool trace64 = false;  // float fields, back-traces in double
     size_t esize = 4;  // bytes per field value
     fs_poisson* poisson = nullptr;
     cudaStream_t stream = nullptr;
@@ -408,6 +462,15 @@ struct fs_smoke
     double* acc[3] = {};  // adjoint of the previous state
     double* part = nullptr;
     double* scal = nullptr;
+    // contribution items of the adjoint's advection step and their grouping
+    // by node (allocated by the first backward pass)
+    int64_t n_items = 0;
+    uint32_t* item_key = nullptr;
+    double* item_val = nullptr;
+    int32_t* item_sorted = nullptr;
+    int32_t* bin_count = nullptr;
+    int32_t* bin_start = nullptr;
+    int32_t* scan_tmp = nullptr;
     double loss = 0.0;
     int64_t launches = 0;
     std::string err;
@@ -429,16 +492,16 @@ int scuda(fs_smoke* s, cudaError_t e, const char* what)
                  std::string(what) + ": " + cudaGetErrorString(e));
 }
 
-template <typename T>
-Fields<T> fields(const fs_smoke* s, void* const* st)
+template <typename S, typename A = S>
+Fields<S, A> fields(const fs_smoke* s, void* const* st)
 {
-    Fields<T> F;
-    F.u = static_cast<const T*>(st[0]);
-    F.v = static_cast<const T*>(st[1]);
-    F.d = static_cast<const T*>(st[2]);
+    Fields<S, A> F;
+    F.u = static_cast<const S*>(st[0]);
+    F.v = static_cast<const S*>(st[1]);
+    F.d = static_cast<const S*>(st[2]);
     F.nx = s->nx;
     F.ny = s->ny;
-    F.h = (T)s->h;
+    F.h = (A)s->h;
     return F;
 }
 
@@ -472,11 +535,15 @@ int step_state(fs_smoke* s, void* const* in, void* const* out)
     const unsigned nb = nblocks(s->n);
     const double dt = s->cfg.dt;
     if (s->fp64)
-        k_advect<double><<<nb, TPB, 0, s->stream>>>(fields<double>(s, in), s->labels, s->cfg.integrator, dt,
-                                                    (double*)out[0], (double*)out[1], (double*)out[2]);
+        k_advect<double, double><<<nb, TPB, 0, s->stream>>>(fields<double>(s, in), s->labels, s->cfg.integrator, dt,
+                                                            (double*)out[0], (double*)out[1], (double*)out[2]);
+    else if (s->trace64)
+        k_advect<float, double><<<nb, TPB, 0, s->stream>>>(fields<float, double>(s, in), s->labels,
+                                                           s->cfg.integrator, dt, (float*)out[0], (float*)out[1],
+                                                           (float*)out[2]);
     else
-        k_advect<float><<<nb, TPB, 0, s->stream>>>(fields<float>(s, in), s->labels, s->cfg.integrator, (float)dt,
-                                                   (float*)out[0], (float*)out[1], (float*)out[2]);
+        k_advect<float, float><<<nb, TPB, 0, s->stream>>>(fields<float>(s, in), s->labels, s->cfg.integrator,
+                                                          (float)dt, (float*)out[0], (float*)out[1], (float*)out[2]);
     s->launches += 1;
     return project_fields(s, out[0], out[1]);
 }
@@ -496,16 +563,26 @@ int adjoint_step(fs_smoke* s, void* const* state_n)
     if (rc) return sfail(s, rc, std::string("adjoint projection: ") + fs_last_error(nullptr));
     k_subtract_gradient<double><<<nb, TPB, 0, s->stream>>>(s->nx, s->ny, s->h, s->labels, s->pres, s->lam[0], s->lam[1]);
     s->launches += 1;
-    // advection
-    for (int k = 0; k < 3; ++k) cudaMemsetAsync(s->acc[k], 0, bytes, s->stream);
+    // advection: contribution items, grouped by node, summed in item order
+    (void)bytes;
+    const Items items{s->item_key, s->item_val, s->n};
     if (s->fp64)
-        k_advect_adjoint<double><<<nb, TPB, 0, s->stream>>>(fields<double>(s, state_n), s->labels, s->cfg.integrator,
-                                                            s->cfg.dt, s->lam[0], s->lam[1], s->lam[2], s->acc[0],
-                                                            s->acc[1], s->acc[2]);
+        k_advect_adjoint<double, double><<<nb, TPB, 0, s->stream>>>(fields<double>(s, state_n), s->labels,
+                                                                    s->cfg.integrator, s->cfg.dt, s->lam[0],
+                                                                    s->lam[1], s->lam[2], items);
+    else if (s->trace64)
+        k_advect_adjoint<float, double><<<nb, TPB, 0, s->stream>>>(fields<float, double>(s, state_n), s->labels,
+                                                                   s->cfg.integrator, s->cfg.dt, s->lam[0],
+                                                                   s->lam[1], s->lam[2], items);
     else
-        k_advect_adjoint<float><<<nb, TPB, 0, s->stream>>>(fields<float>(s, state_n), s->labels, s->cfg.integrator,
-                                                           (float)s->cfg.dt, s->lam[0], s->lam[1], s->lam[2],
-                                                           s->acc[0], s->acc[1], s->acc[2]);
+        k_advect_adjoint<float, float><<<nb, TPB, 0, s->stream>>>(fields<float>(s, state_n), s->labels,
+                                                                  s->cfg.integrator, (float)s->cfg.dt, s->lam[0],
+                                                                  s->lam[1], s->lam[2], items);
+    s->launches += 1;
+    const Launch L{s->stream, &s->launches, 0};
+    group_by_key(L, s->n_items, s->item_key, 3 * s->n, s->bin_count, s->bin_start, s->scan_tmp, s->item_sorted);
+    k_adjoint_gather<<<nblocks(3 * s->n), TPB, 0, s->stream>>>(s->n, s->bin_start, s->item_sorted, s->item_val,
+                                                               s->acc[0], s->acc[1], s->acc[2]);
     s->launches += 1;
     for (int k = 0; k < 3; ++k) std::swap(s->lam[k], s->acc[k]);
     return scuda(s, cudaGetLastError(), "adjoint step");
@@ -516,7 +593,8 @@ void free_smoke(fs_smoke* s)
     if (!s) return;
     cudaSetDevice(s->cfg.device);
     if (s->stream) cudaStreamSynchronize(s->stream);
-    std::vector<void*> ptrs = {s->labels, s->target, s->rhs, s->pres, s->part, s->scal};
+    std::vector<void*> ptrs = {s->labels, s->target, s->rhs, s->pres, s->part, s->scal, s->item_key, s->item_val,
+                               s->item_sorted, s->bin_count, s->bin_start, s->scan_tmp};
     for (int k = 0; k < 3; ++k) {
         ptrs.push_back(s->init[k]);
         ptrs.push_back(s->cur[k]);
@@ -583,7 +661,8 @@ int fs_smoke_create(const fs_smoke_config* cfg, fs_smoke** out)
     const fs_smoke_config& c = *cfg;
     if (c.size_x < 3 || c.size_y < 3 || !(c.length_x > 0) || !(c.length_y > 0) || !(c.dt >= 0) ||
         c.integrator < FS_INTEGRATOR_EULER || c.integrator > FS_INTEGRATOR_RK3 ||
-        (c.precision != FS_SMOKE_FP32 && c.precision != FS_SMOKE_FP64) || c.checkpoint_every < 1 ||
+        (c.precision != FS_SMOKE_FP32 && c.precision != FS_SMOKE_FP64 && c.precision != FS_SMOKE_FP32_TRACE64) ||
+        c.checkpoint_every < 1 ||
         c.projection_method < FS_POISSON_FP32 || c.projection_method > FS_POISSON_MIXED)
         return sfail(nullptr, FS_ERR_INVALID_ARGUMENT, "invalid smoke configuration");
     const double hx = (double)c.length_x / c.size_x, hy = (double)c.length_y / c.size_y;
@@ -597,6 +676,7 @@ int fs_smoke_create(const fs_smoke_config* cfg, fs_smoke** out)
     s->n = (int64_t)c.size_x * c.size_y;
     s->h = hx;
     s->fp64 = c.precision == FS_SMOKE_FP64;
+    s->trace64 = c.precision == FS_SMOKE_FP32_TRACE64;
     s->esize = s->fp64 ? 8 : 4;
     cudaError_t e = cudaSetDevice(c.device);
     if (e != cudaSuccess) {
@@ -758,6 +838,32 @@ int fs_smoke_backward(fs_smoke* s, double* grad_u, double* grad_v, double* grad_
     const unsigned nb = nblocks(s->n);
     const size_t bytes = 8 * (size_t)s->n;
     const int steps = s->steps_done, C = s->cfg.checkpoint_every;
+    if (!s->item_key) {
+        // 3 samples per cell, sample_slots items each; 3 n bins (one per node of u, v, density)
+        const int64_t items = (int64_t)s->n * 3 * sample_slots(s->cfg.integrator);
+        if (items > INT32_MAX || 3 * s->n >= (int64_t)UINT32_MAX)
+            return sfail(s, FS_ERR_TOO_LARGE, "grid too large for the adjoint's contribution items");
+        const size_t bins = (size_t)(3 * s->n) + 2;
+        cudaError_t e = cudaSuccess;
+        auto A = [&](void** p, size_t nbytes) {
+            if (e == cudaSuccess) e = cudaMalloc(p, nbytes);
+        };
+        A((void**)&s->item_key, 4 * (size_t)items);
+        A((void**)&s->item_val, 8 * (size_t)items);
+        A((void**)&s->item_sorted, 4 * (size_t)items);
+        A((void**)&s->bin_count, 4 * bins);
+        A((void**)&s->bin_start, 4 * bins);
+        A((void**)&s->scan_tmp, 4 * scan_tmp_ints((int64_t)bins));
+        if (e != cudaSuccess) {
+            for (void** p : {(void**)&s->item_key, (void**)&s->item_val, (void**)&s->item_sorted,
+                             (void**)&s->bin_count, (void**)&s->bin_start, (void**)&s->scan_tmp}) {
+                cudaFree(*p);
+                *p = nullptr;
+            }
+            return scuda(s, e, "adjoint item buffers");
+        }
+        s->n_items = items;
+    }
     cudaMemsetAsync(s->lam[0], 0, bytes, s->stream);
     cudaMemsetAsync(s->lam[1], 0, bytes, s->stream);
     const double inv_l = s->loss > 0 ? 1.0 / s->loss : 0.0;

@@ -404,6 +404,8 @@ FS_API int64_t fs_batch_kernel_launches(fs_batch* b);
 #define FS_INTEGRATOR_RK3 2
 #define FS_SMOKE_FP32 0
 #define FS_SMOKE_FP64 1
+/* float fields whose back-traces (positions, footprints, samples) run in double */
+#define FS_SMOKE_FP32_TRACE64 2
 
 typedef struct fs_smoke fs_smoke;
 typedef struct fs_smoke_config
@@ -412,7 +414,7 @@ typedef struct fs_smoke_config
     float length_x, length_y;  /* square cells: length_x / size_x == length_y / size_y */
     float dt;
     int integrator;            /* FS_INTEGRATOR_* */
-    int precision;             /* FS_SMOKE_FP32 / FS_SMOKE_FP64 */
+    int precision;             /* FS_SMOKE_FP32 / FS_SMOKE_FP64 / FS_SMOKE_FP32_TRACE64 */
     int projection_method;     /* FS_POISSON_* */
     double cg_tolerance;       /* relative residual of each projection */
     int cg_max_iterations;
