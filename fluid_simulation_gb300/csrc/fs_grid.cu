@@ -35,6 +35,30 @@ struct LabelsFromParticles
     }
 };
 
+// The two per-particle passes of a step over the same positions, fused:
+// LabelsFromParticles (classifyCells) and CountParticles (pressureSolve's
+// count).  A step moves no particle between the two, so the counts are the
+// ones pressureSolve would take.
+struct LabelsAndCounts
+{
+    const float* px;
+    const float* py;
+    uint8_t* lab;
+    int32_t* counts;
+    unsigned* warn;
+    __device__ void operator()(const Seg& s, int64_t k) const
+    {
+        const Geom& g = s.g;
+        const int x = trunc_i(fmul(fdiv(px[s.po + k], g.lx), (float)g.nx));
+        const int y = trunc_i(fmul(fdiv(py[s.po + k], g.ly), (float)g.ny));
+        lab[s.co + clampi(x, 0, g.nx - 1) + (int64_t)clampi(y, 0, g.ny - 1) * g.nx] = LIQUID;
+        if (x >= 0 && x < g.nx && y >= 0 && y < g.ny)
+            atomicAdd(&counts[s.co + x + (int64_t)y * g.nx], 1);
+        else
+            atomicOr(warn, FS_WARN_PARTICLE_OUTSIDE);
+    }
+};
+
 // Border reset (src/FluidDomain.cpp:169-179) and the persistent solid mask.
 struct LabelsFinalize
 {
@@ -166,6 +190,22 @@ struct ExtendInit
         myb[o] = vy;
         vb[o] = vy ? vf[o] : 0.0f;
         if (!vx || !vy) uf[o] = 0.0f;
+    }
+};
+
+// Gravity, Dirichlet and ExtendInit of one face in one pass, in the step's
+// order (src/FluidSolver.cpp:230-232, 490-530): each reads and writes only
+// its own face's velocities (and the labels), so the fusion changes nothing.
+struct ForcesExtendInit
+{
+    Gravity gravity;
+    Dirichlet dirichlet;
+    ExtendInit init;
+    __device__ void operator()(const Seg& s, int64_t c, int i, int j) const
+    {
+        gravity(s, c, i, j);
+        dirichlet(s, c, i, j);
+        init(s, c, i, j);
     }
 };
 
@@ -391,6 +431,21 @@ void labels_from_particles(const Launch& L, const Domain& d, const float* px, co
 void labels_finalize(const Launch& L, const Domain& d, uint8_t* lab, const uint8_t* solid)
 {
     each_cell(L, d, LabelsFinalize{lab, solid});
+}
+
+void labels_and_counts(const Launch& L, const Domain& d, const float* px, const float* py, uint8_t* lab,
+                       int32_t* counts32, unsigned* warn)
+{
+    cudaMemsetAsync(counts32, 0, sizeof(int32_t) * (size_t)d.cells, L.stream);
+    each_particle(L, d, LabelsAndCounts{px, py, lab, counts32, warn});
+}
+
+void forces_extend_init(const Launch& L, const Domain& d, const uint8_t* lab, float* uf, float* vf, float dt,
+                        float* ub, float* vb, uint8_t* mxf, uint8_t* mxb, uint8_t* myf, uint8_t* myb)
+{
+    each_cell(L, d,
+              ForcesExtendInit{Gravity{lab, uf, vf, dt}, Dirichlet{lab, uf, vf},
+                               ExtendInit{lab, uf, vf, ub, vb, mxf, mxb, myf, myb}});
 }
 
 void count_particles(const Launch& L, const Domain& d, const float* px, const float* py, int32_t* counts32,

@@ -88,6 +88,7 @@ struct SplatWork
 {
     uint32_t* keys = nullptr;      // bin of each item
     int32_t* sorted = nullptr;     // items grouped by bin, each bin in item order
+    void* rec = nullptr;           // p2g_binned: 32-byte particle records in binned order
     int32_t* bin_count = nullptr;  // cells + 2
     int32_t* bin_start = nullptr;  // cells + 2
     int32_t* scan_tmp = nullptr;
@@ -99,6 +100,13 @@ struct SplatWork
 // increasing k.  bin_count holds nbins + 1 ints, scan_tmp scan_tmp_ints(nbins).
 void group_by_key(const Launch& L, int64_t n, const uint32_t* keys, int64_t nbins, int32_t* bin_count,
                   int32_t* bin_start, int32_t* scan_tmp, int32_t* sorted);
+// transferVelocityToGridSpread's two splats (u at (x, y - dy/2) of vx, v at
+// (x - dx/2, y) of vy, each with its weights) from one binning of the
+// particles by their own cell, for grids with square cells: su/wu and sv/wv
+// equal ordered_splat's sums and weights to the bit.  A particle whose
+// footprint breaks the binning's assumption sets ST_INTERNAL in *status.
+void p2g_binned(const Launch& L, const Domain& d, const float* px, const float* py, const float* pvx,
+                const float* pvy, float* su, float* wu, float* sv, float* wv, unsigned* status, SplatWork& w);
 // Buffers for up to `items` items over `cells` cells (frees what w held).
 cudaError_t splat_alloc(SplatWork& w, int64_t items, int64_t cells);
 void splat_free(SplatWork& w);
@@ -123,6 +131,12 @@ void labels_from_particles(const Launch& L, const Domain& d, const float* px, co
 void labels_finalize(const Launch& L, const Domain& d, uint8_t* lab, const uint8_t* solid);
 void count_particles(const Launch& L, const Domain& d, const float* px, const float* py, int32_t* counts32,
                      unsigned* warn);
+// labels_from_particles and count_particles in one pass over the particles.
+void labels_and_counts(const Launch& L, const Domain& d, const float* px, const float* py, uint8_t* lab,
+                       int32_t* counts32, unsigned* warn);
+// gravity, dirichlet and extend_init in one pass over the faces.
+void forces_extend_init(const Launch& L, const Domain& d, const uint8_t* lab, float* uf, float* vf, float dt,
+                        float* ub, float* vb, uint8_t* mxf, uint8_t* mxb, uint8_t* myf, uint8_t* myb);
 void p2g_finish(const Launch& L, const Domain& d, const float* sum_u, const float* w_u, const float* sum_v,
                 const float* w_v, float* ub, float* vb);
 void grid_copy2(const Launch& L, const Domain& d, const float* a0, const float* a1, float* b0, float* b1);

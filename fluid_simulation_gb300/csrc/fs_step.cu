@@ -9,17 +9,27 @@ void mark(StepState& st, int k)
     if (st.mark) st.mark(st.owner, k);
 }
 
-// FluidDomain::classifyCells (src/FluidDomain.cpp:150-180).
-void ph_classify(const Launch& L, StepState& st)
+// FluidDomain::classifyCells (src/FluidDomain.cpp:150-180); with_counts:
+// also pressureSolve's particle counts (the step's particles do not move
+// before its pressure solve).
+void ph_classify(const Launch& L, StepState& st, bool with_counts = false)
 {
     labels_clear(L, st.d, st.labels);
-    labels_from_particles(L, st.d, st.px, st.py, st.labels);
+    if (with_counts) labels_and_counts(L, st.d, st.px, st.py, st.labels, st.counts32, st.warn);
+    else labels_from_particles(L, st.d, st.px, st.py, st.labels);
     labels_finalize(L, st.d, st.labels, st.solid);
 }
 
 // transferVelocityToGridSpread (src/FluidSolver.cpp:873-919), then the swap.
 void ph_p2g(const Launch& L, StepState& st)
 {
+    if (st.square_cells) {
+        p2g_binned(L, st.d, st.px, st.py, st.pvx, st.pvy, st.acc[0], st.acc[1], st.acc[2], st.acc[3], st.status,
+                   *st.sw);
+        p2g_finish(L, st.d, st.acc[0], st.acc[1], st.acc[2], st.acc[3], st.UB(), st.VB());
+        *st.front ^= 1;
+        return;
+    }
     p2g_positions(L, st.d, st.px, st.py, st.yu, st.xv);
     const float* vu[2] = {st.pvx, nullptr};
     float* ou[2] = {st.acc[0], st.acc[1]};
@@ -42,12 +52,18 @@ void ph_gravity(const Launch& L, StepState& st, float dt) { gravity(L, st.d, st.
 
 void ph_dirichlet(const Launch& L, StepState& st) { dirichlet(L, st.d, st.labels, st.UF(), st.VF()); }
 
-// extendVelocityIndividual (src/FluidSolver.cpp:485-622), then the swap.
-void ph_extend(const Launch& L, StepState& st)
+// extendVelocityIndividual (src/FluidSolver.cpp:485-622), then the swap;
+// with_forces: gravity and the Dirichlet condition first, fused with the
+// extension's initialisation.
+void ph_extend(const Launch& L, StepState& st, bool with_forces = false, float dt = 0.0f)
 {
     const int vf = *st.vfront;
-    extend_init(L, st.d, st.labels, st.UF(), st.VF(), st.UB(), st.VB(), st.vmx[vf], st.vmx[1 - vf], st.vmy[vf],
-                st.vmy[1 - vf]);
+    if (with_forces)
+        forces_extend_init(L, st.d, st.labels, st.UF(), st.VF(), dt, st.UB(), st.VB(), st.vmx[vf], st.vmx[1 - vf],
+                           st.vmy[vf], st.vmy[1 - vf]);
+    else
+        extend_init(L, st.d, st.labels, st.UF(), st.VF(), st.UB(), st.VB(), st.vmx[vf], st.vmx[1 - vf], st.vmy[vf],
+                    st.vmy[1 - vf]);
     for (int it = 0; it < st.n_ext; ++it) {
         const int f = *st.vfront;
         extend_sweep(L, st.d, st.labels, st.UB(), st.VB(), st.vmx[f], st.vmx[1 - f], st.vmy[f], st.vmy[1 - f]);
@@ -56,10 +72,11 @@ void ph_extend(const Launch& L, StepState& st)
     *st.front ^= 1;
 }
 
-// FluidSolver::pressureSolve (src/FluidSolver.cpp:323-483), then the swap.
-void ph_pressure(const Launch& L, StepState& st, float dt)
+// FluidSolver::pressureSolve (src/FluidSolver.cpp:323-483), then the swap;
+// counted: the particle counts were taken by the step's classification.
+void ph_pressure(const Launch& L, StepState& st, float dt, bool counted = false)
 {
-    count_particles(L, st.d, st.px, st.py, st.counts32, st.warn);
+    if (!counted) count_particles(L, st.d, st.px, st.py, st.counts32, st.warn);
     fluid_index_batch(L, st.d, st.labels, st.fidx, st.cell_of, st.nfluid, st.index_tmp);
     assemble(L, st.d, st.labels, st.fidx, st.cell_of, st.nfluid, st.UF(), st.VF(), st.cg_b, st.cg_down, st.cg_up,
              st.cg_flags, st.counts32, st.counts8);
@@ -120,7 +137,7 @@ void enqueue_phase(const Launch& L, StepState& st, int ph, float dt)
 void enqueue_step(const Launch& L, StepState& st, int method, float dt)
 {
     mark(st, FS_T_CLASSIFY);
-    ph_classify(L, st);
+    ph_classify(L, st, true);
     mark(st, FS_T_P2G);
     if (method == FS_STEP_SEMI_LAGRANGIAN) {
         mark(st, FS_T_FORCES);
@@ -131,12 +148,10 @@ void enqueue_step(const Launch& L, StepState& st, int method, float dt)
         ph_p2g(L, st);
         if (method != FS_STEP_PIC) ph_save_prev(L, st);
         mark(st, FS_T_FORCES);
-        ph_gravity(L, st, dt);
-        ph_dirichlet(L, st);
-        ph_extend(L, st);
+        ph_extend(L, st, true, dt);  // gravity, Dirichlet, extension
     }
     mark(st, FS_T_ASSEMBLY);
-    ph_pressure(L, st, dt);
+    ph_pressure(L, st, dt, true);
     ph_dirichlet(L, st);
     if (method == FS_STEP_FLIP || method == FS_STEP_PICFLIP) ph_save_diff(L, st);
     mark(st, FS_T_G2P);
