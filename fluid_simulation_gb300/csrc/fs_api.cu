@@ -317,8 +317,6 @@ StepState state(fs_handle* h)
     st.cg_x = h->cg.x;
     st.nfluid = h->d_nfluid;
     st.warn = h->d_warn;
-    st.status = h->d_status;
-    st.square_cells = h->g.dx == h->g.dy;
     st.index_tmp = h->scan_tmp;
     st.n_ext = h->n_ext;
     st.solve = solve_hook;

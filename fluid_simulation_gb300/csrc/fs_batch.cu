@@ -73,7 +73,6 @@ struct fs_batch
     int n = 0;
     std::vector<fs_config> cfg;
     std::vector<Seg> seg;                     // host copy of the segment table
-    bool square_cells = true;                 // every simulation has dx == dy
     std::vector<int64_t> cap;                 // particle capacity of each simulation (multiple of DOMAIN_TPB)
     std::vector<std::vector<float>> pending;  // particles set since the last layout (AoS)
     std::vector<char> has_pending;
@@ -407,8 +406,6 @@ StepState state(fs_batch* b)
     st.cg_x = b->cx;
     st.nfluid = b->nfluid;
     st.warn = b->warn;
-    st.status = b->status;
-    st.square_cells = b->square_cells;
     st.index_tmp = b->index_tmp;
     st.n_ext = b->n_ext;
     st.solve = batch_solve;
@@ -642,7 +639,6 @@ int fs_batch_create(int n, const fs_config* cfgs, fs_batch** out)
         g.ly = (float)g.ny * g.dy;
         g.pdx = g.dx;
         g.pdy = g.dx;  // the solver pool's copy keeps delta_x for delta_y (src/FluidSolver.cpp:56-62)
-        if (g.dx != g.dy) b->square_cells = false;
         if (interior(sg) > BATCH_MAX_INTERIOR) {
             g_batch_error = "simulation " + std::to_string(s) + ": more than 65536 interior cells for a batch";
             delete b;

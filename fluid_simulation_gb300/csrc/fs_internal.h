@@ -88,7 +88,6 @@ struct SplatWork
 {
     uint32_t* keys = nullptr;      // bin of each item
     int32_t* sorted = nullptr;     // items grouped by bin, each bin in item order
-    void* rec = nullptr;           // p2g_binned: 32-byte particle records in binned order
     int32_t* bin_count = nullptr;  // cells + 2
     int32_t* bin_start = nullptr;  // cells + 2
     int32_t* scan_tmp = nullptr;
@@ -100,13 +99,6 @@ struct SplatWork
 // increasing k.  bin_count holds nbins + 1 ints, scan_tmp scan_tmp_ints(nbins).
 void group_by_key(const Launch& L, int64_t n, const uint32_t* keys, int64_t nbins, int32_t* bin_count,
                   int32_t* bin_start, int32_t* scan_tmp, int32_t* sorted);
-// transferVelocityToGridSpread's two splats (u at (x, y - dy/2) of vx, v at
-// (x - dx/2, y) of vy, each with its weights) from one binning of the
-// particles by their own cell, for grids with square cells: su/wu and sv/wv
-// equal ordered_splat's sums and weights to the bit.  A particle whose
-// footprint breaks the binning's assumption sets ST_INTERNAL in *status.
-void p2g_binned(const Launch& L, const Domain& d, const float* px, const float* py, const float* pvx,
-                const float* pvy, float* su, float* wu, float* sv, float* wv, unsigned* status, SplatWork& w);
 // Buffers for up to `items` items over `cells` cells (frees what w held).
 cudaError_t splat_alloc(SplatWork& w, int64_t items, int64_t cells);
 void splat_free(SplatWork& w);

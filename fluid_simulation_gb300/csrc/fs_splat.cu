@@ -167,252 +167,7 @@ struct SplatGather
     }
 };
 
-// ---- The particle-to-grid transfer with one binning for u and v.
-// With square cells (dx == dy: the pool's deltas equal the grid's) a
-// particle's u splat position (x, y - dy/2) has its base cell in the
-// particle's own cell (clamp(trunc(x/dx)), clamp(trunc(y/dy))) or the one
-// below it, and its v splat position (x - dx/2, y) in its own cell or the
-// one to the left: the shifted coordinate is never larger, its quotient by
-// the cell size differs by about 1/2, and truncation and clamping are
-// monotone and move values by at most their difference (positions beyond
-// 2^22 cells from the grid clamp both to the same border cell).  So the
-// particles are binned once, by their own cell, and the node (a, b) of u
-// gathers own cells (a-1..a, b-1..b+1), the node of v own cells
-// (a-1..a+1, b-1..b): one merge by particle index over the 8 cells of both.
-// Each particle's footprint fractions are computed once, into a record
-// written in binned order, so the gather reads contiguous records and
-// divides nothing.
-struct P2GRec
-{
-    int32_t idx;  // flattened particle index (the merge order)
-    float fui, fuj, fvi;
-    float fvj, vx, vy;
-    uint32_t bits;  // REC_* below
-};
-static_assert(sizeof(P2GRec) == 32, "two 16-byte loads per record");
-constexpr uint32_t REC_U_DOWN = 1u;   // u base row = own row - 1
-constexpr uint32_t REC_U_XC = 2u;     // u footprint: i1 == i (clamped)
-constexpr uint32_t REC_U_YC = 4u;     // u footprint: j1 == j
-constexpr uint32_t REC_V_LEFT = 8u;   // v base column = own column - 1
-constexpr uint32_t REC_V_XC = 16u;
-constexpr uint32_t REC_V_YC = 32u;
-constexpr uint32_t REC_BAD = 64u;     // a base outside the two cells the binning relies on
-
-// Key of each particle: its own cell (flattened), as the u splat's column
-// and the v splat's row compute it; d.cells for padding.
-__global__ void __launch_bounds__(DOMAIN_TPB) k_p2g_keys(Seg one, const Seg* __restrict__ segs,
-                                                         const int2* __restrict__ blk, int64_t n, uint32_t invalid,
-                                                         const float* __restrict__ px, const float* __restrict__ py,
-                                                         uint32_t* __restrict__ keys, int32_t* __restrict__ bin_count)
-{
-    const int64_t k = (int64_t)blockIdx.x * DOMAIN_TPB + threadIdx.x;
-    if (k >= n) return;
-    Seg s;
-    int64_t local;
-    if (blk) {
-        const int2 m = blk[blockIdx.x];
-        s = segs[m.x];
-        local = (int64_t)m.y + threadIdx.x;
-    } else {
-        s = one;
-        local = k;
-    }
-    uint32_t key = invalid;
-    if (local < s.np) {
-        const int i = clampi(trunc_i(fdiv(px[k], s.g.pdx)), 0, s.g.nx - 1);
-        const int j = clampi(trunc_i(fdiv(py[k], s.g.pdy)), 0, s.g.ny - 1);
-        key = (uint32_t)(s.co + i + (int64_t)j * s.g.nx);
-    }
-    keys[k] = key;
-    atomicAdd(&bin_count[key], 1);
-}
-
-// Footprint of a splat at (x, y) as Splat computes it (include/Grid.h:152-184):
-// fractions, base cell and whether each +1 corner collapses onto the base.
-struct Foot
-{
-    float fi, fj;
-    int i, j;
-    bool xc, yc;
-};
-__device__ __forceinline__ Foot foot(const Geom& g, float x, float y)
-{
-    const float xs = fdiv(x, g.pdx);
-    const float ys = fdiv(y, g.pdy);
-    const int ti = trunc_i(xs), tj = trunc_i(ys);
-    Foot f;
-    f.fi = fsub(xs, (float)ti);
-    f.fj = fsub(ys, (float)tj);
-    f.i = clampi(ti, 0, g.nx - 1);
-    f.j = clampi(tj, 0, g.ny - 1);
-    f.xc = clampi(ti + 1, 0, g.nx - 1) == f.i;
-    f.yc = clampi(tj + 1, 0, g.ny - 1) == f.j;
-    return f;
-}
-
-// Per bin (cell): its particles in index order (insertion sort), then their
-// records in that order.
-struct P2GSortPack
-{
-    const int32_t* bin_start;
-    int32_t* sorted;
-    const float *px, *py, *pvx, *pvy;
-    P2GRec* rec;
-    unsigned* status;
-    __device__ void operator()(const Seg& s, int64_t c, int ci, int cj) const
-    {
-        const int64_t bin = s.co + c;
-        const int b0 = bin_start[bin], b1 = bin_start[bin + 1];
-        if (b1 - b0 >= 2) {
-            for (int i = b0 + 1; i < b1; ++i) {
-                const int t = sorted[i];
-                int j = i - 1;
-                while (j >= b0 && sorted[j] > t) {
-                    sorted[j + 1] = sorted[j];
-                    --j;
-                }
-                sorted[j + 1] = t;
-            }
-        }
-        const Geom& g = s.g;
-        for (int q = b0; q < b1; ++q) {
-            const int k = sorted[q];
-            const float x = px[k], y = py[k];
-            // transferVelocityToGridSpread's positions (src/FluidSolver.cpp:889-896)
-            const Foot fu = foot(g, x, fsub(y, fmul(g.dy, 0.5f)));
-            const Foot fv = foot(g, fsub(x, fmul(g.dx, 0.5f)), y);
-            uint32_t bits = (fu.xc ? REC_U_XC : 0u) | (fu.yc ? REC_U_YC : 0u) | (fv.xc ? REC_V_XC : 0u) |
-                            (fv.yc ? REC_V_YC : 0u);
-            if (fu.j == cj - 1) bits |= REC_U_DOWN;
-            else if (fu.j != cj || fu.i != ci) bits |= REC_BAD;
-            if (fv.i == ci - 1) bits |= REC_V_LEFT;
-            else if (fv.i != ci || fv.j != cj) bits |= REC_BAD;
-            if (bits & REC_BAD) atomicOr(status, ST_INTERNAL);
-            P2GRec r;
-            r.idx = k;
-            r.fui = fu.fi;
-            r.fuj = fu.fj;
-            r.fvi = fv.fi;
-            r.fvj = fv.fj;
-            r.vx = pvx[k];
-            r.vy = pvy[k];
-            r.bits = bits;
-            rec[q] = r;
-        }
-    }
-};
-
-// Grid::addToValueInterpolated's four corners (00, 10, 01, 11) of one record
-// at node (a, b): value * weights into acc, in the reference's order.
-__device__ __forceinline__ void corners(float& acc, float& wacc, int i, int j, bool xc, bool yc, float fi, float fj,
-                                        float value, int a, int b)
-{
-    const int i1 = xc ? i : i + 1, j1 = yc ? j : j + 1;
-    const float omi = fsub(1.0f, fi), omj = fsub(1.0f, fj);
-    const float value_0 = fmul(omj, value), value_1 = fmul(fj, value);
-    // the weight channel splats 1.0: fmul(x, 1.0f) == x
-    if (i == a && j == b) {
-        acc = fadd(acc, fmul(omi, value_0));
-        wacc = fadd(wacc, fmul(omi, omj));
-    }
-    if (i1 == a && j == b) {
-        acc = fadd(acc, fmul(fi, value_0));
-        wacc = fadd(wacc, fmul(fi, omj));
-    }
-    if (i == a && j1 == b) {
-        acc = fadd(acc, fmul(omi, value_1));
-        wacc = fadd(wacc, fmul(omi, fj));
-    }
-    if (i1 == a && j1 == b) {
-        acc = fadd(acc, fmul(fi, value_1));
-        wacc = fadd(wacc, fmul(fi, fj));
-    }
-}
-
-// Node (a, b) of u and of v: merge the records of own cells (a-1..a+1) x
-// (b-1..b+1) but (a+1, b+1) by particle index; u takes those of columns
-// a-1..a, v those of rows b-1..b.
-struct P2GGather
-{
-    const int32_t* bin_start;
-    const P2GRec* rec;
-    float *su, *wu, *sv, *wv;
-    __device__ void operator()(const Seg& s, int64_t c, int a, int b) const
-    {
-        const Geom& g = s.g;
-        int cur[8], end[8], head[8];
-#pragma unroll
-        for (int q = 0; q < 8; ++q) {
-            const int di = q % 3 - 1, dj = q / 3 - 1;  // q = 8 would be (+1, +1): not needed
-            const int ci = a + di, cj = b + dj;
-            if (ci >= 0 && ci < g.nx && cj >= 0 && cj < g.ny) {
-                const int64_t cell = s.co + ci + (int64_t)cj * g.nx;
-                cur[q] = bin_start[cell];
-                end[q] = bin_start[cell + 1];
-            } else {
-                cur[q] = end[q] = 0;
-            }
-            head[q] = cur[q] < end[q] ? rec[cur[q]].idx : INT32_MAX;
-        }
-        float au = 0.0f, awu = 0.0f, av = 0.0f, awv = 0.0f;
-        for (;;) {
-            int best = INT32_MAX, bq = -1;
-#pragma unroll
-            for (int q = 0; q < 8; ++q)
-                if (head[q] < best) {
-                    best = head[q];
-                    bq = q;
-                }
-            if (bq < 0) break;
-            P2GRec r;
-            int di = 0, dj = 0;
-#pragma unroll
-            for (int q = 0; q < 8; ++q)
-                if (q == bq) {
-                    r = rec[cur[q]];
-                    ++cur[q];
-                    head[q] = cur[q] < end[q] ? rec[cur[q]].idx : INT32_MAX;
-                    di = q % 3 - 1;
-                    dj = q / 3 - 1;
-                }
-            const int ci = a + di, cj = b + dj;
-            if (di <= 0)
-                corners(au, awu, ci, (r.bits & REC_U_DOWN) ? cj - 1 : cj, (r.bits & REC_U_XC) != 0,
-                        (r.bits & REC_U_YC) != 0, r.fui, r.fuj, r.vx, a, b);
-            if (dj <= 0)
-                corners(av, awv, (r.bits & REC_V_LEFT) ? ci - 1 : ci, cj, (r.bits & REC_V_XC) != 0,
-                        (r.bits & REC_V_YC) != 0, r.fvi, r.fvj, r.vy, a, b);
-        }
-        const int64_t o = s.co + c;
-        su[o] = au;
-        wu[o] = awu;
-        sv[o] = av;
-        wv[o] = awv;
-    }
-};
-
 }  // namespace
-
-void p2g_binned(const Launch& L, const Domain& d, const float* px, const float* py, const float* pvx,
-                const float* pvy, float* su, float* wu, float* sv, float* wv, unsigned* status, SplatWork& w)
-{
-    const int64_t ncell = d.cells, n = d.parts;
-    cudaMemsetAsync(w.bin_count, 0, sizeof(int32_t) * (size_t)(ncell + 2), L.stream);
-    if (n > 0) {
-        k_p2g_keys<<<domain_blocks(n), DOMAIN_TPB, 0, L.stream>>>(d.one, d.segs, d.segs ? d.pblk : nullptr, n,
-                                                                   (uint32_t)ncell, px, py, w.keys, w.bin_count);
-        L.count();
-    }
-    scan_exclusive_i32(L, w.bin_count, w.bin_start, ncell + 1, w.scan_tmp);
-    if (n > 0) {
-        k_bin_scatter<<<domain_blocks(n), DOMAIN_TPB, 0, L.stream>>>(n, (uint32_t)ncell, w.keys, w.bin_start,
-                                                                      w.bin_count, w.sorted);
-        L.count();
-    }
-    P2GRec* rec = reinterpret_cast<P2GRec*>(w.rec);
-    each_cell(L, d, P2GSortPack{w.bin_start, w.sorted, px, py, pvx, pvy, rec, status});
-    each_cell(L, d, P2GGather{w.bin_start, rec, su, wu, sv, wv});
-}
 
 void group_by_key(const Launch& L, int64_t n, const uint32_t* keys, int64_t nbins, int32_t* bin_count,
                   int32_t* bin_start, int32_t* scan_tmp, int32_t* sorted)
@@ -441,7 +196,6 @@ cudaError_t splat_alloc(SplatWork& w, int64_t items, int64_t cells)
     };
     A((void**)&w.keys, 4 * (size_t)items);
     A((void**)&w.sorted, 4 * (size_t)items);
-    A((void**)&w.rec, 32 * (size_t)items);
     A((void**)&w.bin_count, 4 * bins);
     A((void**)&w.bin_start, 4 * bins);
     A((void**)&w.scan_tmp, 4 * scan_tmp_ints((int64_t)bins));
@@ -456,8 +210,7 @@ cudaError_t splat_alloc(SplatWork& w, int64_t items, int64_t cells)
 
 void splat_free(SplatWork& w)
 {
-    for (void* p : {(void*)w.keys, (void*)w.sorted, (void*)w.rec, (void*)w.bin_count, (void*)w.bin_start,
-                    (void*)w.scan_tmp})
+    for (void* p : {(void*)w.keys, (void*)w.sorted, (void*)w.bin_count, (void*)w.bin_start, (void*)w.scan_tmp})
         cudaFree(p);
     w = SplatWork{};
 }

@@ -23,13 +23,6 @@ void ph_classify(const Launch& L, StepState& st, bool with_counts = false)
 // transferVelocityToGridSpread (src/FluidSolver.cpp:873-919), then the swap.
 void ph_p2g(const Launch& L, StepState& st)
 {
-    if (st.square_cells) {
-        p2g_binned(L, st.d, st.px, st.py, st.pvx, st.pvy, st.acc[0], st.acc[1], st.acc[2], st.acc[3], st.status,
-                   *st.sw);
-        p2g_finish(L, st.d, st.acc[0], st.acc[1], st.acc[2], st.acc[3], st.UB(), st.VB());
-        *st.front ^= 1;
-        return;
-    }
     p2g_positions(L, st.d, st.px, st.py, st.yu, st.xv);
     const float* vu[2] = {st.pvx, nullptr};
     float* ou[2] = {st.acc[0], st.acc[1]};

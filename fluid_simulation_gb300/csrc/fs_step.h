@@ -34,8 +34,6 @@ struct StepState
     float* cg_x;
     int32_t* nfluid;  // [simulation]
     unsigned* warn;
-    unsigned* status;    // device status word (ST_* bits)
-    bool square_cells;   // every simulation has dx == dy: p2g_binned applies
     int32_t* index_tmp;  // scratch of the fluid indexing
     int n_ext;
     // The pressure solve of the assembled systems, and the per-phase timer mark
