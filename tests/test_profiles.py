@@ -36,11 +36,16 @@ def _commands():
 COMMANDS = _commands()
 
 
-def _kernel_names():
+def _kernel_names(demangled=False):
+    """__global__ function names; with demangled names (ncu
+    --kernel-name-base demangled) also the functors the generic kernels take
+    as template arguments."""
     names = set()
     for path in glob.glob(os.path.join(CSRC, "*.cu")) + glob.glob(os.path.join(CSRC, "*.cuh")):
         src = open(path).read()
         names.update(re.findall(r"__global__\s+void\s+(?:__launch_bounds__\([^)]*\)\s+)?(\w+)", src))
+        if demangled:
+            names.update(re.findall(r"^struct\s+(\w+)", src, re.M))
     return names
 
 
@@ -57,7 +62,8 @@ def test_profile_command_is_runnable(fname, cmd, monkeypatch):
         pattern = argv[argv.index("-k") + 1]
         assert pattern.startswith("regex:")
         rx = re.compile(pattern[len("regex:"):])
-        assert any(rx.search(n) for n in _kernel_names()), (fname, pattern)
+        demangled = "--kernel-name-base" in argv and argv[argv.index("--kernel-name-base") + 1] == "demangled"
+        assert any(rx.search(n) for n in _kernel_names(demangled)), (fname, pattern)
     i = argv.index("bench.py")
     assert argv[i - 1] == "python"
     sys.path.insert(0, ROOT)
