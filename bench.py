@@ -172,7 +172,7 @@ def parse():
     ap.add_argument("--no-forms", action="store_true", help="skip the batched and mixed-precision forms")
     ap.add_argument("--batch", type=int, default=512, help="members of the batched form")
     ap.add_argument("--projection-size", type=int, default=4096, help="grid side of the mixed-precision form")
-    ap.add_argument("--projection-methods", default="mixed_multigrid,mixed_f32_dots,mixed_f64_dots,fp64",
+    ap.add_argument("--projection-methods", default="mixed_multigrid,mixed_f32_dots,mixed_ds_dots,mixed_f64_dots,fp64",
                     help="solves of the mixed-precision form, in order (also fp32: the step's Jacobi CG alone)")
     ap.add_argument("--projection-max-iterations", type=int, default=200000,
                     help="CG iteration cap of each projection solve (a small cap makes a short profiling case)")
@@ -497,13 +497,18 @@ def measure_projection(args, local_rank):
     methods = {"mixed_multigrid": (fsg.POISSON_MIXED_MG, fsg.CG_FLOAT),
                "mixed_f32_dots": (fsg.POISSON_MIXED, fsg.CG_FLOAT),
                "mixed_f64_dots": (fsg.POISSON_MIXED, fsg.CG_DOUBLE),
+               "mixed_ds_dots": (fsg.POISSON_MIXED, fsg.CG_DS),
                "fp64": (fsg.POISSON_FP64, fsg.CG_FLOAT),
                "fp32": (fsg.POISSON_FP32, fsg.CG_FLOAT)}
+    sols = {}
     for name in args.projection_methods.split(","):
         method, inner = methods[name]
         st = ps.solve(method, 1e-10, args.projection_max_iterations, inner_tol=1e-3, inner_precision=inner)
+        x = ps.solution()
+        if name in ("mixed_ds_dots", "mixed_f64_dots"):
+            sols[name] = x
         out[name] = {"ms": st["ms"], "residual": st["residual"],
-                     "residual_fp64_host": fp64_residual(labels, rhs, ps.solution()),
+                     "residual_fp64_host": fp64_residual(labels, rhs, x),
                      "outer_iterations": st["outer_iterations"], "inner_iterations": st["inner_iterations"],
                      "cell_solves_per_s": n * n / (st["ms"] / 1000.0)}
     out["residual_fp64_host"] = ("||b - A x|| / ||b|| recomputed in float64 on the host from the returned x "
@@ -514,6 +519,11 @@ def measure_projection(args, local_rank):
                           ("mixed_f64_dots", "speedup_mixed_f64_dots_vs_fp64")):
             if name in out:
                 out[key] = out["fp64"]["ms"] / out[name]["ms"]
+        if "mixed_ds_dots" in out:
+            out["speedup_mixed_ds_dots_vs_fp64"] = out["fp64"]["ms"] / out["mixed_ds_dots"]["ms"]
+    if len(sols) == 2:
+        a, b = sols["mixed_ds_dots"], sols["mixed_f64_dots"]
+        out["ds_vs_f64_dots_max_rel_diff"] = float(np.abs(a - b).max() / np.abs(b).max())
     ps.close()
     out["fp64_direct_512"] = projection_vs_direct(512, methods, args, local_rank)
     return out

@@ -27,7 +27,7 @@ STEP_SEMI_LAGRANGIAN, STEP_PIC, STEP_FLIP, STEP_PICFLIP = range(4)
 (PH_CLASSIFY, PH_P2G, PH_SAVE_PREV, PH_GRAVITY, PH_DIRICHLET, PH_EXTEND, PH_PRESSURE, PH_SAVE_DIFF,
  PH_G2P_PICFLIP, PH_G2P_PIC, PH_G2P_FLIP, PH_ADVECT_SAFE, PH_ADVECT, PH_SL_VELOCITY, PH_SL_PARTICLES,
  PH_SWAP) = range(16)
-CG_FLOAT, CG_DOUBLE = 0, 1
+CG_FLOAT, CG_DOUBLE, CG_DS = 0, 1, 2
 POISSON_FP32, POISSON_FP64, POISSON_MIXED, POISSON_MGPCG, POISSON_MIXED_MG = 0, 1, 2, 3, 4
 SOLVER_JACOBI_PCG, SOLVER_MGPCG = 0, 1
 INTEGRATOR_EULER, INTEGRATOR_RK2, INTEGRATOR_RK3 = 0, 1, 2
@@ -254,7 +254,7 @@ class FluidSim:
         self._check(self.lib.fs_set_cg(self.h, float(tol), int(maxit)))
 
     def set_cg_precision(self, precision: int) -> None:
-        """CG_FLOAT (0, the reference's precision) or CG_DOUBLE (1)."""
+        """CG_FLOAT (0, the reference's precision), CG_DOUBLE (1) or CG_DS (2, double-single)."""
         self._check(self.lib.fs_set_cg_precision(self.h, int(precision)))
 
     def set_pressure_solver(self, solver: int) -> None:

@@ -501,7 +501,7 @@ int fs_create(const fs_config* cfg, fs_handle** out)
     h->gy = cfg->gravity_y;
     h->cg_tol = cfg->cg_tolerance;
     h->cg_maxit = cfg->cg_max_iterations;
-    h->cg_fp64 = cfg->cg_precision == FS_CG_DOUBLE ? 1 : 0;
+    h->cg_fp64 = cfg->cg_precision == FS_CG_DOUBLE ? 1 : cfg->cg_precision == FS_CG_DS ? 2 : 0;
     h->n_ext = cfg->extension_iterations;
     // Matrix coefficients through double pow() as in src/FluidSolver.cpp:381-410.
     const double dx2 = std::pow((double)g.dx, 2);
@@ -634,9 +634,9 @@ int fs_set_cg(fs_handle* h, double tol, int maxit)
 
 int fs_set_cg_precision(fs_handle* h, int precision)
 {
-    if (!h || (precision != FS_CG_FLOAT && precision != FS_CG_DOUBLE))
+    if (!h || (precision != FS_CG_FLOAT && precision != FS_CG_DOUBLE && precision != FS_CG_DS))
         return h ? fail(h, FS_ERR_INVALID_ARGUMENT, "unknown CG precision") : FS_ERR_INVALID_ARGUMENT;
-    const int fp64 = precision == FS_CG_DOUBLE ? 1 : 0;
+    const int fp64 = precision == FS_CG_DOUBLE ? 1 : precision == FS_CG_DS ? 2 : 0;
     if (fp64 != h->cg_fp64) clear_graphs(h);
     h->cg_fp64 = fp64;
     return FS_OK;

@@ -616,6 +616,11 @@ int fs_batch_create(int n, const fs_config* cfgs, fs_batch** out)
     b->pending.resize(n);
     b->has_pending.assign(n, 0);
     b->n_ext = cfgs[0].extension_iterations;
+    if (cfgs[0].cg_precision == FS_CG_DS) {
+        g_batch_error = "double-single CG dot products are not available for batches";
+        delete b;
+        return FS_ERR_INVALID_ARGUMENT;
+    }
     b->fp64 = cfgs[0].cg_precision == FS_CG_DOUBLE ? 1 : 0;
     std::vector<int2> cblk;
     std::vector<CgSystem> sys(n);

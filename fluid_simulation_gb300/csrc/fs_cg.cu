@@ -108,6 +108,8 @@ struct Smem
 template <typename R> struct Ar;
 template <> struct Ar<float>
 {
+    using Acc = float;
+    using Elem = float;
     static __device__ __forceinline__ float add(float a, float b) { return fadd(a, b); }
     static __device__ __forceinline__ float mul(float a, float b) { return fmul(a, b); }
     static __device__ __forceinline__ float prod(float a, float b) { return fmul(a, b); }
@@ -119,6 +121,8 @@ template <> struct Ar<float>
 };
 template <> struct Ar<double>
 {
+    using Acc = double;
+    using Elem = double;
     static __device__ __forceinline__ double add(double a, double b) { return dadd(a, b); }
     static __device__ __forceinline__ double mul(double a, double b) { return dmul(a, b); }
     static __device__ __forceinline__ double prod(float a, float b) { return dmul((double)a, (double)b); }
@@ -128,6 +132,44 @@ template <> struct Ar<double>
     static __device__ __forceinline__ double& lvlA(Smem& s, int a, int k) { return s.lvlA[a][k]; }
     static __device__ __forceinline__ double& lvlB(Smem& s, int a, int k) { return s.lvlB[a][k]; }
 };
+
+// Double-single dot products (FS_CG_DS): each float*float product exactly,
+// as an unevaluated pair of floats (fmul, then fmaf for its rounding error),
+// the first tree level -- the 32 elements of one warp -- added in such pairs
+// (TwoSum of the high parts, then the error and both low parts added in float;
+// the pair is not renormalised between levels), converted to double exactly
+// at the warp's root, and every
+// level above in double, as FS_CG_DOUBLE.  The pairs carry about 48 bits, so
+// the sums stay close to FP64 while GB300's FP64 pipe, where the double
+// variant spends its time, does almost nothing per element.
+struct ds
+{
+    float hi, lo;
+};
+__device__ __forceinline__ ds ds_prod(float a, float b)
+{
+    const float p = fmul(a, b);
+    return ds{p, __fmaf_rn(a, b, -p)};
+}
+__device__ __forceinline__ ds ds_add(ds a, ds b)
+{
+    const float s = fadd(a.hi, b.hi);
+    const float v = fsub(s, a.hi);
+    float e = fadd(fsub(a.hi, fsub(s, v)), fsub(b.hi, v));
+    e = fadd(e, a.lo);
+    e = fadd(e, b.lo);
+    return ds{s, e};
+}
+struct DSD
+{
+};
+template <> struct Ar<DSD> : Ar<double>
+{
+    using Elem = ds;
+    static __device__ __forceinline__ ds prod(float a, float b) { return ds_prod(a, b); }
+};
+template <typename R> using Acc = typename Ar<R>::Acc;
+template <typename R> using Elem = typename Ar<R>::Elem;
 
 template <typename R>
 __device__ __forceinline__ R warp_tree(R v)
@@ -204,14 +246,30 @@ struct ClusterSync
     }
 };
 
+// The level-1 tree of one warp's elements, as an accumulation value.
+template <typename R>
+__device__ __forceinline__ Acc<R> elem_tree(Elem<R> v)
+{
+    if constexpr (std::is_same<R, DSD>::value) {
+#pragma unroll
+        for (int s = 16; s >= 1; s >>= 1) {
+            const ds o{__shfl_down_sync(0xffffffffu, v.hi, s), __shfl_down_sync(0xffffffffu, v.lo, s)};
+            v = ds_add(v, o);
+        }
+        return dadd((double)v.hi, (double)v.lo);
+    } else {
+        return warp_tree<R>(v);
+    }
+}
+
 // Level-1 (warp) tree of NV values for chunk slot `slot`; lane 0 keeps it.
 template <typename R, int NV>
-__device__ __forceinline__ void level1(const R (&v)[NV], int slot, Smem& sm)
+__device__ __forceinline__ void level1(const Elem<R> (&v)[NV], int slot, Smem& sm)
 {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
     for (int k = 0; k < NV; ++k) {
-        const R t = warp_tree<R>(v[k]);
+        const Acc<R> t = elem_tree<R>(v[k]);
         if (lane == 0) Ar<R>::red(sm, slot, warp, k) = t;
     }
 }
@@ -222,11 +280,11 @@ __device__ __forceinline__ void level2(const CgArgs& a, int buf, int chunk0, int
 {
     __syncthreads();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    R* part = reinterpret_cast<R*>(a.partials);
+    Acc<R>* part = reinterpret_cast<Acc<R>*>(a.partials);
     if (warp < nslots) {
 #pragma unroll
         for (int k = 0; k < NV; ++k) {
-            const R t = warp_tree<R>(Ar<R>::red(sm, warp, lane, k));
+            const Acc<R> t = warp_tree<Acc<R>>(Ar<R>::red(sm, warp, lane, k));
             if (lane == 0) __stcg(&part[((size_t)buf * 2 + k) * a.max_chunks + chunk0 + warp], t);
         }
     }
@@ -235,10 +293,10 @@ __device__ __forceinline__ void level2(const CgArgs& a, int buf, int chunk0, int
 
 // Levels 3+: every CTA reduces all chunk partials of buffer buf.
 template <typename R, int NV>
-__device__ __forceinline__ void reduce_all(const CgArgs& a, int buf, int nchunks, Smem& sm, R (&out)[NV])
+__device__ __forceinline__ void reduce_all(const CgArgs& a, int buf, int nchunks, Smem& sm, Acc<R> (&out)[NV])
 {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const R* src = reinterpret_cast<const R*>(a.partials) + (size_t)buf * 2 * a.max_chunks;
+    const Acc<R>* src = reinterpret_cast<const Acc<R>*>(a.partials) + (size_t)buf * 2 * a.max_chunks;
     if (nchunks == 1) {
 #pragma unroll
         for (int k = 0; k < NV; ++k) out[k] = __ldcg(&src[(size_t)k * a.max_chunks]);
@@ -253,8 +311,8 @@ __device__ __forceinline__ void reduce_all(const CgArgs& a, int buf, int nchunks
             const int e = warp * 32 + lane;
 #pragma unroll
             for (int k = 0; k < NV; ++k) {
-                const R v = e < nchunks ? __ldcg(&src[(size_t)k * a.max_chunks + e]) : R(0);
-                const R t = warp_tree<R>(v);
+                const Acc<R> v = e < nchunks ? __ldcg(&src[(size_t)k * a.max_chunks + e]) : Acc<R>(0);
+                const Acc<R> t = warp_tree<Acc<R>>(v);
                 if (lane == 0) Ar<R>::lvlB(sm, warp, k) = t;
             }
         }
@@ -264,7 +322,7 @@ __device__ __forceinline__ void reduce_all(const CgArgs& a, int buf, int nchunks
             if (n == 1) {
                 out[k] = Ar<R>::lvlB(sm, 0, k);
             } else {
-                const R t = warp_tree<R>(lane < n ? Ar<R>::lvlB(sm, lane, k) : R(0));
+                const Acc<R> t = warp_tree<Acc<R>>(lane < n ? Ar<R>::lvlB(sm, lane, k) : Acc<R>(0));
                 out[k] = __shfl_sync(0xffffffffu, t, 0);
             }
         }
@@ -274,8 +332,8 @@ __device__ __forceinline__ void reduce_all(const CgArgs& a, int buf, int nchunks
         const int e = g * 32 + lane;
 #pragma unroll
         for (int k = 0; k < NV; ++k) {
-            const R v = e < nchunks ? __ldcg(&src[(size_t)k * a.max_chunks + e]) : R(0);
-            const R t = warp_tree<R>(v);
+            const Acc<R> v = e < nchunks ? __ldcg(&src[(size_t)k * a.max_chunks + e]) : Acc<R>(0);
+            const Acc<R> t = warp_tree<Acc<R>>(v);
             if (lane == 0) Ar<R>::lvlA(sm, g, k) = t;
         }
     }
@@ -287,10 +345,10 @@ __device__ __forceinline__ void reduce_all(const CgArgs& a, int buf, int nchunks
             const int e = warp * 32 + lane;
 #pragma unroll
             for (int k = 0; k < NV; ++k) {
-                R v;
-                if (inA) v = e < n ? Ar<R>::lvlA(sm, e, k) : R(0);
-                else v = e < n ? Ar<R>::lvlB(sm, e, k) : R(0);
-                const R t = warp_tree<R>(v);
+                Acc<R> v;
+                if (inA) v = e < n ? Ar<R>::lvlA(sm, e, k) : Acc<R>(0);
+                else v = e < n ? Ar<R>::lvlB(sm, e, k) : Acc<R>(0);
+                const Acc<R> t = warp_tree<Acc<R>>(v);
                 if (lane == 0) {
                     if (inA) Ar<R>::lvlB(sm, warp, k) = t;
                     else Ar<R>::lvlA(sm, warp, k) = t;
@@ -311,20 +369,20 @@ __device__ __forceinline__ void reduce_all(const CgArgs& a, int buf, int nchunks
 // level2 + reduce_all (a lone chunk's partial is the result as it stands),
 // without the round trip of the partials through global memory.
 template <typename R, int NV>
-__device__ __forceinline__ void local_reduce(int nchunks, Smem& sm, R (&out)[NV])
+__device__ __forceinline__ void local_reduce(int nchunks, Smem& sm, Acc<R> (&out)[NV])
 {
     __syncthreads();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     if (warp == 0) {
 #pragma unroll
         for (int k = 0; k < NV; ++k) {
-            R mine = R(0);
+            Acc<R> mine = Acc<R>(0);
             for (int s = 0; s < nchunks; ++s) {
-                R t = warp_tree<R>(Ar<R>::red(sm, s, lane, k));
+                Acc<R> t = warp_tree<Acc<R>>(Ar<R>::red(sm, s, lane, k));
                 t = __shfl_sync(0xffffffffu, t, 0);
                 if (lane == s) mine = t;
             }
-            const R res = nchunks == 1 ? mine : warp_tree<R>(lane < nchunks ? mine : R(0));
+            const Acc<R> res = nchunks == 1 ? mine : warp_tree<Acc<R>>(lane < nchunks ? mine : Acc<R>(0));
             if (lane == 0) Ar<R>::lvlB(sm, 0, k) = res;
         }
     }
@@ -366,7 +424,7 @@ __device__ __forceinline__ void cg_stream(const CgArgs& a, Smem& sm, int nf, int
         for (int sl = 0; sl < nslot; ++sl) {
             const int s = base + sl;
             const int e = (c0 + s) * CHUNK + tid;
-            R v[2] = {R(0), R(0)};
+            Elem<R> v[2] = {Elem<R>(), Elem<R>()};
             if (e < nf) {
                 const float r = a.b[e];
                 const uint8_t fl = a.flags[e];
@@ -381,20 +439,20 @@ __device__ __forceinline__ void cg_stream(const CgArgs& a, Smem& sm, int nf, int
         }
         if (!local) level2<R, 2>(a, 0, c0 + base, nslot, sm);
     }
-    R red2[2];
+    Acc<R> red2[2];
     if (local) {
         local_reduce<R, 2>(nchunks, sm, red2);
     } else {
         if (!sync.barrier(a, sm)) return;
         reduce_all<R, 2>(a, 0, nchunks, sm, red2);
     }
-    const R bb = red2[0];
-    R rz = red2[1];
-    R rr = bb;
+    const Acc<R> bb = red2[0];
+    Acc<R> rz = red2[1];
+    Acc<R> rr = bb;
     int iters = 0;
-    bool done = bb == R(0);
-    const R tolr = (R)a.tol;
-    R thr = Ar<R>::mul(Ar<R>::mul(tolr, tolr), bb);
+    bool done = bb == Acc<R>(0);
+    const Acc<R> tolr = (Acc<R>)a.tol;
+    Acc<R> thr = Ar<R>::mul(Ar<R>::mul(tolr, tolr), bb);
     if (thr < Ar<R>::tiny()) thr = Ar<R>::tiny();
     if (!done && rr < thr) done = true;
 
@@ -407,7 +465,7 @@ __device__ __forceinline__ void cg_stream(const CgArgs& a, Smem& sm, int nf, int
             for (int sl = 0; sl < nslot; ++sl) {
                 const int s = base + sl;
                 const int e = (c0 + s) * CHUNK + tid;
-                R v[1] = {R(0)};
+                Elem<R> v[1] = {Elem<R>()};
                 if (e < nf) {
                     const float pe = remote_p(a, e, first, beta);
                     const unsigned fl = a.flags[e];
@@ -425,7 +483,7 @@ __device__ __forceinline__ void cg_stream(const CgArgs& a, Smem& sm, int nf, int
             }
             if (!local) level2<R, 1>(a, 1, c0 + base, nslot, sm);
         }
-        R red1[1];
+        Acc<R> red1[1];
         if (local) {
             local_reduce<R, 1>(nchunks, sm, red1);
         } else {
@@ -440,7 +498,7 @@ __device__ __forceinline__ void cg_stream(const CgArgs& a, Smem& sm, int nf, int
             for (int sl = 0; sl < nslot; ++sl) {
                 const int s = base + sl;
                 const int e = (c0 + s) * CHUNK + tid;
-                R v[2] = {R(0), R(0)};
+                Elem<R> v[2] = {Elem<R>(), Elem<R>()};
                 if (e < nf) {
                     const float pn = remote_p(a, e, first, beta);
                     float x = __ldcg(&a.x[e]);
@@ -634,7 +692,7 @@ __device__ __forceinline__ void cg_pipe(const CgArgs& a, Smem& sm, unsigned char
         const int nslot = min(32, kb - base);
         for (int sl = 0; sl < nslot; ++sl) {
             const int e = (c0 + base + sl) * CHUNK + tid;
-            R v[2] = {R(0), R(0)};
+            Elem<R> v[2] = {Elem<R>(), Elem<R>()};
             if (e < nf) {
                 const float r = a.b[e];
                 const uint8_t fl = a.flags[e];
@@ -650,19 +708,19 @@ __device__ __forceinline__ void cg_pipe(const CgArgs& a, Smem& sm, unsigned char
         level2<R, 2>(a, 0, c0 + base, nslot, sm);
     }
     prologue_a();
-    R red2[2];
+    Acc<R> red2[2];
     if (!sync.barrier(a, sm)) {
         cp_wait_all();
         return;
     }
     reduce_all<R, 2>(a, 0, nchunks, sm, red2);
-    const R bb = red2[0];
-    R rz = red2[1];
-    R rr = bb;
+    const Acc<R> bb = red2[0];
+    Acc<R> rz = red2[1];
+    Acc<R> rr = bb;
     int iters = 0;
-    bool done = bb == R(0);
-    const R tolr = (R)a.tol;
-    R thr = Ar<R>::mul(Ar<R>::mul(tolr, tolr), bb);
+    bool done = bb == Acc<R>(0);
+    const Acc<R> tolr = (Acc<R>)a.tol;
+    Acc<R> thr = Ar<R>::mul(Ar<R>::mul(tolr, tolr), bb);
     if (thr < Ar<R>::tiny()) thr = Ar<R>::tiny();
     if (!done && rr < thr) done = true;
 
@@ -699,7 +757,7 @@ __device__ __forceinline__ void cg_pipe(const CgArgs& a, Smem& sm, unsigned char
             if (e < nf) pe = pnew(ez[lane], ez[32 + lane]);
             float pl = __shfl_up_sync(0xffffffffu, pe, 1);
             float pr = __shfl_down_sync(0xffffffffu, pe, 1);
-            R v[1] = {R(0)};
+            Elem<R> v[1] = {Elem<R>()};
             if (e < nf) {
                 const unsigned fl = en[512 + lane];
                 const int dn = reinterpret_cast<const int*>(en + 256)[lane];
@@ -729,7 +787,7 @@ __device__ __forceinline__ void cg_pipe(const CgArgs& a, Smem& sm, unsigned char
         static_assert(PA_PEEL == 3, "three peeled slots above");
         for (int k = PA_PEEL; k < kb; ++k) step_a(k, IntC<pa_wait1(PA_PEEL)>{}, IntC<pa_wait2(PA_PEEL)>{});
         prologue_b();
-        R red1[1];
+        Acc<R> red1[1];
         if (!sync.barrier(a, sm)) {
             cp_wait_all();
             return;
@@ -749,7 +807,7 @@ __device__ __forceinline__ void cg_pipe(const CgArgs& a, Smem& sm, unsigned char
             const float* en = reinterpret_cast<const float*>(wb + ob);
             const unsigned char* efl = wb + ob + 640;
             const int e = (c0 + k) * CHUNK + warp * 32 + lane;
-            R v[2] = {R(0), R(0)};
+            Elem<R> v[2] = {Elem<R>(), Elem<R>()};
             if (e < nf) {
                 const float pn = pnew(en[lane], en[32 + lane]);
                 float x = en[64 + lane];
@@ -898,7 +956,7 @@ __device__ __forceinline__ bool cg_lean(const CgArgs& a, Smem& sm, unsigned char
         if constexpr (PREG) pn[s] = 0.0f;
         if (s < kb) {
             const int e = (c0 + s) * CHUNK + tid;
-            R v[2] = {R(0), R(0)};
+            Elem<R> v[2] = {Elem<R>(), Elem<R>()};
             if (e < nf) {
                 const float rb = a.b[e];
                 const unsigned fl = a.flags[e];
@@ -943,7 +1001,7 @@ __device__ __forceinline__ bool cg_lean(const CgArgs& a, Smem& sm, unsigned char
         }
     };
     if (!local) level2<R, 2>(a, 0, c0, kb, sm);
-    R red2[2];
+    Acc<R> red2[2];
     if (local) {
         local_reduce<R, 2>(nchunks, sm, red2);
     } else {
@@ -951,13 +1009,13 @@ __device__ __forceinline__ bool cg_lean(const CgArgs& a, Smem& sm, unsigned char
         prefetch(false);
         reduce_all<R, 2>(a, 0, nchunks, sm, red2);
     }
-    const R bb = red2[0];
-    R rz = red2[1];
-    R rr = bb;
+    const Acc<R> bb = red2[0];
+    Acc<R> rz = red2[1];
+    Acc<R> rr = bb;
     int iters = 0;
-    bool done = bb == R(0);
-    const R tolr = (R)a.tol;
-    R thr = Ar<R>::mul(Ar<R>::mul(tolr, tolr), bb);
+    bool done = bb == Acc<R>(0);
+    const Acc<R> tolr = (Acc<R>)a.tol;
+    Acc<R> thr = Ar<R>::mul(Ar<R>::mul(tolr, tolr), bb);
     if (thr < Ar<R>::tiny()) thr = Ar<R>::tiny();
     if (!done && rr < thr) done = true;
 
@@ -988,7 +1046,7 @@ __device__ __forceinline__ bool cg_lean(const CgArgs& a, Smem& sm, unsigned char
 #pragma unroll
         for (int s = 0; s < K; ++s) {
             if (s < kb) {
-                R v[1] = {R(0)};
+                Elem<R> v[1] = {Elem<R>()};
                 if ((c0 + s) * CHUNK + tid < nf) {
                     const float ps = PREG ? pn[s] : pv[s * CHUNK + tid];
                     float acc = 0.0f;
@@ -1021,7 +1079,7 @@ __device__ __forceinline__ bool cg_lean(const CgArgs& a, Smem& sm, unsigned char
             }
         }
         if (!local) level2<R, 1>(a, 1, c0, kb, sm);
-        R red1[1];
+        Acc<R> red1[1];
         if (local) {
             local_reduce<R, 1>(nchunks, sm, red1);
         } else {
@@ -1035,7 +1093,7 @@ __device__ __forceinline__ bool cg_lean(const CgArgs& a, Smem& sm, unsigned char
         for (int s = 0; s < K; ++s) {
             if (s < kb) {
                 const int e = (c0 + s) * CHUNK + tid;
-                R v[2] = {R(0), R(0)};
+                Elem<R> v[2] = {Elem<R>(), Elem<R>()};
                 if (e < nf) {
                     const float ps = PREG ? pn[s] : pv[s * CHUNK + tid];
                     const int l = s * CHUNK + tid;
@@ -1105,10 +1163,11 @@ __global__ void k_cg_route(const int32_t* __restrict__ nfluid, int max_chunks, i
     route[1] = large ? nf : 0;
 }
 
-// Large systems with FP32 dot products, on the system k_cg_route gave it
-// (none: return without a result; k_cg wrote it): up to KBIG chunks per CTA
-// in registers and shared memory, from PIPE_MIN_CHUNKS on streamed through
-// the cp.async pipeline.
+// Large systems with float (R = float) or double-single (R = DSD) dot
+// products, on the system k_cg_route gave it (none: return without a result;
+// k_cg wrote it): up to KBIG chunks per CTA in registers and shared memory,
+// from PIPE_MIN_CHUNKS on streamed through the cp.async pipeline.
+template <typename R>
 __global__ void __launch_bounds__(CG_THREADS, 1) k_cg_large(CgArgs a)
 {
     __shared__ Smem sm;
@@ -1126,9 +1185,9 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg_large(CgArgs a)
     __syncthreads();
     GridSync sync{true, 0u, active};
     if (per_cta <= KBIG) {
-        if (!cg_lean<KBIG, float>(a, sm, dyn, nf, nchunks, sync)) cg_stream<float>(a, sm, nf, nchunks, sync);
+        if (!cg_lean<KBIG, R>(a, sm, dyn, nf, nchunks, sync)) cg_stream<R>(a, sm, nf, nchunks, sync);
     } else {
-        cg_pipe<float>(a, sm, dyn, nf, nchunks, sync);
+        cg_pipe<R>(a, sm, dyn, nf, nchunks, sync);
     }
 }
 
@@ -1234,23 +1293,22 @@ int cg_prepare(CgWork& w, int device)
 {
     int sms = 0, per_sm = 0;
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) return -1;
-    if (cudaFuncSetAttribute(k_cg<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)DYN_BYTES) !=
-            cudaSuccess ||
-        cudaFuncSetAttribute(k_cg<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)DYN_BYTES) !=
+    for (const void* f : {(const void*)k_cg<float>, (const void*)k_cg<double>, (const void*)k_cg<DSD>})
+        if (cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)DYN_BYTES) != cudaSuccess)
+            return -1;
+    for (const void* f : {(const void*)k_cg_large<float>, (const void*)k_cg_large<DSD>})
+        if (cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)LARGE_DYN_BYTES) !=
             cudaSuccess)
-        return -1;
-    if (cudaFuncSetAttribute(k_cg_large, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)LARGE_DYN_BYTES) !=
-        cudaSuccess)
-        return -1;
-    for (const void* f : {(const void*)k_cg<float>, (const void*)k_cg<double>}) {
+            return -1;
+    for (const void* f : {(const void*)k_cg<float>, (const void*)k_cg<double>, (const void*)k_cg<DSD>}) {
         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, f, CG_THREADS, DYN_BYTES) != cudaSuccess)
             return -1;
         if (per_sm < 1) return -1;
     }
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cg_large, CG_THREADS, LARGE_DYN_BYTES) !=
-            cudaSuccess ||
-        per_sm < 1)
-        return -1;
+    for (const void* f : {(const void*)k_cg_large<float>, (const void*)k_cg_large<DSD>})
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, f, CG_THREADS, LARGE_DYN_BYTES) != cudaSuccess ||
+            per_sm < 1)
+            return -1;
     w.grid = sms;  // one CTA per SM: fewer barrier arrivals
     return 0;
 }
@@ -1288,10 +1346,13 @@ void cg_solve(const Launch& L, CgWork& w, const int32_t* nfluid, const float* b,
     a.dyn_bytes = (int)DYN_BYTES;
     cudaMemsetAsync(w.barrier, 0, sizeof(unsigned), L.stream);
     void* args[] = {&a};
-    const void* kernel = fp64 ? (const void*)k_cg<double> : (const void*)k_cg<float>;
+    const void* kernel = fp64 == 2 ? (const void*)k_cg<DSD>
+                         : fp64  ? (const void*)k_cg<double>
+                                 : (const void*)k_cg<float>;
     // Arrays with room for more than KREG chunks per CTA: k_cg_route decides
-    // on the device which of k_cg and k_cg_large solves.
-    const bool large = !fp64 && w.route && (a.max_chunks + w.grid - 1) / w.grid > KREG;
+    // on the device which of k_cg and k_cg_large solves (float and
+    // double-single dots; double dots gain nothing from it).
+    const bool large = fp64 != 1 && w.route && (a.max_chunks + w.grid - 1) / w.grid > KREG;
     if (large) {
         k_cg_route<<<1, 1, 0, L.stream>>>(nfluid, a.max_chunks, w.grid, w.route);
         L.count();
@@ -1302,8 +1363,8 @@ void cg_solve(const Launch& L, CgWork& w, const int32_t* nfluid, const float* b,
     if (large) {
         a.nfluid = w.route + 1;
         a.dyn_bytes = (int)LARGE_DYN_BYTES;
-        cudaLaunchCooperativeKernel((const void*)k_cg_large, dim3(w.grid), dim3(CG_THREADS), args,
-                                    LARGE_DYN_BYTES, L.stream);
+        cudaLaunchCooperativeKernel(fp64 == 2 ? (const void*)k_cg_large<DSD> : (const void*)k_cg_large<float>,
+                                    dim3(w.grid), dim3(CG_THREADS), args, LARGE_DYN_BYTES, L.stream);
         L.count();
     }
 }

@@ -203,7 +203,9 @@ struct CgWork
     uint64_t wait_ns = 2000000000ull;    // bound of every device-side wait
 };
 int cg_prepare(CgWork& w, int device);  // picks the cooperative grid size
-// fp64: 0 = float dot products (the reference's precision), 1 = double.
+// fp64: 0 = float dot products (the reference's precision), 1 = double,
+// 2 = double-single (FS_CG_DS: compensated float pairs within each warp,
+// double above).
 void cg_solve(const Launch& L, CgWork& w, const int32_t* nfluid, const float* b, const float* diag_tab,
               const int32_t* down, const int32_t* up, const uint8_t* flags, float off, double tol, int maxit,
               int fp64, unsigned* status);

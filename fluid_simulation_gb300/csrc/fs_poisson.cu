@@ -493,7 +493,7 @@ int solve_impl(fs_poisson* p, int method, double tol, int max_iterations, double
     fs_poisson_stats st{};
     cudaMemsetAsync(p->status, 0, 4, p->stream);
     cudaEventRecord(p->ev[0], p->stream);
-    const int fp64dots = inner_precision == FS_CG_DOUBLE ? 1 : 0;
+    const int fp64dots = inner_precision == FS_CG_DOUBLE ? 1 : inner_precision == FS_CG_DS ? 2 : 0;
     const bool use_mg = method == FS_POISSON_MGPCG || method == FS_POISSON_MIXED_MG;
     if (use_mg) {
         if (!p->mg) {

@@ -102,6 +102,13 @@ extern "C" {
  * one fixed summation order, so results are reproducible run to run. */
 #define FS_CG_FLOAT 0
 #define FS_CG_DOUBLE 1
+/* Double-single: each float*float product exact as a pair of floats (product
+ * and its fmaf error), the 32 products of each warp summed in such pairs
+ * (TwoSum of the high parts, the low parts added to its error), every level
+ * above in double;
+ * no counterpart in the reference.  Steps and fs_poisson_solve's inner CG;
+ * not batches. */
+#define FS_CG_DS 2
 
 /* Timed phases reported in fs_step_stats.ms_phase when timing is enabled. */
 #define FS_T_CLASSIFY 0   /* labels */

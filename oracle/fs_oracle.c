@@ -44,7 +44,7 @@ struct fso_sim
     int n_ext;
     double cg_tol;
     int cg_maxit;
-    int cg_double;        /* dot-product precision: 0 float, 1 double */
+    int cg_double;        /* dot-product precision: 0 float, 1 double, 2 double-single */
     int use_stock;
 
     float* u[2];
@@ -258,7 +258,7 @@ void fso_set_cg(fso_sim* s, double tol, int maxit)
     s->cg_tol = tol;
     s->cg_maxit = maxit;
 }
-void fso_set_cg_precision(fso_sim* s, int precision) { s->cg_double = precision != 0; }
+void fso_set_cg_precision(fso_sim* s, int precision) { s->cg_double = precision; }
 void fso_set_gravity(fso_sim* s, float gx, float gy)
 {
     s->gx = gx;
@@ -586,6 +586,59 @@ static double dot_d(fso_sim* s, const float* a, const float* b, int n)
     return rsum32(s->cg_acc, n);
 }
 
+/* Double-single dot product (the GPU's FS_CG_DS; no counterpart in the
+ * reference): each float*float product exactly as a float pair (the product
+ * and its fmaf error), each group of 32 consecutive elements summed in such
+ * pairs along the 32-ary stride-halving tree -- TwoSum of the high parts, the
+ * error and both low parts added to it in float, no renormalisation -- each
+ * group's pair converted to double (high + low, exact), and the groups summed
+ * by rsum32. */
+typedef struct {
+    float hi, lo;
+} fso_ds;
+
+static fso_ds ds_prod(float a, float b)
+{
+    fso_ds r;
+    r.hi = a * b;
+    r.lo = fmaf(a, b, -r.hi);
+    return r;
+}
+
+static fso_ds ds_add(fso_ds a, fso_ds b)
+{
+    const float s = a.hi + b.hi;
+    const float v = s - a.hi;
+    float e = (a.hi - (s - v)) + (b.hi - v);
+    e = e + a.lo;
+    e = e + b.lo;
+    fso_ds r;
+    r.hi = s;
+    r.lo = e;
+    return r;
+}
+
+static double dot_ds(fso_sim* s, const float* a, const float* b, int n)
+{
+    const int groups = (n + 31) / 32;
+    for (int g = 0; g < groups; ++g) {
+        fso_ds t[32];
+        for (int l = 0; l < 32; ++l) {
+            const int k = g * 32 + l;
+            if (k < n) {
+                t[l] = ds_prod(a[k], b[k]);
+            } else {
+                t[l].hi = 0.0f;
+                t[l].lo = 0.0f;
+            }
+        }
+        for (int st = 16; st >= 1; st >>= 1)
+            for (int l = 0; l < st; ++l) t[l] = ds_add(t[l], t[l + st]);
+        s->cg_acc[g] = (double)t[0].hi + (double)t[0].lo;
+    }
+    return rsum32(s->cg_acc, groups);
+}
+
 /* Float products summed in float (the precision of Eigen's VectorXf::dot). */
 static float dot_f(fso_sim* s, const float* a, const float* b, int n)
 {
@@ -664,7 +717,8 @@ static void cg_solve(fso_sim* s, int n, float off)
     }
     s->cg_iters = 0;
     s->cg_error = 0.0;
-    if (s->cg_double) FSO_CG_BODY(double, dot_d, DBL_MIN);
+    if (s->cg_double == 2) FSO_CG_BODY(double, dot_ds, DBL_MIN);
+    else if (s->cg_double) FSO_CG_BODY(double, dot_d, DBL_MIN);
     else FSO_CG_BODY(float, dot_f, FLT_MIN);
 }
 
@@ -1164,7 +1218,7 @@ int fso_poisson_solve(int nx, int ny, float lx, float ly, const uint8_t* labels,
             if (k >= 0) b[k] = rhs[IDX(s, i, j)];
         }
     int outer = 0, inner = 0;
-    s->cg_double = inner_precision != 0;
+    s->cg_double = inner_precision;
     if (method == 0) { /* float CG */
         for (int k = 0; k < nf; ++k) s->cg_b[k] = (float)b[k];
         s->cg_tol = tol;

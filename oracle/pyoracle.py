@@ -151,7 +151,7 @@ class OracleSim:
         self.lib.fso_set_cg(self.h, float(tol), int(maxit))
 
     def set_cg_precision(self, precision: int) -> None:
-        """0: float dot products (the reference's precision); 1: double."""
+        """0: float dot products (the reference's precision); 1: double; 2: double-single."""
         self.lib.fso_set_cg_precision(self.h, int(precision))
 
     def set_gravity(self, gx: float, gy: float) -> None:

@@ -159,7 +159,7 @@ def test_obstacle_and_gravity_override():
     assert_same(g.state(), o.state(), where="obstacle")
 
 
-@pytest.mark.parametrize("precision", [fsg.CG_FLOAT, fsg.CG_DOUBLE])
+@pytest.mark.parametrize("precision", [fsg.CG_FLOAT, fsg.CG_DOUBLE, fsg.CG_DS])
 def test_large_grid_one_step_bit_exact(precision):
     """512x512 dam break with an obstacle (~430k particles), one full step:
     multi-CTA CG with grid barriers, register-resident CG state (at most 4

@@ -60,7 +60,7 @@ def test_restatement_residuals(method):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("shape", [(64, 64), (200, 130)])
-@pytest.mark.parametrize("method,inner_precision", [(0, 0), (0, 1), (1, 0), (2, 0), (2, 1)])
+@pytest.mark.parametrize("method,inner_precision", [(0, 0), (0, 1), (0, 2), (1, 0), (2, 0), (2, 1), (2, 2)])
 def test_gpu_matches_restatement_bit_exact(shape, method, inner_precision):
     import fluid_simulation_gb300 as fsg
     from fluid_simulation_gb300 import build as fsbuild
@@ -117,13 +117,15 @@ _LARGE_CASES = [
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("precision", [0, 2], ids=["float_dots", "ds_dots"])
 @pytest.mark.parametrize("case,make,n_fluid,per_cta,tol,maxit,iters", _LARGE_CASES, ids=[c[0] for c in _LARGE_CASES])
-def test_gpu_large_system_forms_match_restatement(case, make, n_fluid, per_cta, tol, maxit, iters):
+def test_gpu_large_system_forms_match_restatement(case, make, n_fluid, per_cta, tol, maxit, iters, precision):
     """Systems of more than 8 chunks of 1024 cells per CTA with float dot
     products are solved by k_cg_large: up to 12 chunks per CTA in the
     register-resident form with 4-byte rows (a CTA whose halo does not fit
-    streams instead), from 20 on through the cp.async pipeline.  Iterations,
-    the residual and every bit of the solution equal the restatement's."""
+    streams instead), from 20 on through the cp.async pipeline; float or
+    double-single dot products.  Iterations, the residual and every bit of
+    the solution equal the restatement's."""
     import torch
 
     import fluid_simulation_gb300 as fsg
@@ -138,11 +140,13 @@ def test_gpu_large_system_forms_match_restatement(case, make, n_fluid, per_cta, 
         assert (-(-n_fluid // 1024) + sms - 1) // sms == per_cta
     ps = fsg.PoissonSolver(nx, ny, float(nx), float(ny))
     ps.set_problem(labels, rhs)
-    st = ps.solve(0, tol, maxit)
+    st = ps.solve(0, tol, maxit, inner_precision=precision)
     x = ps.solution()
     ps.close()
-    xo, so = po.poisson_solve(labels, rhs, float(nx), float(ny), 0, tol, maxit)
-    assert st["inner_iterations"] == so["inner_iterations"] == iters
+    xo, so = po.poisson_solve(labels, rhs, float(nx), float(ny), 0, tol, maxit, inner_precision=precision)
+    if precision == 0:
+        assert st["inner_iterations"] == so["inner_iterations"] == iters
+    assert st["inner_iterations"] == so["inner_iterations"]
     assert st["residual"] == so["residual"]
     assert np.array_equal(x.view(np.uint64), xo.view(np.uint64))
 
