@@ -70,6 +70,12 @@ def test_batch_rejects_simulations_beyond_its_limits():
     with pytest.raises(fsg.FsError) as e:
         fsg.FluidBatch([])
     assert e.value.code == 1
+    # double-single dot products are a handle and Poisson option only
+    lib.fs_config_init(fsg.C.byref(cfg), 64, 64)
+    cfg.cg_precision = fsg.CG_DS
+    with pytest.raises(fsg.FsError) as e:
+        fsg.FluidBatch([cfg])
+    assert e.value.code == 1 and "double-single" in str(e.value)
 
 
 @pytest.mark.gpu
