@@ -552,7 +552,6 @@ int step_state(fs_smoke* s, void* const* in, void* const* out)
 int adjoint_step(fs_smoke* s, void* const* state_n)
 {
     const unsigned nb = nblocks(s->n);
-    const size_t bytes = 8 * (size_t)s->n;
     // projection (symmetric with the wall condition): lam_uv <- M lam_uv
     k_close_faces<<<nb, TPB, 0, s->stream>>>(s->nx, s->ny, s->labels, s->lam[0], s->lam[1]);
     k_divergence<double><<<nb, TPB, 0, s->stream>>>(s->nx, s->ny, s->h, s->labels, s->lam[0], s->lam[1], s->rhs);
@@ -564,7 +563,6 @@ int adjoint_step(fs_smoke* s, void* const* state_n)
     k_subtract_gradient<double><<<nb, TPB, 0, s->stream>>>(s->nx, s->ny, s->h, s->labels, s->pres, s->lam[0], s->lam[1]);
     s->launches += 1;
     // advection: contribution items, grouped by node, summed in item order
-    (void)bytes;
     const Items items{s->item_key, s->item_val, s->n};
     if (s->fp64)
         k_advect_adjoint<double, double><<<nb, TPB, 0, s->stream>>>(fields<double>(s, state_n), s->labels,
