@@ -265,3 +265,26 @@ def test_restated_float_cg_against_scipy_cg():
     xr = x[fluid]
     assert np.linalg.norm(xr - xd) / np.linalg.norm(xd) < 1e-4
     assert np.linalg.norm(xs - xd) / np.linalg.norm(xd) < 1e-4
+
+
+def test_bench_fp64_checks_agree_with_the_assembled_system():
+    """bench.py's host-side FP64 checks of the projection forms: the
+    matrix-free residual equals the assembled sparse system's, and the direct
+    solve satisfies it to round-off."""
+    import importlib.util
+    import os
+
+    spec = importlib.util.spec_from_file_location(
+        "bench_mod", os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "bench.py"))
+    bench = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(bench)
+    labels, rhs = scenes.projection_problem(64, seed=9)
+    A, b, fluid = _system(labels, rhs)
+    rng = np.random.default_rng(4)
+    x = np.where(fluid, rng.standard_normal(labels.shape), 0.0)
+    ref = np.linalg.norm(b - A @ x[fluid]) / np.linalg.norm(b)
+    assert abs(bench.fp64_residual(labels, rhs, x) - ref) <= 1e-12 * ref
+    xd, cidx, nc = bench.fp64_direct_solution(labels, rhs)
+    xs = np.zeros(labels.shape)
+    xs[fluid] = xd
+    assert bench.fp64_residual(labels, rhs, xs) < 1e-12
