@@ -173,7 +173,8 @@ def parse():
     ap.add_argument("--batch", type=int, default=512, help="members of the batched form")
     ap.add_argument("--projection-size", type=int, default=4096, help="grid side of the mixed-precision form")
     ap.add_argument("--projection-methods", default="mixed_multigrid,mixed_f32_dots,mixed_ds_dots,mixed_f64_dots,fp64",
-                    help="solves of the mixed-precision form, in order (also fp32: the step's Jacobi CG alone)")
+                    help="solves of the mixed-precision form, in order (also fp32: the step's Jacobi CG alone, "
+                         "and fp32_ds_dots: the same with double-single dots)")
     ap.add_argument("--projection-max-iterations", type=int, default=200000,
                     help="CG iteration cap of each projection solve (a small cap makes a short profiling case)")
     ap.add_argument("--batch-plan", type=int, choices=[1, 2, 4, 8], default=None,
@@ -499,7 +500,8 @@ def measure_projection(args, local_rank):
                "mixed_f64_dots": (fsg.POISSON_MIXED, fsg.CG_DOUBLE),
                "mixed_ds_dots": (fsg.POISSON_MIXED, fsg.CG_DS),
                "fp64": (fsg.POISSON_FP64, fsg.CG_FLOAT),
-               "fp32": (fsg.POISSON_FP32, fsg.CG_FLOAT)}
+               "fp32": (fsg.POISSON_FP32, fsg.CG_FLOAT),
+               "fp32_ds_dots": (fsg.POISSON_FP32, fsg.CG_DS)}
     sols = {}
     for name in args.projection_methods.split(","):
         method, inner = methods[name]
