@@ -560,6 +560,7 @@ int fs_create(const fs_config* cfg, fs_handle** out)
     A(dalloc(&h->scan_tmp, scan_tmp_ints(ncell + 2)));
     for (auto& ev : h->ev) A(cudaEventCreate(&ev));
     h->cg.max_cells = ncell;
+    if (h->cg.partials) h->cg.groups = h->cg.partials + 4 * max_chunks;  // the second half of partials
     if (ok && cg_prepare(h->cg, h->device) != 0) {
         ok = false;
         e = cudaErrorInvalidConfiguration;

@@ -16,13 +16,16 @@
 //     tree" (groups of 32 consecutive elements, s = 16..1: a[l] += a[l+s],
 //     repeated on the group results) -- a warp shuffle tree, then a tree over
 //     warps (one 1024-element chunk per CTA pass), then a tree over chunk
-//     partials that every CTA evaluates redundantly after a grid barrier.  The
-//     result does not depend on the launch shape.  Two precisions (template
-//     parameter R): float products, sums, alpha, beta and threshold -- the
-//     precision of the reference's Eigen VectorXf CG, and the default; or
-//     exact float*float products summed in double with alpha and beta rounded
-//     once to float.  GB300's FP64 rate is a small fraction of its FP32 rate,
-//     so the double variant costs FP64 issue slots in every reduction.
+//     partials that every CTA evaluates redundantly after a grid barrier
+//     (double trees over many chunks first divide their widest level among
+//     the CTAs, behind a second barrier).  The result does not depend on the
+//     launch shape.  Three precisions (template parameter R): float products,
+//     sums, alpha, beta and threshold -- the precision of the reference's
+//     Eigen VectorXf CG, and the default; exact float*float products summed
+//     in double with alpha and beta rounded once to float; or the same with
+//     the warp level in double-single pairs (DSD).  GB300's FP64 rate is a
+//     small fraction of its FP32 rate, so the double variants cost FP64 issue
+//     slots in every reduction.
 //
 // Per iteration there are two grid barriers (after p.q and after r.r, r.z).
 // The search direction p_new = z + beta p_old is not exchanged through a third
@@ -78,6 +81,8 @@ struct CgArgs
     float *x, *r, *z, *p, *q;  // fluid-index vectors (global)
     double* partials;          // [2 buffers][2 values][MAX chunks]
     int max_chunks;
+    double* groups;            // [2 buffers][2 values][max_groups] group partials, or null
+    int max_groups;
     unsigned* barrier;
     unsigned* status;
     CgResult* result;
@@ -93,6 +98,7 @@ struct Smem
         double lvlA[1024][2];
         float redf[32][32][2];
         float lvlAf[1024][2];
+        float2 redp[32][32][2];  // level-1 results as double-single pairs
     };
     union {
         double lvlB[32][2];
@@ -115,7 +121,9 @@ template <> struct Ar<float>
     static __device__ __forceinline__ float prod(float a, float b) { return fmul(a, b); }
     static __device__ __forceinline__ float ratio(float a, float b) { return fdiv(a, b); }
     static __device__ __forceinline__ float tiny() { return 1.17549435e-38f; }
-    static __device__ __forceinline__ float& red(Smem& s, int a, int b, int k) { return s.redf[a][b][k]; }
+    using Lv1 = float;
+    static __device__ __forceinline__ void put1(Smem& s, int a, int b, int k, float t) { s.redf[a][b][k] = t; }
+    static __device__ __forceinline__ float get1(Smem& s, int a, int b, int k) { return s.redf[a][b][k]; }
     static __device__ __forceinline__ float& lvlA(Smem& s, int a, int k) { return s.lvlAf[a][k]; }
     static __device__ __forceinline__ float& lvlB(Smem& s, int a, int k) { return s.lvlBf[a][k]; }
 };
@@ -128,7 +136,9 @@ template <> struct Ar<double>
     static __device__ __forceinline__ double prod(float a, float b) { return dmul((double)a, (double)b); }
     static __device__ __forceinline__ float ratio(double a, double b) { return (float)(a / b); }
     static __device__ __forceinline__ double tiny() { return 2.2250738585072014e-308; }
-    static __device__ __forceinline__ double& red(Smem& s, int a, int b, int k) { return s.red[a][b][k]; }
+    using Lv1 = double;
+    static __device__ __forceinline__ void put1(Smem& s, int a, int b, int k, double t) { s.red[a][b][k] = t; }
+    static __device__ __forceinline__ double get1(Smem& s, int a, int b, int k) { return s.red[a][b][k]; }
     static __device__ __forceinline__ double& lvlA(Smem& s, int a, int k) { return s.lvlA[a][k]; }
     static __device__ __forceinline__ double& lvlB(Smem& s, int a, int k) { return s.lvlB[a][k]; }
 };
@@ -137,11 +147,11 @@ template <> struct Ar<double>
 // as an unevaluated pair of floats (fmul, then fmaf for its rounding error),
 // the first tree level -- the 32 elements of one warp -- added in such pairs
 // (TwoSum of the high parts, then the error and both low parts added in float;
-// the pair is not renormalised between levels), converted to double exactly
-// at the warp's root, and every
-// level above in double, as FS_CG_DOUBLE.  The pairs carry about 48 bits, so
-// the sums stay close to FP64 while GB300's FP64 pipe, where the double
-// variant spends its time, does almost nothing per element.
+// the pair is not renormalised between levels), the warp's root pair turned
+// into a double (hi + lo, one double addition), and every level above in
+// double, as FS_CG_DOUBLE.  The pairs carry about 48 bits, so the sums stay
+// close to FP64 while GB300's FP64 pipe, where the double variant spends its
+// time, does almost nothing per element.
 struct ds
 {
     float hi, lo;
@@ -167,6 +177,20 @@ template <> struct Ar<DSD> : Ar<double>
 {
     using Elem = ds;
     static __device__ __forceinline__ ds prod(float a, float b) { return ds_prod(a, b); }
+    // A warp's root pair is kept as a pair and becomes a double where the
+    // level-2 tree reads 32 of them, one per lane: one conversion instruction
+    // per 32 warp trees instead of one per tree, on a pipe that does about two
+    // FP64 lanes per clock per SM.
+    using Lv1 = ds;
+    static __device__ __forceinline__ void put1(Smem& s, int a, int b, int k, ds t)
+    {
+        s.redp[a][b][k] = make_float2(t.hi, t.lo);
+    }
+    static __device__ __forceinline__ double get1(Smem& s, int a, int b, int k)
+    {
+        const float2 t = s.redp[a][b][k];
+        return dadd((double)t.x, (double)t.y);
+    }
 };
 template <typename R> using Acc = typename Ar<R>::Acc;
 template <typename R> using Elem = typename Ar<R>::Elem;
@@ -246,9 +270,9 @@ struct ClusterSync
     }
 };
 
-// The level-1 tree of one warp's elements, as an accumulation value.
+// The level-1 tree of one warp's elements (lane 0's value is the result).
 template <typename R>
-__device__ __forceinline__ Acc<R> elem_tree(Elem<R> v)
+__device__ __forceinline__ typename Ar<R>::Lv1 elem_tree(Elem<R> v)
 {
     if constexpr (std::is_same<R, DSD>::value) {
 #pragma unroll
@@ -256,7 +280,7 @@ __device__ __forceinline__ Acc<R> elem_tree(Elem<R> v)
             const ds o{__shfl_down_sync(0xffffffffu, v.hi, s), __shfl_down_sync(0xffffffffu, v.lo, s)};
             v = ds_add(v, o);
         }
-        return dadd((double)v.hi, (double)v.lo);
+        return v;
     } else {
         return warp_tree<R>(v);
     }
@@ -269,8 +293,8 @@ __device__ __forceinline__ void level1(const Elem<R> (&v)[NV], int slot, Smem& s
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
     for (int k = 0; k < NV; ++k) {
-        const Acc<R> t = elem_tree<R>(v[k]);
-        if (lane == 0) Ar<R>::red(sm, slot, warp, k) = t;
+        const typename Ar<R>::Lv1 t = elem_tree<R>(v[k]);
+        if (lane == 0) Ar<R>::put1(sm, slot, warp, k, t);
     }
 }
 
@@ -284,22 +308,22 @@ __device__ __forceinline__ void level2(const CgArgs& a, int buf, int chunk0, int
     if (warp < nslots) {
 #pragma unroll
         for (int k = 0; k < NV; ++k) {
-            const Acc<R> t = warp_tree<Acc<R>>(Ar<R>::red(sm, warp, lane, k));
+            const Acc<R> t = warp_tree<Acc<R>>(Ar<R>::get1(sm, warp, lane, k));
             if (lane == 0) __stcg(&part[((size_t)buf * 2 + k) * a.max_chunks + chunk0 + warp], t);
         }
     }
     __syncthreads();
 }
 
-// Levels 3+: every CTA reduces all chunk partials of buffer buf.
+// Levels 3+ of the tree over the nchunks values src[k * stride + e], in one CTA.
 template <typename R, int NV>
-__device__ __forceinline__ void reduce_all(const CgArgs& a, int buf, int nchunks, Smem& sm, Acc<R> (&out)[NV])
+__device__ __forceinline__ void tree_levels(const Acc<R>* src, size_t stride, int nchunks, Smem& sm,
+                                            Acc<R> (&out)[NV])
 {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const Acc<R>* src = reinterpret_cast<const Acc<R>*>(a.partials) + (size_t)buf * 2 * a.max_chunks;
     if (nchunks == 1) {
 #pragma unroll
-        for (int k = 0; k < NV; ++k) out[k] = __ldcg(&src[(size_t)k * a.max_chunks]);
+        for (int k = 0; k < NV; ++k) out[k] = __ldcg(&src[(size_t)k * stride]);
         return;
     }
     int n = (nchunks + 31) / 32;
@@ -311,7 +335,7 @@ __device__ __forceinline__ void reduce_all(const CgArgs& a, int buf, int nchunks
             const int e = warp * 32 + lane;
 #pragma unroll
             for (int k = 0; k < NV; ++k) {
-                const Acc<R> v = e < nchunks ? __ldcg(&src[(size_t)k * a.max_chunks + e]) : Acc<R>(0);
+                const Acc<R> v = e < nchunks ? __ldcg(&src[(size_t)k * stride + e]) : Acc<R>(0);
                 const Acc<R> t = warp_tree<Acc<R>>(v);
                 if (lane == 0) Ar<R>::lvlB(sm, warp, k) = t;
             }
@@ -332,7 +356,7 @@ __device__ __forceinline__ void reduce_all(const CgArgs& a, int buf, int nchunks
         const int e = g * 32 + lane;
 #pragma unroll
         for (int k = 0; k < NV; ++k) {
-            const Acc<R> v = e < nchunks ? __ldcg(&src[(size_t)k * a.max_chunks + e]) : Acc<R>(0);
+            const Acc<R> v = e < nchunks ? __ldcg(&src[(size_t)k * stride + e]) : Acc<R>(0);
             const Acc<R> t = warp_tree<Acc<R>>(v);
             if (lane == 0) Ar<R>::lvlA(sm, g, k) = t;
         }
@@ -364,6 +388,46 @@ __device__ __forceinline__ void reduce_all(const CgArgs& a, int buf, int nchunks
     if (inA) __syncthreads();  // lvlA shares storage with the next phase's level-1 results
 }
 
+// Levels 3+ over the chunk partials of buffer buf, after the barrier that
+// published them.  Every CTA evaluates the whole tree itself; when the tree is
+// double and its widest level (the group trees over 32 chunk partials each)
+// is wide, the CTAs first divide the group trees among themselves, publish
+// them behind one more barrier and evaluate only the levels above: the same
+// tree and the same operations, traded for one more exchange (~2.4 us)
+// against the group trees' FP64 work, which GB300 executes at about two
+// lanes per clock per SM (~40 ns per group and value in every CTA).
+// Returns false if a barrier gave up.
+constexpr int SPLIT_MIN = 64;  // group trees x values from which the CTAs divide them
+template <typename R, int NV, class Sync>
+__device__ __forceinline__ bool reduce_all(const CgArgs& a, int buf, int nchunks, Smem& sm, Acc<R> (&out)[NV],
+                                           Sync& sync)
+{
+    const Acc<R>* src = reinterpret_cast<const Acc<R>*>(a.partials) + (size_t)buf * 2 * a.max_chunks;
+    if constexpr (std::is_same<Acc<R>, double>::value && std::is_same<Sync, GridSync>::value) {
+        const int ngroups = (nchunks + 31) / 32;
+        if (a.groups && ngroups * NV >= SPLIT_MIN && sync.size() > 1) {
+            const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+            const int rank = sync.rank(), size = sync.size();
+            double* grp = a.groups + (size_t)buf * 2 * a.max_groups;
+            for (int g = rank + warp * size; g < ngroups; g += 32 * size) {
+                const int e = g * 32 + lane;
+#pragma unroll
+                for (int k = 0; k < NV; ++k) {
+                    const double v = e < nchunks ? __ldcg(&src[(size_t)k * a.max_chunks + e]) : 0.0;
+                    const double t = warp_tree<double>(v);
+                    if (lane == 0) __stcg(&grp[(size_t)k * a.max_groups + g], t);
+                }
+            }
+            __syncthreads();  // the CTA's group stores precede thread 0's release
+            if (!sync.barrier(a, sm)) return false;
+            tree_levels<R, NV>(grp, (size_t)a.max_groups, ngroups, sm, out);
+            return true;
+        }
+    }
+    tree_levels<R, NV>(src, (size_t)a.max_chunks, nchunks, sm, out);
+    return true;
+}
+
 // Levels 2+ when one CTA owns all of at most 32 chunks: one warp reduces each
 // chunk's 32 level-1 results and then the chunk partials, the same tree as
 // level2 + reduce_all (a lone chunk's partial is the result as it stands),
@@ -378,7 +442,7 @@ __device__ __forceinline__ void local_reduce(int nchunks, Smem& sm, Acc<R> (&out
         for (int k = 0; k < NV; ++k) {
             Acc<R> mine = Acc<R>(0);
             for (int s = 0; s < nchunks; ++s) {
-                Acc<R> t = warp_tree<Acc<R>>(Ar<R>::red(sm, s, lane, k));
+                Acc<R> t = warp_tree<Acc<R>>(Ar<R>::get1(sm, s, lane, k));
                 t = __shfl_sync(0xffffffffu, t, 0);
                 if (lane == s) mine = t;
             }
@@ -444,7 +508,7 @@ __device__ __forceinline__ void cg_stream(const CgArgs& a, Smem& sm, int nf, int
         local_reduce<R, 2>(nchunks, sm, red2);
     } else {
         if (!sync.barrier(a, sm)) return;
-        reduce_all<R, 2>(a, 0, nchunks, sm, red2);
+        if (!reduce_all<R, 2>(a, 0, nchunks, sm, red2, sync)) return;
     }
     const Acc<R> bb = red2[0];
     Acc<R> rz = red2[1];
@@ -488,7 +552,7 @@ __device__ __forceinline__ void cg_stream(const CgArgs& a, Smem& sm, int nf, int
             local_reduce<R, 1>(nchunks, sm, red1);
         } else {
             if (!sync.barrier(a, sm)) return;
-            reduce_all<R, 1>(a, 1, nchunks, sm, red1);
+            if (!reduce_all<R, 1>(a, 1, nchunks, sm, red1, sync)) return;
         }
         const float alpha = Ar<R>::ratio(rz, red1[0]);
 
@@ -523,7 +587,7 @@ __device__ __forceinline__ void cg_stream(const CgArgs& a, Smem& sm, int nf, int
             local_reduce<R, 2>(nchunks, sm, red2);
         } else {
             if (!sync.barrier(a, sm)) return;
-            reduce_all<R, 2>(a, 0, nchunks, sm, red2);
+            if (!reduce_all<R, 2>(a, 0, nchunks, sm, red2, sync)) return;
         }
         rr = red2[0];
         iters = it;
@@ -713,7 +777,10 @@ __device__ __forceinline__ void cg_pipe(const CgArgs& a, Smem& sm, unsigned char
         cp_wait_all();
         return;
     }
-    reduce_all<R, 2>(a, 0, nchunks, sm, red2);
+    if (!reduce_all<R, 2>(a, 0, nchunks, sm, red2, sync)) {
+        cp_wait_all();
+        return;
+    }
     const Acc<R> bb = red2[0];
     Acc<R> rz = red2[1];
     Acc<R> rr = bb;
@@ -792,7 +859,10 @@ __device__ __forceinline__ void cg_pipe(const CgArgs& a, Smem& sm, unsigned char
             cp_wait_all();
             return;
         }
-        reduce_all<R, 1>(a, 1, nchunks, sm, red1);
+        if (!reduce_all<R, 1>(a, 1, nchunks, sm, red1, sync)) {
+            cp_wait_all();
+            return;
+        }
         const float alpha = Ar<R>::ratio(rz, red1[0]);
 
         // ---- phase B: x += alpha p, r -= alpha q, z = M^-1 r; publish z, p; partial r.r, r.z
@@ -834,7 +904,10 @@ __device__ __forceinline__ void cg_pipe(const CgArgs& a, Smem& sm, unsigned char
             cp_wait_all();
             return;
         }
-        reduce_all<R, 2>(a, 0, nchunks, sm, red2);
+        if (!reduce_all<R, 2>(a, 0, nchunks, sm, red2, sync)) {
+            cp_wait_all();
+            return;
+        }
         rr = red2[0];
         iters = it;
         if (rr < thr) break;
@@ -1007,7 +1080,7 @@ __device__ __forceinline__ bool cg_lean(const CgArgs& a, Smem& sm, unsigned char
     } else {
         if (!sync.barrier(a, sm)) return true;
         prefetch(false);
-        reduce_all<R, 2>(a, 0, nchunks, sm, red2);
+        if (!reduce_all<R, 2>(a, 0, nchunks, sm, red2, sync)) return true;
     }
     const Acc<R> bb = red2[0];
     Acc<R> rz = red2[1];
@@ -1084,7 +1157,7 @@ __device__ __forceinline__ bool cg_lean(const CgArgs& a, Smem& sm, unsigned char
             local_reduce<R, 1>(nchunks, sm, red1);
         } else {
             if (!sync.barrier(a, sm)) return true;
-            reduce_all<R, 1>(a, 1, nchunks, sm, red1);
+            if (!reduce_all<R, 1>(a, 1, nchunks, sm, red1, sync)) return true;
         }
         const float alpha = Ar<R>::ratio(rz, red1[0]);
 
@@ -1119,7 +1192,7 @@ __device__ __forceinline__ bool cg_lean(const CgArgs& a, Smem& sm, unsigned char
         } else {
             if (!sync.barrier(a, sm)) return true;
             prefetch(true);
-            reduce_all<R, 2>(a, 0, nchunks, sm, red2);
+            if (!reduce_all<R, 2>(a, 0, nchunks, sm, red2, sync)) return true;
         }
         rr = red2[0];
         iters = it;
@@ -1258,6 +1331,8 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg_cluster(CgBatchArgs ba)
     a.q = ba.q + sy.co;
     a.partials = ba.partials + sy.part_off;
     a.max_chunks = sy.max_chunks;
+    a.groups = nullptr;
+    a.max_groups = 0;
     a.barrier = nullptr;
     a.status = ba.status;
     a.result = ba.result + sim;
@@ -1338,6 +1413,8 @@ void cg_solve(const Launch& L, CgWork& w, const int32_t* nfluid, const float* b,
     a.q = w.q;
     a.partials = w.partials;
     a.max_chunks = (int)((w.max_cells + CHUNK - 1) / CHUNK);
+    a.groups = w.groups;
+    a.max_groups = (a.max_chunks + 31) / 32;
     a.barrier = w.barrier;
     a.status = status;
     a.result = w.result;

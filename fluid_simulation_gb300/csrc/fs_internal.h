@@ -194,6 +194,7 @@ struct CgWork
 {
     float *x, *r, *z, *p, *q;
     double* partials;   // chunk partials of the reductions, [2 buffers][2 values][max chunks]
+    double* groups = nullptr;  // group partials, [2 buffers][2 values][ceil(max chunks / 32)], or null
     unsigned* barrier;  // arrival counter of the grid barrier, cleared before every solve
     CgResult* result;
     int32_t* route = nullptr;  // 2 ints: the fluid cells k_cg and the pipelined kernel take (large systems)

@@ -196,6 +196,8 @@ struct Cg64Args
     double *x, *r, *z, *p, *q;
     double* partials;  // [2 buffers][2 values][max chunks]
     int max_chunks;
+    double* groups;    // [2 buffers][2 values][max_groups] group partials, or null
+    int max_groups;
     unsigned* barrier;
     unsigned* status;
     CgResult* result;
@@ -212,28 +214,36 @@ struct Smem64
 };
 
 // Grid barrier + levels 3+ over all chunk partials of buffer buf (NV values).
+// When the group trees (32 chunk partials each) are many, the CTAs divide
+// them among themselves and publish them behind a second barrier, as the
+// float-vector CG's reduction does: the same tree, one more exchange, and a
+// fraction of the FP64 work in each CTA.
+constexpr int SPLIT_MIN64 = 64;  // group trees x values from which the CTAs divide them
 template <int NV>
 __device__ bool exchange64(const Cg64Args& a, int buf, int nchunks, unsigned& target, Smem64& sm, double (&out)[NV])
 {
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        int ok = 1;
-        target += gridDim.x;
-        red_release_add_u32(a.barrier, 1u);
-        if (!count_reached(ld_acquire_u32(a.barrier), target)) {
-            const uint64_t t0 = globaltimer_ns();
-            while (!count_reached(ld_acquire_u32(a.barrier), target)) {
-                if (globaltimer_ns() - t0 > WAIT_LIMIT_NS) {
-                    atomicOr(a.status, ST_TIMEOUT);
-                    ok = 0;
-                    break;
+    auto barrier = [&]() -> bool {
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            int ok = 1;
+            target += gridDim.x;
+            red_release_add_u32(a.barrier, 1u);
+            if (!count_reached(ld_acquire_u32(a.barrier), target)) {
+                const uint64_t t0 = globaltimer_ns();
+                while (!count_reached(ld_acquire_u32(a.barrier), target)) {
+                    if (globaltimer_ns() - t0 > WAIT_LIMIT_NS) {
+                        atomicOr(a.status, ST_TIMEOUT);
+                        ok = 0;
+                        break;
+                    }
                 }
             }
+            sm.flag = ok;
         }
-        sm.flag = ok;
-    }
-    __syncthreads();
-    if (!sm.flag) return false;
+        __syncthreads();
+        return sm.flag != 0;
+    };
+    if (!barrier()) return false;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const double* src = a.partials + (size_t)buf * 2 * a.max_chunks;
     if (nchunks == 1) {
@@ -242,12 +252,27 @@ __device__ bool exchange64(const Cg64Args& a, int buf, int nchunks, unsigned& ta
         return true;
     }
     const int n3 = (nchunks + 31) / 32;
-    for (int g = warp; g < n3; g += 32) {
-        const int e = g * 32 + lane;
+    if (a.groups && n3 * NV >= SPLIT_MIN64 && gridDim.x > 1) {
+        double* grp = a.groups + (size_t)buf * 2 * a.max_groups;
+        for (int g = (int)blockIdx.x + warp * (int)gridDim.x; g < n3; g += 32 * (int)gridDim.x) {
+            const int e = g * 32 + lane;
 #pragma unroll
-        for (int k = 0; k < NV; ++k) {
-            const double t = warp_tree64(e < nchunks ? __ldcg(&src[(size_t)k * a.max_chunks + e]) : 0.0);
-            if (lane == 0) sm.lvlA[g][k] = t;
+            for (int k = 0; k < NV; ++k) {
+                const double t = warp_tree64(e < nchunks ? __ldcg(&src[(size_t)k * a.max_chunks + e]) : 0.0);
+                if (lane == 0) __stcg(&grp[(size_t)k * a.max_groups + g], t);
+            }
+        }
+        if (!barrier()) return false;
+        for (int i = threadIdx.x; i < n3 * NV; i += T)
+            sm.lvlA[i / NV][i % NV] = __ldcg(&grp[(size_t)(i % NV) * a.max_groups + i / NV]);
+    } else {
+        for (int g = warp; g < n3; g += 32) {
+            const int e = g * 32 + lane;
+#pragma unroll
+            for (int k = 0; k < NV; ++k) {
+                const double t = warp_tree64(e < nchunks ? __ldcg(&src[(size_t)k * a.max_chunks + e]) : 0.0);
+                if (lane == 0) sm.lvlA[g][k] = t;
+            }
         }
     }
     __syncthreads();
@@ -543,6 +568,8 @@ int solve_impl(fs_poisson* p, int method, double tol, int max_iterations, double
         a.q = p->cq;
         a.partials = p->cpart;
         a.max_chunks = (int)((p->ncell + T - 1) / T);
+        a.groups = p->cpart + 4 * (size_t)a.max_chunks;
+        a.max_groups = (a.max_chunks + 31) / 32;
         a.barrier = p->barrier64;
         a.status = p->status;
         a.result = p->result64;
@@ -671,13 +698,13 @@ FS_API int fs_poisson_create(int size_x, int size_y, float length_x, float lengt
     for (double** d : {&p->rhs, &p->b, &p->x, &p->r, &p->cx, &p->cr, &p->cz, &p->cp, &p->cq}) A((void**)d, 8 * N);
     A((void**)&p->part, 8 * max_chunks);
     A((void**)&p->scal, 8 * 4);
-    A((void**)&p->cpart, 8 * 4 * max_chunks);
+    A((void**)&p->cpart, 8 * 8 * max_chunks);  // chunk partials, then the group partials
     A((void**)&p->b32, 4 * N);
     A((void**)&p->status, 4);
     A((void**)&p->barrier64, 4);
     A((void**)&p->result64, sizeof(CgResult));
     for (float** f : {&p->cg.x, &p->cg.r, &p->cg.z, &p->cg.p, &p->cg.q}) A((void**)f, 4 * NP);
-    A((void**)&p->cg.partials, 8 * 4 * max_chunks);
+    A((void**)&p->cg.partials, 8 * 8 * max_chunks);  // chunk partials, then the group partials
     A((void**)&p->cg.barrier, 4);
     A((void**)&p->cg.result, sizeof(CgResult));
     A((void**)&p->cg.route, 8);
@@ -687,6 +714,7 @@ FS_API int fs_poisson_create(int size_x, int size_y, float length_x, float lengt
     if (e == cudaSuccess) e = cudaMemsetAsync(p->nfluid, 0, 4, p->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(p->stream);
     p->cg.max_cells = n;
+    if (p->cg.partials) p->cg.groups = p->cg.partials + 4 * max_chunks;
     if (e == cudaSuccess && cg_prepare(p->cg, device) != 0) e = cudaErrorInvalidConfiguration;
     if (e == cudaSuccess) {
         int sms = 0;

@@ -117,15 +117,18 @@ _LARGE_CASES = [
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("precision", [0, 2], ids=["float_dots", "ds_dots"])
+@pytest.mark.parametrize("precision", [0, 1, 2], ids=["float_dots", "double_dots", "ds_dots"])
 @pytest.mark.parametrize("case,make,n_fluid,per_cta,tol,maxit,iters", _LARGE_CASES, ids=[c[0] for c in _LARGE_CASES])
 def test_gpu_large_system_forms_match_restatement(case, make, n_fluid, per_cta, tol, maxit, iters, precision):
-    """Systems of more than 8 chunks of 1024 cells per CTA with float dot
-    products are solved by k_cg_large: up to 12 chunks per CTA in the
-    register-resident form with 4-byte rows (a CTA whose halo does not fit
-    streams instead), from 20 on through the cp.async pipeline; float or
-    double-single dot products.  Iterations, the residual and every bit of
-    the solution equal the restatement's."""
+    """Systems of more than 8 chunks of 1024 cells per CTA with float or
+    double-single dot products are solved by k_cg_large: up to 12 chunks per
+    CTA in the register-resident form with 4-byte rows (a CTA whose halo does
+    not fit streams instead), from 20 on through the cp.async pipeline; with
+    double dot products by k_cg's streaming form.  From 32 group trees of 32
+    chunk partials per reduction on (about 1M fluid cells for the two-value
+    reductions, 2M for the one-value ones), double and double-single trees
+    divide their group trees among the CTAs.  Iterations, the residual and
+    every bit of the solution equal the restatement's."""
     import torch
 
     import fluid_simulation_gb300 as fsg
@@ -147,6 +150,32 @@ def test_gpu_large_system_forms_match_restatement(case, make, n_fluid, per_cta, 
     if precision == 0:
         assert st["inner_iterations"] == so["inner_iterations"] == iters
     assert st["inner_iterations"] == so["inner_iterations"]
+    assert st["residual"] == so["residual"]
+    assert np.array_equal(x.view(np.uint64), xo.view(np.uint64))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("n,seed,tol,maxit", [(1280, 17, 1e-30, 40), (2048, 13, 1e-30, 40), (2048, 13, 0.1, 400)],
+                         ids=["1280_cut", "2048_cut", "2048_tolerance"])
+def test_gpu_fp64_cg_wide_reductions_match_restatement(n, seed, tol, maxit):
+    """The FP64 CG (method 1) on systems of 1.55M and 3.98M fluid cells,
+    whose reductions divide their group trees among the CTAs (from 32 groups
+    of 32 chunk partials for two values, 64 for one): iterations, residual
+    and every bit of the solution equal the restatement's."""
+    import fluid_simulation_gb300 as fsg
+    from fluid_simulation_gb300 import build as fsbuild
+
+    fsbuild.build()
+    labels, rhs = scenes.projection_problem(n, seed=seed)
+    ps = fsg.PoissonSolver(n, n, float(n), float(n))
+    ps.set_problem(labels, rhs)
+    st = ps.solve(1, tol, maxit)
+    x = ps.solution()
+    ps.close()
+    xo, so = po.poisson_solve(labels, rhs, float(n), float(n), 1, tol, maxit)
+    assert st["inner_iterations"] == so["inner_iterations"]
+    if tol < 1e-20:
+        assert st["inner_iterations"] == maxit
     assert st["residual"] == so["residual"]
     assert np.array_equal(x.view(np.uint64), xo.view(np.uint64))
 
