@@ -81,14 +81,14 @@ struct CgArgs
     float *x, *r, *z, *p, *q;  // fluid-index vectors (global)
     double* partials;          // [2 buffers][2 values][MAX chunks]
     int max_chunks;
-    double* groups;            // [2 buffers][2 values][max_groups] group partials, or null
-    int max_groups;
     unsigned* barrier;
     unsigned* status;
     CgResult* result;
     unsigned missing;          // arrivals the grid barrier waits for beyond the grid (test hook; normally 0)
     uint64_t wait_ns;          // bound of a barrier wait
     int dyn_bytes;             // dynamic shared memory of the launch
+    double* groups;            // [2 buffers][2 values][max_groups] group partials, or null
+    int max_groups;
 };
 
 struct Smem
@@ -315,15 +315,15 @@ __device__ __forceinline__ void level2(const CgArgs& a, int buf, int chunk0, int
     __syncthreads();
 }
 
-// Levels 3+ of the tree over the nchunks values src[k * stride + e], in one CTA.
+// Levels 3+: every CTA reduces all chunk partials of buffer buf.
 template <typename R, int NV>
-__device__ __forceinline__ void tree_levels(const Acc<R>* src, size_t stride, int nchunks, Smem& sm,
-                                            Acc<R> (&out)[NV])
+__device__ __forceinline__ void reduce_chunks(const CgArgs& a, int buf, int nchunks, Smem& sm, Acc<R> (&out)[NV])
 {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const Acc<R>* src = reinterpret_cast<const Acc<R>*>(a.partials) + (size_t)buf * 2 * a.max_chunks;
     if (nchunks == 1) {
 #pragma unroll
-        for (int k = 0; k < NV; ++k) out[k] = __ldcg(&src[(size_t)k * stride]);
+        for (int k = 0; k < NV; ++k) out[k] = __ldcg(&src[(size_t)k * a.max_chunks]);
         return;
     }
     int n = (nchunks + 31) / 32;
@@ -335,7 +335,7 @@ __device__ __forceinline__ void tree_levels(const Acc<R>* src, size_t stride, in
             const int e = warp * 32 + lane;
 #pragma unroll
             for (int k = 0; k < NV; ++k) {
-                const Acc<R> v = e < nchunks ? __ldcg(&src[(size_t)k * stride + e]) : Acc<R>(0);
+                const Acc<R> v = e < nchunks ? __ldcg(&src[(size_t)k * a.max_chunks + e]) : Acc<R>(0);
                 const Acc<R> t = warp_tree<Acc<R>>(v);
                 if (lane == 0) Ar<R>::lvlB(sm, warp, k) = t;
             }
@@ -356,7 +356,7 @@ __device__ __forceinline__ void tree_levels(const Acc<R>* src, size_t stride, in
         const int e = g * 32 + lane;
 #pragma unroll
         for (int k = 0; k < NV; ++k) {
-            const Acc<R> v = e < nchunks ? __ldcg(&src[(size_t)k * stride + e]) : Acc<R>(0);
+            const Acc<R> v = e < nchunks ? __ldcg(&src[(size_t)k * a.max_chunks + e]) : Acc<R>(0);
             const Acc<R> t = warp_tree<Acc<R>>(v);
             if (lane == 0) Ar<R>::lvlA(sm, g, k) = t;
         }
@@ -402,8 +402,8 @@ template <typename R, int NV, class Sync>
 __device__ __forceinline__ bool reduce_all(const CgArgs& a, int buf, int nchunks, Smem& sm, Acc<R> (&out)[NV],
                                            Sync& sync)
 {
-    const Acc<R>* src = reinterpret_cast<const Acc<R>*>(a.partials) + (size_t)buf * 2 * a.max_chunks;
     if constexpr (std::is_same<Acc<R>, double>::value && std::is_same<Sync, GridSync>::value) {
+        const double* src = a.partials + (size_t)buf * 2 * a.max_chunks;
         const int ngroups = (nchunks + 31) / 32;
         if (a.groups && ngroups * NV >= SPLIT_MIN && sync.size() > 1) {
             const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -420,11 +420,15 @@ __device__ __forceinline__ bool reduce_all(const CgArgs& a, int buf, int nchunks
             }
             __syncthreads();  // the CTA's group stores precede thread 0's release
             if (!sync.barrier(a, sm)) return false;
-            tree_levels<R, NV>(grp, (size_t)a.max_groups, ngroups, sm, out);
+            // the levels above, as reduce_chunks over the group partials
+            CgArgs ag = a;
+            ag.partials = a.groups;
+            ag.max_chunks = a.max_groups;
+            reduce_chunks<R, NV>(ag, buf, ngroups, sm, out);
             return true;
         }
     }
-    tree_levels<R, NV>(src, (size_t)a.max_chunks, nchunks, sm, out);
+    reduce_chunks<R, NV>(a, buf, nchunks, sm, out);
     return true;
 }
 
