@@ -147,11 +147,10 @@ struct Splat
     float v00, v10, v01, v11;
 };
 
-__device__ __forceinline__ Splat splat(const Geom& g, float gdx, float gdy, float x, float y, float value)
+// The footprint from the scaled position (xs, ys) = (x / gdx, y / gdy).
+__device__ __forceinline__ Splat splat_scaled(const Geom& g, float xs, float ys, float value)
 {
     Splat s;
-    const float xs = fdiv(x, gdx);
-    const float ys = fdiv(y, gdy);
     int i = trunc_i(xs);
     int j = trunc_i(ys);
     const int i1 = i + 1;
@@ -170,6 +169,11 @@ __device__ __forceinline__ Splat splat(const Geom& g, float gdx, float gdy, floa
     s.v01 = fmul(omi, value_1);
     s.v11 = fmul(i_frac, value_1);
     return s;
+}
+
+__device__ __forceinline__ Splat splat(const Geom& g, float gdx, float gdy, float x, float y, float value)
+{
+    return splat_scaled(g, fdiv(x, gdx), fdiv(y, gdy), value);
 }
 
 // Adds, in the reference's corner order 00, 10, 01, 11, the corners of s that

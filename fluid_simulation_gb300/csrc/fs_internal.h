@@ -91,6 +91,7 @@ struct SplatWork
     int32_t* bin_count = nullptr;  // cells + 2
     int32_t* bin_start = nullptr;  // cells + 2
     int32_t* scan_tmp = nullptr;
+    float *xs = nullptr, *ys = nullptr;  // scaled positions x / dx, y / dy of the valid items
     int64_t cap_items = 0;
     int64_t cells = 0;
 };

@@ -10,7 +10,9 @@
 // grid node gathers the items of the (up to) four base cells that can reach
 // it, merging the four item lists by item index.  Each node thus adds exactly
 // the same float terms in exactly the same order as the reference's
-// sequential loop, and the result is bit-identical.
+// sequential loop, and the result is bit-identical.  The key pass keeps each
+// item's scaled position (x / dx, y / dy), so that the four nodes of a
+// footprint do not repeat its two divisions.
 #include "fs_domain.cuh"
 
 namespace fs {
@@ -24,7 +26,8 @@ __global__ void __launch_bounds__(DOMAIN_TPB) k_splat_keys(Seg one, const Seg* _
                                                            int64_t n, uint32_t invalid, const float* __restrict__ x,
                                                            const float* __restrict__ y,
                                                            const uint8_t* __restrict__ valid,
-                                                           uint32_t* __restrict__ keys, int32_t* __restrict__ bin_count)
+                                                           uint32_t* __restrict__ keys, int32_t* __restrict__ bin_count,
+                                                           float* __restrict__ xs, float* __restrict__ ys)
 {
     const int64_t k = (int64_t)blockIdx.x * DOMAIN_TPB + threadIdx.x;
     if (k >= n) return;
@@ -41,8 +44,11 @@ __global__ void __launch_bounds__(DOMAIN_TPB) k_splat_keys(Seg one, const Seg* _
     const int64_t count = cells ? (int64_t)s.g.nx * s.g.ny : s.np;
     uint32_t key = invalid;
     if (local < count && (!valid || valid[k])) {
-        const Splat sp = splat(s.g, pool ? s.g.pdx : s.g.dx, pool ? s.g.pdy : s.g.dy, x[k], y[k], 0.0f);
+        const float sx = fdiv(x[k], pool ? s.g.pdx : s.g.dx), sy = fdiv(y[k], pool ? s.g.pdy : s.g.dy);
+        const Splat sp = splat_scaled(s.g, sx, sy, 0.0f);
         key = (uint32_t)(s.co + sp.i + (int64_t)sp.j * s.g.nx);
+        xs[k] = sx;
+        ys[k] = sy;
     }
     keys[k] = key;
     atomicAdd(&bin_count[key], 1);
@@ -110,8 +116,7 @@ __global__ void k_bin_sort(int64_t nbins, const int32_t* __restrict__ bin_start,
 // item index and adds the corners of each item's footprint that land on it.
 struct SplatGather
 {
-    bool pool;
-    const float *x, *y;
+    const float *xs, *ys;  // scaled positions
     int channels;
     const float *val0, *val1;
     const int32_t* bin_start;  // flattened cells + 2
@@ -120,7 +125,6 @@ struct SplatGather
     __device__ void operator()(const Seg& s, int64_t c, int a, int b) const
     {
         const Geom& g = s.g;
-        const float gdx = pool ? g.pdx : g.dx, gdy = pool ? g.pdy : g.dy;
         int cur[4], end[4];
         int nb = 0;
 #pragma unroll
@@ -154,11 +158,11 @@ struct SplatGather
                     ++cur[q];
                     head[q] = cur[q] < end[q] ? sorted[cur[q]] : INT32_MAX;
                 }
-            const float xi = x[best], yi = y[best];
-            const Splat s0 = splat(g, gdx, gdy, xi, yi, val0 ? val0[best] : 1.0f);
+            const float xi = xs[best], yi = ys[best];
+            const Splat s0 = splat_scaled(g, xi, yi, val0 ? val0[best] : 1.0f);
             acc0 = splat_accumulate(acc0, s0, a, b);
             if (channels > 1) {
-                const Splat s1 = splat(g, gdx, gdy, xi, yi, val1 ? val1[best] : 1.0f);
+                const Splat s1 = splat_scaled(g, xi, yi, val1 ? val1[best] : 1.0f);
                 acc1 = splat_accumulate(acc1, s1, a, b);
             }
         }
@@ -198,6 +202,8 @@ cudaError_t splat_alloc(SplatWork& w, int64_t items, int64_t cells)
     A((void**)&w.sorted, 4 * (size_t)items);
     A((void**)&w.bin_count, 4 * bins);
     A((void**)&w.bin_start, 4 * bins);
+    A((void**)&w.xs, 4 * (size_t)items);
+    A((void**)&w.ys, 4 * (size_t)items);
     A((void**)&w.scan_tmp, 4 * scan_tmp_ints((int64_t)bins));
     if (e != cudaSuccess) {
         splat_free(w);
@@ -210,7 +216,8 @@ cudaError_t splat_alloc(SplatWork& w, int64_t items, int64_t cells)
 
 void splat_free(SplatWork& w)
 {
-    for (void* p : {(void*)w.keys, (void*)w.sorted, (void*)w.bin_count, (void*)w.bin_start, (void*)w.scan_tmp})
+    for (void* p : {(void*)w.keys, (void*)w.sorted, (void*)w.bin_count, (void*)w.bin_start, (void*)w.scan_tmp,
+                    (void*)w.xs, (void*)w.ys})
         cudaFree(p);
     w = SplatWork{};
 }
@@ -227,7 +234,7 @@ void ordered_splat(const Launch& L, const Domain& d, bool items_are_cells, bool 
         const int2* blk = d.segs ? (items_are_cells ? d.cblk : d.pblk) : nullptr;
         k_splat_keys<<<domain_blocks(n), DOMAIN_TPB, 0, L.stream>>>(d.one, d.segs, blk, items_are_cells, pool_deltas,
                                                                      n, (uint32_t)ncell, x, y, valid, w.keys,
-                                                                     w.bin_count);
+                                                                     w.bin_count, w.xs, w.ys);
         L.count();
     }
     scan_exclusive_i32(L, w.bin_count, w.bin_start, ncell + 1, w.scan_tmp);
@@ -238,8 +245,8 @@ void ordered_splat(const Launch& L, const Domain& d, bool items_are_cells, bool 
         L.count(2);
     }
     each_cell(L, d,
-              SplatGather{pool_deltas, x, y, channels, values[0], channels > 1 ? values[1] : nullptr, w.bin_start,
-                          w.sorted, out[0], channels > 1 ? out[1] : nullptr});
+              SplatGather{w.xs, w.ys, channels, values[0], channels > 1 ? values[1] : nullptr, w.bin_start, w.sorted,
+                          out[0], channels > 1 ? out[1] : nullptr});
 }
 
 }  // namespace fs

@@ -1,0 +1,41 @@
+"""Device memory of a simulation handle against the budget stated for
+integrators: about 127 bytes per cell and 56 bytes per particle of capacity
+(the capacity doubles from 4096 as particles are added)."""
+import pytest
+
+import fluid_simulation_gb300 as fsg
+from fluid_simulation_gb300 import scenes
+
+CELL_BYTES = 127
+PARTICLE_BYTES = 56
+
+
+def capacity(n: int) -> int:
+    cap = 4096
+    while cap < n:
+        cap *= 2
+    return cap
+
+
+@pytest.mark.gpu
+def test_handle_device_memory_within_budget():
+    """fs_create + fs_set_particles of the 1024^2 benchmark workload, measured
+    as the drop in free device memory (cudaMalloc rounds each buffer up, so
+    the band is wide)."""
+    import torch
+
+    from fluid_simulation_gb300 import build as fsbuild
+
+    fsbuild.build()
+    sc = scenes.dam_break_large(1024)
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    sim = fsg.FluidSim.from_scene(sc)
+    torch.cuda.synchronize()
+    used = free0 - torch.cuda.mem_get_info()[0]
+    sim.close()
+    n = len(sc.particles)
+    budget = CELL_BYTES * sc.size_x * sc.size_y + PARTICLE_BYTES * capacity(n)
+    print(f"handle device memory: {used / 2**20:.1f} MiB measured, {budget / 2**20:.1f} MiB budgeted "
+          f"({sc.size_x}x{sc.size_y} cells, {n} particles, capacity {capacity(n)})")
+    assert 0.8 * budget <= used <= 1.1 * budget + (64 << 20), (used, budget)
