@@ -18,24 +18,25 @@ def capacity(n: int) -> int:
 
 
 @pytest.mark.gpu
-def test_handle_device_memory_within_budget():
-    """fs_create + fs_set_particles of the 1024^2 benchmark workload, measured
-    as the drop in free device memory (cudaMalloc rounds each buffer up, so
-    the band is wide)."""
+@pytest.mark.parametrize("n", [1024, 4096])
+def test_handle_device_memory_within_budget(n):
+    """fs_create + fs_set_particles of the benchmark's dam break at n^2 (1.7M
+    and 27.5M particles), measured as the drop in free device memory
+    (cudaMalloc rounds each buffer up, so the band is wide)."""
     import torch
 
     from fluid_simulation_gb300 import build as fsbuild
 
     fsbuild.build()
-    sc = scenes.dam_break_large(1024)
+    sc = scenes.dam_break_large(n)
     torch.cuda.synchronize()
     free0 = torch.cuda.mem_get_info()[0]
     sim = fsg.FluidSim.from_scene(sc)
     torch.cuda.synchronize()
     used = free0 - torch.cuda.mem_get_info()[0]
     sim.close()
-    n = len(sc.particles)
-    budget = CELL_BYTES * sc.size_x * sc.size_y + PARTICLE_BYTES * capacity(n)
+    npart = len(sc.particles)
+    budget = CELL_BYTES * sc.size_x * sc.size_y + PARTICLE_BYTES * capacity(npart)
     print(f"handle device memory: {used / 2**20:.1f} MiB measured, {budget / 2**20:.1f} MiB budgeted "
-          f"({sc.size_x}x{sc.size_y} cells, {n} particles, capacity {capacity(n)})")
+          f"({sc.size_x}x{sc.size_y} cells, {npart} particles, capacity {capacity(npart)})")
     assert 0.8 * budget <= used <= 1.1 * budget + (64 << 20), (used, budget)
