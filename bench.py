@@ -179,6 +179,8 @@ def parse():
                     help="CG iteration cap of each projection solve (a small cap makes a short profiling case)")
     ap.add_argument("--batch-plan", type=int, choices=[1, 2, 4, 8], default=None,
                     help="batched form: CG chunks per CTA instead of the autotuner's choice")
+    ap.add_argument("--batch-trajectory-steps", type=int, default=100,
+                    help="steps of the batched form's trajectory from its initial state (0: skip)")
     ap.add_argument("--handles-steps", type=int, default=5,
                     help="batched form: steps of the same members as plain handles, one after another (0: skip)")
     ap.add_argument("--trajectory-steps", type=int, default=500,
@@ -442,7 +444,47 @@ def measure_batched(args, local_rank, plain_value, flush):
                              "steps": nh, "handles_device_ms_per_step": h["device_ms"],
                              "handles_wall_ms_per_step": h["wall_ms"], "batch_ms_per_step_same_steps": batch_ms,
                              "speedup_device": h["device_ms"] / batch_ms, "speedup_wall": h["wall_ms"] / batch_ms}
+    if args.batch_trajectory_steps > 0:
+        out["trajectory"] = measure_batch_trajectory(sc, cells, args.batch_trajectory_steps, local_rank, flush)
     return out
+
+
+def measure_batch_trajectory(sc, cells, n, local_rank, flush):
+    """The batched configuration as it states it: n (100) steps of a fresh
+    batch from the members' initial states, per-step device time.  The cluster
+    plan is sized from fluid counts, which exist once a step has classified the
+    cells, so step 1 runs on the default plan; the tuner then runs (it leaves
+    the state as it found it, and its time is not a step's) and steps 2..n use
+    its choice.  Step 1 also captures the step's graph, and so does step 2 for
+    the new plan."""
+    import torch
+
+    import fluid_simulation_gb300 as fsg
+
+    b = fsg.FluidBatch.from_scenes(sc, device=local_rank)
+    stream = torch.cuda.ExternalStream(b.stream(), device=local_rank)
+    ms, itmax, tuned = [], {}, None
+    for k in range(n):
+        if k == 1:
+            tuned = b.tune(fsg.STEP_PICFLIP, 0.005, steps=2)
+        with torch.cuda.stream(stream):
+            flush.zero_()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+        b.step(fsg.STEP_PICFLIP, 0.005)
+        e1.record(stream)
+        b.synchronize()
+        ms.append(e0.elapsed_time(e1))
+        if k in (0, n // 2, n - 1):
+            itmax[k + 1] = max(b.stats(m)["cg_iterations"] for m in range(len(sc)))
+    b.close()
+    t = sum(ms) / 1000.0
+    return {"workload": "the batched workload, steps 1..%d from its initial state, tuned after step 1" % n,
+            "steps": n, "value": cells * n / t, "unit": UNIT, "ms_per_step": 1000.0 * t / n,
+            "ms_step_1": ms[0], "ms_per_step_after_first": float(np.mean(ms[1:])) if n > 1 else None,
+            "cg_plan_chunks_per_cta": tuned["chunks_per_cta"] if tuned else None,
+            "cg_iterations_max_at_step": itmax}
 
 
 def measure_handles(scs, pre_steps, steps, local_rank, flush):
