@@ -186,8 +186,9 @@ def parse():
     ap.add_argument("--trajectory-steps", type=int, default=500,
                     help="trajectory form: steps of the workload from its initial state (0: skip)")
     ap.add_argument("--phases-size", type=int, default=4096, help="grid side of the per-phase roofline form (0: skip)")
+    ap.add_argument("--smoke-size", type=int, default=256, help="grid side of the differentiable smoke form (0: skip)")
     ap.add_argument("--only-form", choices=["batched", "mixed_precision", "multigrid", "large_step", "trajectory",
-                                            "phases"], default=None,
+                                            "phases", "smoke"], default=None,
                     help="measure one form alone (profiling runs) and print its JSON object")
     return ap.parse_args()
 
@@ -691,6 +692,44 @@ def measure_trajectory(args, local_rank, flush, peak):
             "per_phase_roofline": per_phase_rows(bsum, phases, n, peak), "per_phase_model": PHASE_MODEL}
 
 
+def measure_smoke(args, local_rank):
+    """The differentiable-smoke form: --smoke-size (256)^2, a Gaussian blob in
+    seeded Fourier-mode velocity, 64 RK2 steps at dt = 0.01 with the mixed
+    projection to 1e-10 (FP64 refinement around Jacobi- or multigrid-
+    preconditioned float corrections), checkpoints every 8 steps; the forward
+    pass (loss) and the backward pass (gradient of the loss with respect to
+    the initial u, v and density, read back to the host), each timed by the
+    host clock after one untimed forward + backward."""
+    import fluid_simulation_gb300 as fsg
+    from fluid_simulation_gb300 import scenes
+
+    n, steps, dt = args.smoke_size, 64, 0.01
+    u, v, d, t = scenes.smoke_problem(n)
+    out = {"workload": "smoke %dx%d, Gaussian blob (sigma 20), Fourier-mode velocity k<=8, %d RK2 steps at dt=%g, "
+                       "projection to 1e-10, checkpoints every 8 steps" % (n, n, steps, dt)}
+    for name, prec, proj in (("fp32", fsg.SMOKE_FP32, fsg.POISSON_MIXED),
+                             ("fp32_trace64", fsg.SMOKE_FP32_TRACE64, fsg.POISSON_MIXED),
+                             ("fp64", fsg.SMOKE_FP64, fsg.POISSON_MIXED),
+                             ("fp32_trace64_multigrid", fsg.SMOKE_FP32_TRACE64, fsg.POISSON_MIXED_MG),
+                             ("fp64_multigrid", fsg.SMOKE_FP64, fsg.POISSON_MIXED_MG)):
+        sm = fsg.Smoke(n, n, dt=dt, integrator=fsg.INTEGRATOR_RK2, precision=prec, projection_method=proj,
+                       cg_tolerance=1e-10, checkpoint_every=8, device=local_rank)
+        sm.set_state(u, v, d)
+        sm.set_target(t)
+        sm.forward(steps)
+        sm.backward()
+        sm.set_state(u, v, d)
+        t0 = time.perf_counter()
+        loss = sm.forward(steps)
+        t1 = time.perf_counter()
+        sm.backward()
+        t2 = time.perf_counter()
+        sm.close()
+        out[name] = {"loss": loss, "forward_ms": 1000.0 * (t1 - t0), "backward_ms": 1000.0 * (t2 - t1),
+                     "forward_cell_steps_per_s": n * n * steps / (t1 - t0)}
+    return out
+
+
 def measure_phases(args, local_rank, flush, peak):
     """Per-phase roofline rows of the plain step on the dam break at
     --phases-size (4096^2: about 6.9M fluid cells and 27M particles): 2
@@ -788,6 +827,8 @@ def run_gpu(args, rank, world, local_rank):
                 out = measure_trajectory(args, local_rank, flush, peaks()[0])
             elif args.only_form == "phases":
                 out = measure_phases(args, local_rank, flush, peaks()[0])
+            elif args.only_form == "smoke":
+                out = measure_smoke(args, local_rank)
             else:
                 out = measure_projection(args, local_rank)
             print(json.dumps({"form": args.only_form, **out}), flush=True)
@@ -879,6 +920,8 @@ def run_gpu(args, rank, world, local_rank):
             forms["trajectory_500"] = measure_trajectory(args, local_rank, flush, peak)
         if args.phases_size > 0:
             forms["phases_4096"] = measure_phases(args, local_rank, flush, peak)
+        if args.smoke_size > 0:
+            forms["smoke"] = measure_smoke(args, local_rank)
     # roofline of the dominant kernel (the CG)
     cg_s = sum(cg_ms) / 1000.0
     achieved = CG_BYTES_PER_CELL_ITER * fi / cg_s / 1e9 if cg_s > 0 else None

@@ -661,7 +661,7 @@ int fs_smoke_create(const fs_smoke_config* cfg, fs_smoke** out)
         c.integrator < FS_INTEGRATOR_EULER || c.integrator > FS_INTEGRATOR_RK3 ||
         (c.precision != FS_SMOKE_FP32 && c.precision != FS_SMOKE_FP64 && c.precision != FS_SMOKE_FP32_TRACE64) ||
         c.checkpoint_every < 1 ||
-        c.projection_method < FS_POISSON_FP32 || c.projection_method > FS_POISSON_MIXED)
+        c.projection_method < FS_POISSON_FP32 || c.projection_method > FS_POISSON_MIXED_MG)
         return sfail(nullptr, FS_ERR_INVALID_ARGUMENT, "invalid smoke configuration");
     const double hx = (double)c.length_x / c.size_x, hy = (double)c.length_y / c.size_y;
     if (std::fabs(hx - hy) > 1e-12 * hx) return sfail(nullptr, FS_ERR_INVALID_ARGUMENT, "cells must be square");

@@ -403,7 +403,8 @@ FS_API int64_t fs_batch_kernel_launches(fs_batch* b);
  * and returns L = ||density - target||_2; fs_smoke_backward returns dL/d(the
  * initial u, v, density) from a hand-written adjoint, recomputing the states
  * between checkpoints stored every checkpoint_every steps.  Fields are float
- * or double on the device (precision); adjoints accumulate in double.  Host
+ * or double on the device (precision); adjoints are double, each node adding
+ * its contributions in a fixed order, so gradients repeat to the bit.  Host
  * arrays are size_x * size_y doubles, row-major: u(i, j) on the face at
  * (i h, (j + 1/2) h), v(i, j) at ((i + 1/2) h, j h), density at cell centres. */
 #define FS_INTEGRATOR_EULER 0
@@ -422,10 +423,10 @@ typedef struct fs_smoke_config
     float dt;
     int integrator;            /* FS_INTEGRATOR_* */
     int precision;             /* FS_SMOKE_FP32 / FS_SMOKE_FP64 / FS_SMOKE_FP32_TRACE64 */
-    int projection_method;     /* FS_POISSON_* */
+    int projection_method;     /* FS_POISSON_* (FS_POISSON_MIXED_MG: multigrid-preconditioned corrections) */
     double cg_tolerance;       /* relative residual of each projection */
     int cg_max_iterations;
-    double inner_tolerance;    /* FS_POISSON_MIXED: tolerance of each float correction */
+    double inner_tolerance;    /* FS_POISSON_MIXED(_MG): tolerance of each float correction */
     int checkpoint_every;      /* steps between stored states */
     int device;
     int reserved[8];
