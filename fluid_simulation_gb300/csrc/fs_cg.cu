@@ -151,25 +151,7 @@ template <> struct Ar<double>
 // into a double (hi + lo, one double addition), and every level above in
 // double, as FS_CG_DOUBLE.  The pairs carry about 48 bits, so the sums stay
 // close to FP64 while GB300's FP64 pipe, where the double variant spends its
-// time, does almost nothing per element.
-struct ds
-{
-    float hi, lo;
-};
-__device__ __forceinline__ ds ds_prod(float a, float b)
-{
-    const float p = fmul(a, b);
-    return ds{p, __fmaf_rn(a, b, -p)};
-}
-__device__ __forceinline__ ds ds_add(ds a, ds b)
-{
-    const float s = fadd(a.hi, b.hi);
-    const float v = fsub(s, a.hi);
-    float e = fadd(fsub(a.hi, fsub(s, v)), fsub(b.hi, v));
-    e = fadd(e, a.lo);
-    e = fadd(e, b.lo);
-    return ds{s, e};
-}
+// time, does almost nothing per element.  (ds, ds_prod, ds_add: fs_common.cuh.)
 struct DSD
 {
 };

@@ -35,6 +35,29 @@ __device__ __forceinline__ float fdiv(float a, float b) { return __fdiv_rn(a, b)
 __device__ __forceinline__ double dadd(double a, double b) { return __dadd_rn(a, b); }
 __device__ __forceinline__ double dmul(double a, double b) { return __dmul_rn(a, b); }
 
+// Double-single pairs: a float*float product exactly as an unevaluated sum
+// hi + lo (fmul, then fmaf for its rounding error), and pairs added with a
+// TwoSum of the high parts, the error and both low parts then added in float
+// (not renormalised).  About 48 bits in float arithmetic alone.
+struct ds
+{
+    float hi, lo;
+};
+__device__ __forceinline__ ds ds_prod(float a, float b)
+{
+    const float p = fmul(a, b);
+    return ds{p, __fmaf_rn(a, b, -p)};
+}
+__device__ __forceinline__ ds ds_add(ds a, ds b)
+{
+    const float s = fadd(a.hi, b.hi);
+    const float v = fsub(s, a.hi);
+    float e = fadd(fsub(a.hi, fsub(s, v)), fsub(b.hi, v));
+    e = fadd(e, a.lo);
+    e = fadd(e, b.lo);
+    return ds{s, e};
+}
+
 // C++ (int)x for float x: truncation toward zero.
 __device__ __forceinline__ int trunc_i(float x) { return __float2int_rz(x); }
 

@@ -248,15 +248,19 @@ __global__ void k_post1(Level F, Level C, const Scal* __restrict__ S)
 
 // Adds v over the block (fixed tree), stores the block partial and returns
 // true in the last block of the grid to do so, with the fixed-order sum of all
-// partials in *total (every thread of that block).
-__device__ __forceinline__ bool block_reduce(double v, double* __restrict__ part, unsigned* ticket, double* total)
+// partials in *total (every thread of that block).  Threads and warps add in
+// double-single pairs; each warp's pair becomes a double (hi + lo) once, and
+// the levels above are double.  GB300 executes FP64 at about two lanes per
+// clock per SM, where a double product and add per cell bound these kernels.
+__device__ __forceinline__ bool block_reduce(ds v, double* __restrict__ part, unsigned* ticket, double* total)
 {
     __shared__ double sh[32];
     __shared__ bool last;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
 #pragma unroll
-    for (int s = 16; s >= 1; s >>= 1) v += __shfl_down_sync(0xffffffffu, v, s);
-    if (lane == 0) sh[warp] = v;
+    for (int s = 16; s >= 1; s >>= 1)
+        v = ds_add(v, ds{__shfl_down_sync(0xffffffffu, v.hi, s), __shfl_down_sync(0xffffffffu, v.lo, s)});
+    if (lane == 0) sh[warp] = dadd((double)v.hi, (double)v.lo);
     __syncthreads();
     if (threadIdx.x == 0) {
         double b = 0.0;
@@ -298,11 +302,11 @@ __global__ void k_post2(Level L, const float* __restrict__ r0, double* __restric
 {
     if (S->done) return;
     const int n = L.nx * L.ny;
-    double v = 0.0;
+    ds v{0.0f, 0.0f};
     for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
         const float z = sweep_at(L.nbi[c], L.inv_h2, L.b[c], Around{L.tmp, c, L.nx});
         L.x[c] = z;
-        if (r0) v += (double)r0[c] * z;
+        if (r0) v = ds_add(v, ds_prod(r0[c], z));
     }
     if (!r0) return;  // uniform over the grid
     double rz;
@@ -437,12 +441,12 @@ __global__ void k_cg_init(Level L, const float* __restrict__ b, float* __restric
                           double* __restrict__ part, Scal* __restrict__ S, double tol, int maxit)
 {
     const int n = L.nx * L.ny;
-    double v = 0.0;
+    ds v{0.0f, 0.0f};
     for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
         const float rv = L.type[c] == LIQUID ? -b[c] : 0.0f;
         x[c] = 0.0f;
         r[c] = rv;
-        v += (double)rv * rv;
+        v = ds_add(v, ds_prod(rv, rv));
     }
     double bb;
     if (block_reduce(v, part, &S->ticket, &bb) && threadIdx.x == 0) {
@@ -467,7 +471,7 @@ __global__ void k_p_spmv(Level L, const float* __restrict__ z, float* __restrict
     const float beta = S->beta;
     const float* pold = S->cur ? p1 : p0;
     float* pnew = S->cur ? p0 : p1;
-    double v = 0.0;
+    ds v{0.0f, 0.0f};
     for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
         const uint8_t m = L.nbi[c];
         const Around zs{z, c, L.nx}, ps{pold, c, L.nx};
@@ -476,7 +480,7 @@ __global__ void k_p_spmv(Level L, const float* __restrict__ z, float* __restrict
         const float qc = liquid(m) ? neg_apply(m, L.inv_h2, pn) : 0.0f;
         pnew[c] = pc;
         q[c] = qc;
-        v += (double)pc * qc;
+        v = ds_add(v, ds_prod(pc, qc));
     }
     double pq;
     if (block_reduce(v, part, &S->ticket, &pq) && threadIdx.x == 0) {
@@ -493,12 +497,12 @@ __global__ void k_update_xr(int64_t n, const float* __restrict__ p0, const float
     if (S->done) return;
     const float* pnew = S->cur ? p0 : p1;
     const float a = S->alpha;
-    double v = 0.0;
+    ds v{0.0f, 0.0f};
     for (int64_t c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
         x[c] += a * pnew[c];
         const float rv = r[c] - a * q[c];
         r[c] = rv;
-        v += (double)rv * rv;
+        v = ds_add(v, ds_prod(rv, rv));
     }
     double rr;
     if (block_reduce(v, part, &S->ticket, &rr) && threadIdx.x == 0) {
