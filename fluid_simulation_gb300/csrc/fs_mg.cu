@@ -352,67 +352,75 @@ __global__ void __launch_bounds__(FUSED_THREADS, 1)
         for (int c = tid; c < n; c += FUSED_THREADS) B[0][c] = fu.lv[0].b[c];
     }
     __syncthreads();
-    // down: pre-smoothing and restriction
+    // down: pre-smoothing and restriction (each level's sizes and shared
+    // arrays held in registers for its loops)
     for (int k = 0; k + 1 < fu.n; ++k) {
-        const Level& L = fu.lv[k];
-        const int n = L.nx * L.ny;
-        for (int c = tid; c < n; c += FUSED_THREADS) T[k][c] = first_sweep(M[k][c], L.inv_h2, B[k][c]);
+        const int lnx = fu.lv[k].nx, lny = fu.lv[k].ny, cnx = fu.lv[k + 1].nx, cny = fu.lv[k + 1].ny;
+        const float inv_h2 = fu.lv[k].inv_h2;
+        float* const Xk = X[k];
+        float* const Tk = T[k];
+        float* const Bk = B[k];
+        float* const Bc = B[k + 1];
+        const uint8_t* const Mk = M[k];
+        const uint8_t* const Mc = M[k + 1];
+        const int n = lnx * lny;
+        for (int c = tid; c < n; c += FUSED_THREADS) Tk[c] = first_sweep(Mk[c], inv_h2, Bk[c]);
         __syncthreads();
-        for (int c = tid; c < n; c += FUSED_THREADS)
-            X[k][c] = sweep_at(M[k][c], L.inv_h2, B[k][c], Around{T[k], c, L.nx});
+        for (int c = tid; c < n; c += FUSED_THREADS) Xk[c] = sweep_at(Mk[c], inv_h2, Bk[c], Around{Tk, c, lnx});
         __syncthreads();
-        const Level& C = fu.lv[k + 1];
-        const int nc = C.nx * C.ny;
+        const int nc = cnx * cny;
         for (int c = tid; c < nc; c += FUSED_THREADS) {
             float s = 0.0f;
-            if (liquid(M[k + 1][c])) {
-                const int J = c / C.nx, I = c - J * C.nx;
+            if (liquid(Mc[c])) {
+                const int J = c / cnx, I = c - J * cnx;
                 for (int dj = 0; dj < 2; ++dj)
                     for (int di = 0; di < 2; ++di) {
                         const int i = 2 * I + di, j = 2 * J + dj;
-                        if (i >= L.nx || j >= L.ny) continue;
-                        const int f = i + j * L.nx;
-                        const uint8_t m = M[k][f];
-                        if (liquid(m)) s += B[k][f] - neg_apply(m, L.inv_h2, Around{X[k], f, L.nx});
+                        if (i >= lnx || j >= lny) continue;
+                        const int f = i + j * lnx;
+                        const uint8_t m = Mk[f];
+                        if (liquid(m)) s += Bk[f] - neg_apply(m, inv_h2, Around{Xk, f, lnx});
                     }
                 s = 0.25f * s;
             }
-            B[k + 1][c] = s;
+            Bc[c] = s;
         }
         __syncthreads();
     }
     // the coarsest level: COARSE_SWEEPS sweeps from 0
     {
         const int k = fu.n - 1;
-        const Level& L = fu.lv[k];
-        const int n = L.nx * L.ny;
-        for (int c = tid; c < n; c += FUSED_THREADS) X[k][c] = 0.0f;
+        const int lnx = fu.lv[k].nx, n = fu.lv[k].nx * fu.lv[k].ny;
+        const float inv_h2 = fu.lv[k].inv_h2;
+        float* const Xk = X[k];
+        float* const Tk = T[k];
+        const float* const Bk = B[k];
+        const uint8_t* const Mk = M[k];
+        for (int c = tid; c < n; c += FUSED_THREADS) Xk[c] = 0.0f;
         __syncthreads();
         for (int s = 0; s < COARSE_SWEEPS; ++s) {
-            const float* xin = (s & 1) ? T[k] : X[k];
-            float* xout = (s & 1) ? X[k] : T[k];
-            for (int c = tid; c < n; c += FUSED_THREADS)
-                xout[c] = sweep_at(M[k][c], L.inv_h2, B[k][c], Around{xin, c, L.nx});
+            const float* xin = (s & 1) ? Tk : Xk;
+            float* xout = (s & 1) ? Xk : Tk;
+            for (int c = tid; c < n; c += FUSED_THREADS) xout[c] = sweep_at(Mk[c], inv_h2, Bk[c], Around{xin, c, lnx});
             __syncthreads();
         }
         static_assert((COARSE_SWEEPS & 1) == 0, "the coarse result ends in X");
     }
     // up: prolongation and post-smoothing
     for (int k = fu.n - 2; k >= 0; --k) {
-        const Level& L = fu.lv[k];
-        const Level& C = fu.lv[k + 1];
-        const int n = L.nx * L.ny;
-        {
-            const float* x = X[k];
-            const float* xc = X[k + 1];
-            for (int c = tid; c < n; c += FUSED_THREADS) {
-                const int j = c / L.nx, i = c - j * L.nx;
-                T[k][c] = post1_at(M[k][c], i, j, L.nx, C.nx, L.inv_h2, B[k][c], x, xc);
-            }
+        const int lnx = fu.lv[k].nx, cnx = fu.lv[k + 1].nx, n = fu.lv[k].nx * fu.lv[k].ny;
+        const float inv_h2 = fu.lv[k].inv_h2;
+        float* const Xk = X[k];
+        float* const Tk = T[k];
+        const float* const Xc = X[k + 1];
+        const float* const Bk = B[k];
+        const uint8_t* const Mk = M[k];
+        for (int c = tid; c < n; c += FUSED_THREADS) {
+            const int j = c / lnx, i = c - j * lnx;
+            Tk[c] = post1_at(Mk[c], i, j, lnx, cnx, inv_h2, Bk[c], Xk, Xc);
         }
         __syncthreads();
-        for (int c = tid; c < n; c += FUSED_THREADS)
-            X[k][c] = sweep_at(M[k][c], L.inv_h2, B[k][c], Around{T[k], c, L.nx});
+        for (int c = tid; c < n; c += FUSED_THREADS) Xk[c] = sweep_at(Mk[c], inv_h2, Bk[c], Around{Tk, c, lnx});
         __syncthreads();
     }
     const int n0 = fu.lv[0].nx * fu.lv[0].ny;
