@@ -93,6 +93,9 @@ struct fs_handle
     int64_t n_part = 0, cap_part = 0;
 
     SplatWork sw{};
+    SplatWork sw2{};              // the v splats' scratch, beside the u splats on aux
+    cudaStream_t aux = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr;
 
     // pressure solve
     CgWork cg{};
@@ -173,7 +176,8 @@ void clear_graphs(fs_handle* h)
 cudaError_t ensure_splat_capacity(fs_handle* h, int64_t items)
 {
     if (items <= h->sw.cap_items) return cudaSuccess;
-    const cudaError_t e = splat_alloc(h->sw, items, h->ncell);
+    cudaError_t e = splat_alloc(h->sw, items, h->ncell);
+    if (e == cudaSuccess) e = splat_alloc(h->sw2, items, h->ncell);
     clear_graphs(h);
     return e;
 }
@@ -310,6 +314,10 @@ StepState state(fs_handle* h)
     st.yu = h->yu;
     st.xv = h->xv;
     st.sw = &h->sw;
+    st.sw2 = &h->sw2;
+    st.aux = h->aux;
+    st.fork = h->fork;
+    st.join = h->join;
     st.cg_b = h->cg_b;
     st.cg_down = h->cg_down;
     st.cg_up = h->cg_up;
@@ -368,6 +376,13 @@ void destroy_all(fs_handle* h)
                     h->cg_flags, h->d_nfluid, h->d_status, h->d_warn, h->scan_tmp};
     for (void* p : ptrs) cudaFree(p);
     splat_free(h->sw);
+    splat_free(h->sw2);
+    if (h->aux) {
+        cudaStreamSynchronize(h->aux);
+        cudaStreamDestroy(h->aux);
+    }
+    for (cudaEvent_t e : {h->fork, h->join})
+        if (e) cudaEventDestroy(e);
     mg_destroy(h->mg);
     cudaFree(h->mg_b);
     for (DevSource& src : h->sources) {
@@ -519,6 +534,9 @@ int fs_create(const fs_config* cfg, fs_handle** out)
     };
     A(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
     h->own_stream = true;
+    A(cudaStreamCreateWithFlags(&h->aux, cudaStreamNonBlocking));
+    A(cudaEventCreateWithFlags(&h->fork, cudaEventDisableTiming));
+    A(cudaEventCreateWithFlags(&h->join, cudaEventDisableTiming));
     for (int b = 0; b < 2; ++b) {
         A(dalloc(&h->u[b], N));
         A(dalloc(&h->v[b], N));

@@ -20,16 +20,44 @@ void ph_classify(const Launch& L, StepState& st, bool with_counts = false)
     labels_finalize(L, st.d, st.labels, st.solid);
 }
 
+// The two problems of a pair of splats (u faces, then v faces): u on L's
+// stream and v on the auxiliary one when the state has it (forked from and
+// joined back into L's stream, in a captured graph as outside one), else both
+// on L's stream.
+template <class U, class V>
+void splat_pair(const Launch& L, StepState& st, U u_problem, V v_problem)
+{
+    if (!st.sw2 || !st.aux) {
+        u_problem(L, *st.sw);
+        v_problem(L, *st.sw);
+        return;
+    }
+    cudaEventRecord(st.fork, L.stream);
+    cudaStreamWaitEvent(st.aux, st.fork, 0);
+    Launch La = L;
+    La.stream = st.aux;
+    u_problem(L, *st.sw);
+    v_problem(La, *st.sw2);
+    cudaEventRecord(st.join, st.aux);
+    cudaStreamWaitEvent(L.stream, st.join, 0);
+}
+
 // transferVelocityToGridSpread (src/FluidSolver.cpp:873-919), then the swap.
 void ph_p2g(const Launch& L, StepState& st)
 {
     p2g_positions(L, st.d, st.px, st.py, st.yu, st.xv);
-    const float* vu[2] = {st.pvx, nullptr};
-    float* ou[2] = {st.acc[0], st.acc[1]};
-    ordered_splat(L, st.d, false, true, st.px, st.yu, nullptr, 2, vu, ou, *st.sw);
-    const float* vv[2] = {st.pvy, nullptr};
-    float* ov[2] = {st.acc[2], st.acc[3]};
-    ordered_splat(L, st.d, false, true, st.xv, st.py, nullptr, 2, vv, ov, *st.sw);
+    splat_pair(
+        L, st,
+        [&](const Launch& Lu, SplatWork& w) {
+            const float* vu[2] = {st.pvx, nullptr};
+            float* ou[2] = {st.acc[0], st.acc[1]};
+            ordered_splat(Lu, st.d, false, true, st.px, st.yu, nullptr, 2, vu, ou, w);
+        },
+        [&](const Launch& Lv, SplatWork& w) {
+            const float* vv[2] = {st.pvy, nullptr};
+            float* ov[2] = {st.acc[2], st.acc[3]};
+            ordered_splat(Lv, st.d, false, true, st.xv, st.py, nullptr, 2, vv, ov, w);
+        });
     p2g_finish(L, st.d, st.acc[0], st.acc[1], st.acc[2], st.acc[3], st.UB(), st.VB());
     *st.front ^= 1;
 }
@@ -92,12 +120,18 @@ void ph_sl_velocity(const Launch& L, StepState& st, float dt)
 {
     sl_faces(L, st.d, st.labels, st.UF(), st.VF(), dt, st.sl[0], st.sl[1], st.sl[2], st.sl_ok[0], st.sl[3], st.sl[4],
              st.sl[5], st.sl_ok[1]);
-    const float* vu[1] = {st.sl[2]};
-    float* ou[1] = {st.UB()};
-    ordered_splat(L, st.d, true, false, st.sl[0], st.sl[1], st.sl_ok[0], 1, vu, ou, *st.sw);
-    const float* vv[1] = {st.sl[5]};
-    float* ov[1] = {st.VB()};
-    ordered_splat(L, st.d, true, false, st.sl[3], st.sl[4], st.sl_ok[1], 1, vv, ov, *st.sw);
+    splat_pair(
+        L, st,
+        [&](const Launch& Lu, SplatWork& w) {
+            const float* vu[1] = {st.sl[2]};
+            float* ou[1] = {st.UB()};
+            ordered_splat(Lu, st.d, true, false, st.sl[0], st.sl[1], st.sl_ok[0], 1, vu, ou, w);
+        },
+        [&](const Launch& Lv, SplatWork& w) {
+            const float* vv[1] = {st.sl[5]};
+            float* ov[1] = {st.VB()};
+            ordered_splat(Lv, st.d, true, false, st.sl[3], st.sl[4], st.sl_ok[1], 1, vv, ov, w);
+        });
 }
 
 }  // namespace

@@ -28,6 +28,11 @@ struct StepState
     uint8_t* sl_ok[2];
     float *px, *py, *pvx, *pvy, *yu, *xv;
     SplatWork* sw;
+    // With a second scratch, an auxiliary stream and two events, the v
+    // problem of each pair of splats runs on aux beside the u problem.
+    SplatWork* sw2 = nullptr;
+    cudaStream_t aux = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr;
     float* cg_b;
     int32_t *cg_down, *cg_up;
     uint8_t* cg_flags;
