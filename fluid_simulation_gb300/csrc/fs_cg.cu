@@ -269,10 +269,23 @@ __device__ __forceinline__ typename Ar<R>::Lv1 elem_tree(Elem<R> v)
 }
 
 // Level-1 (warp) tree of NV values for chunk slot `slot`; lane 0 keeps it.
+// Two float values go through one tree of packed adds (add.rn.f32x2: each
+// half rounded as its own fadd), the same sums with half the add instructions.
 template <typename R, int NV>
 __device__ __forceinline__ void level1(const Elem<R> (&v)[NV], int slot, Smem& sm)
 {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if constexpr (std::is_same<R, float>::value && NV == 2) {
+        float2 t = make_float2(v[0], v[1]);
+#pragma unroll
+        for (int s = 16; s >= 1; s >>= 1)
+            t = __fadd2_rn(t, make_float2(__shfl_down_sync(0xffffffffu, t.x, s), __shfl_down_sync(0xffffffffu, t.y, s)));
+        if (lane == 0) {
+            Ar<R>::put1(sm, slot, warp, 0, t.x);
+            Ar<R>::put1(sm, slot, warp, 1, t.y);
+        }
+        return;
+    }
 #pragma unroll
     for (int k = 0; k < NV; ++k) {
         const typename Ar<R>::Lv1 t = elem_tree<R>(v[k]);
