@@ -185,6 +185,26 @@ __device__ __forceinline__ R warp_tree(R v)
     return v;
 }
 
+// The warp trees of NV values in place; with PACK, two floats share one tree
+// of packed adds (add.rn.f32x2: each half rounded as its own fadd).  The
+// grid-synchronised kernels pack; in the cluster kernel the paired values
+// cost spills.
+template <typename A, int NV, bool PACK = true>
+__device__ __forceinline__ void warp_trees(A (&v)[NV])
+{
+    if constexpr (PACK && std::is_same<A, float>::value && NV == 2) {
+        float2 t = make_float2(v[0], v[1]);
+#pragma unroll
+        for (int s = 16; s >= 1; s >>= 1)
+            t = __fadd2_rn(t, make_float2(__shfl_down_sync(0xffffffffu, t.x, s), __shfl_down_sync(0xffffffffu, t.y, s)));
+        v[0] = t.x;
+        v[1] = t.y;
+    } else {
+#pragma unroll
+        for (int k = 0; k < NV; ++k) v[k] = warp_tree<A>(v[k]);
+    }
+}
+
 // Barrier over the active CTAs.  Thread 0 arrives with a release reduction on
 // the counter (bar.sync first makes the CTA's writes part of what it
 // releases) and spins with acquire loads; the closing bar.sync hands the
@@ -276,13 +296,11 @@ __device__ __forceinline__ void level1(const Elem<R> (&v)[NV], int slot, Smem& s
 {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     if constexpr (std::is_same<R, float>::value && NV == 2) {
-        float2 t = make_float2(v[0], v[1]);
-#pragma unroll
-        for (int s = 16; s >= 1; s >>= 1)
-            t = __fadd2_rn(t, make_float2(__shfl_down_sync(0xffffffffu, t.x, s), __shfl_down_sync(0xffffffffu, t.y, s)));
+        float t[2] = {v[0], v[1]};
+        warp_trees<float, 2>(t);
         if (lane == 0) {
-            Ar<R>::put1(sm, slot, warp, 0, t.x);
-            Ar<R>::put1(sm, slot, warp, 1, t.y);
+            Ar<R>::put1(sm, slot, warp, 0, t[0]);
+            Ar<R>::put1(sm, slot, warp, 1, t[1]);
         }
         return;
     }
@@ -294,25 +312,36 @@ __device__ __forceinline__ void level1(const Elem<R> (&v)[NV], int slot, Smem& s
 }
 
 // Level-2 trees for slots [0, nslots) -> chunk partials part[buf][k][chunk0 + slot].
-template <typename R, int NV>
+template <typename R, int NV, bool PACK = true>
 __device__ __forceinline__ void level2(const CgArgs& a, int buf, int chunk0, int nslots, Smem& sm)
 {
     __syncthreads();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     Acc<R>* part = reinterpret_cast<Acc<R>*>(a.partials);
     if (warp < nslots) {
+        if constexpr (PACK && std::is_same<Acc<R>, float>::value && NV == 2) {
+            Acc<R> t[NV];
 #pragma unroll
-        for (int k = 0; k < NV; ++k) {
-            const Acc<R> t = warp_tree<Acc<R>>(Ar<R>::get1(sm, warp, lane, k));
-            if (lane == 0) __stcg(&part[((size_t)buf * 2 + k) * a.max_chunks + chunk0 + warp], t);
+            for (int k = 0; k < NV; ++k) t[k] = Ar<R>::get1(sm, warp, lane, k);
+            warp_trees<Acc<R>, NV>(t);
+#pragma unroll
+            for (int k = 0; k < NV; ++k)
+                if (lane == 0) __stcg(&part[((size_t)buf * 2 + k) * a.max_chunks + chunk0 + warp], t[k]);
+        } else {
+#pragma unroll
+            for (int k = 0; k < NV; ++k) {
+                const Acc<R> t = warp_tree<Acc<R>>(Ar<R>::get1(sm, warp, lane, k));
+                if (lane == 0) __stcg(&part[((size_t)buf * 2 + k) * a.max_chunks + chunk0 + warp], t);
+            }
         }
     }
     __syncthreads();
 }
 
-// Levels 3+: every CTA reduces all chunk partials of buffer buf.
+// Levels 3+: every CTA reduces all chunk partials of buffer buf, one value
+// after the other.
 template <typename R, int NV>
-__device__ __forceinline__ void reduce_chunks(const CgArgs& a, int buf, int nchunks, Smem& sm, Acc<R> (&out)[NV])
+__device__ __forceinline__ void reduce_chunks_one(const CgArgs& a, int buf, int nchunks, Smem& sm, Acc<R> (&out)[NV])
 {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const Acc<R>* src = reinterpret_cast<const Acc<R>*>(a.partials) + (size_t)buf * 2 * a.max_chunks;
@@ -383,6 +412,91 @@ __device__ __forceinline__ void reduce_chunks(const CgArgs& a, int buf, int nchu
     if (inA) __syncthreads();  // lvlA shares storage with the next phase's level-1 results
 }
 
+// The same with the two values of a float reduction in packed trees (PACK),
+// else reduce_chunks_one.
+template <typename R, int NV, bool PACK = true>
+__device__ __forceinline__ void reduce_chunks(const CgArgs& a, int buf, int nchunks, Smem& sm, Acc<R> (&out)[NV])
+{
+    if constexpr (!(PACK && std::is_same<Acc<R>, float>::value && NV == 2)) {
+        reduce_chunks_one<R, NV>(a, buf, nchunks, sm, out);
+        return;
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const Acc<R>* src = reinterpret_cast<const Acc<R>*>(a.partials) + (size_t)buf * 2 * a.max_chunks;
+    if (nchunks == 1) {
+#pragma unroll
+        for (int k = 0; k < NV; ++k) out[k] = __ldcg(&src[(size_t)k * a.max_chunks]);
+        return;
+    }
+    int n = (nchunks + 31) / 32;
+    if (n <= 32) {
+        // group trees into lvlB, then every warp evaluates the tree over the
+        // groups itself (lvlB is not reused before the next reduction's
+        // group trees, so no trailing barrier)
+        if (warp < n) {
+            const int e = warp * 32 + lane;
+            Acc<R> t[NV];
+#pragma unroll
+            for (int k = 0; k < NV; ++k) t[k] = e < nchunks ? __ldcg(&src[(size_t)k * a.max_chunks + e]) : Acc<R>(0);
+            warp_trees<Acc<R>, NV>(t);
+#pragma unroll
+            for (int k = 0; k < NV; ++k)
+                if (lane == 0) Ar<R>::lvlB(sm, warp, k) = t[k];
+        }
+        __syncthreads();
+        if (n == 1) {
+#pragma unroll
+            for (int k = 0; k < NV; ++k) out[k] = Ar<R>::lvlB(sm, 0, k);
+        } else {
+            Acc<R> t[NV];
+#pragma unroll
+            for (int k = 0; k < NV; ++k) t[k] = lane < n ? Ar<R>::lvlB(sm, lane, k) : Acc<R>(0);
+            warp_trees<Acc<R>, NV>(t);
+#pragma unroll
+            for (int k = 0; k < NV; ++k) out[k] = __shfl_sync(0xffffffffu, t[k], 0);
+        }
+        return;
+    }
+    for (int g = warp; g < n; g += 32) {
+        const int e = g * 32 + lane;
+        Acc<R> t[NV];
+#pragma unroll
+        for (int k = 0; k < NV; ++k) t[k] = e < nchunks ? __ldcg(&src[(size_t)k * a.max_chunks + e]) : Acc<R>(0);
+        warp_trees<Acc<R>, NV>(t);
+#pragma unroll
+        for (int k = 0; k < NV; ++k)
+            if (lane == 0) Ar<R>::lvlA(sm, g, k) = t[k];
+    }
+    __syncthreads();
+    bool inA = true;
+    while (n > 1) {
+        const int m = (n + 31) / 32;
+        if (warp < m) {
+            const int e = warp * 32 + lane;
+            Acc<R> t[NV];
+#pragma unroll
+            for (int k = 0; k < NV; ++k) {
+                if (inA) t[k] = e < n ? Ar<R>::lvlA(sm, e, k) : Acc<R>(0);
+                else t[k] = e < n ? Ar<R>::lvlB(sm, e, k) : Acc<R>(0);
+            }
+            warp_trees<Acc<R>, NV>(t);
+#pragma unroll
+            for (int k = 0; k < NV; ++k) {
+                if (lane == 0) {
+                    if (inA) Ar<R>::lvlB(sm, warp, k) = t[k];
+                    else Ar<R>::lvlA(sm, warp, k) = t[k];
+                }
+            }
+        }
+        __syncthreads();
+        inA = !inA;
+        n = m;
+    }
+#pragma unroll
+    for (int k = 0; k < NV; ++k) out[k] = inA ? Ar<R>::lvlA(sm, 0, k) : Ar<R>::lvlB(sm, 0, k);
+    if (inA) __syncthreads();  // lvlA shares storage with the next phase's level-1 results
+}
+
 // Levels 3+ over the chunk partials of buffer buf, after the barrier that
 // published them.  Every CTA evaluates the whole tree itself; when the tree is
 // double and its widest level (the group trees over 32 chunk partials each)
@@ -423,7 +537,7 @@ __device__ __forceinline__ bool reduce_all(const CgArgs& a, int buf, int nchunks
             return true;
         }
     }
-    reduce_chunks<R, NV>(a, buf, nchunks, sm, out);
+    reduce_chunks<R, NV, std::is_same<Sync, GridSync>::value>(a, buf, nchunks, sm, out);
     return true;
 }
 
@@ -500,7 +614,7 @@ __device__ __forceinline__ void cg_stream(const CgArgs& a, Smem& sm, int nf, int
             }
             level1<R, 2>(v, sl, sm);
         }
-        if (!local) level2<R, 2>(a, 0, c0 + base, nslot, sm);
+        if (!local) level2<R, 2, std::is_same<Sync, GridSync>::value>(a, 0, c0 + base, nslot, sm);
     }
     Acc<R> red2[2];
     if (local) {
@@ -544,7 +658,7 @@ __device__ __forceinline__ void cg_stream(const CgArgs& a, Smem& sm, int nf, int
                 }
                 level1<R, 1>(v, sl, sm);
             }
-            if (!local) level2<R, 1>(a, 1, c0 + base, nslot, sm);
+            if (!local) level2<R, 1, std::is_same<Sync, GridSync>::value>(a, 1, c0 + base, nslot, sm);
         }
         Acc<R> red1[1];
         if (local) {
@@ -580,7 +694,7 @@ __device__ __forceinline__ void cg_stream(const CgArgs& a, Smem& sm, int nf, int
                 }
                 level1<R, 2>(v, sl, sm);
             }
-            if (!local) level2<R, 2>(a, 0, c0 + base, nslot, sm);
+            if (!local) level2<R, 2, std::is_same<Sync, GridSync>::value>(a, 0, c0 + base, nslot, sm);
         }
         if (local) {
             local_reduce<R, 2>(nchunks, sm, red2);
@@ -1072,7 +1186,7 @@ __device__ __forceinline__ bool cg_lean(const CgArgs& a, Smem& sm, unsigned char
             }
         }
     };
-    if (!local) level2<R, 2>(a, 0, c0, kb, sm);
+    if (!local) level2<R, 2, std::is_same<Sync, GridSync>::value>(a, 0, c0, kb, sm);
     Acc<R> red2[2];
     if (local) {
         local_reduce<R, 2>(nchunks, sm, red2);
@@ -1150,7 +1264,7 @@ __device__ __forceinline__ bool cg_lean(const CgArgs& a, Smem& sm, unsigned char
                 level1<R, 1>(v, s, sm);
             }
         }
-        if (!local) level2<R, 1>(a, 1, c0, kb, sm);
+        if (!local) level2<R, 1, std::is_same<Sync, GridSync>::value>(a, 1, c0, kb, sm);
         Acc<R> red1[1];
         if (local) {
             local_reduce<R, 1>(nchunks, sm, red1);
@@ -1185,7 +1299,7 @@ __device__ __forceinline__ bool cg_lean(const CgArgs& a, Smem& sm, unsigned char
                 level1<R, 2>(v, s, sm);
             }
         }
-        if (!local) level2<R, 2>(a, 0, c0, kb, sm);
+        if (!local) level2<R, 2, std::is_same<Sync, GridSync>::value>(a, 0, c0, kb, sm);
         if (local) {
             local_reduce<R, 2>(nchunks, sm, red2);
         } else {
