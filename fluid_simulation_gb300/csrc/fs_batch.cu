@@ -120,6 +120,7 @@ struct fs_batch
     std::vector<ClassPlan> plan;
     std::vector<int> plan_chunks;  // chunks each simulation's cluster is sized for
     int plan_target = 8;
+    bool counted = false;  // a step has counted every simulation's fluid cells
 
     int front = 0, vfront = 0;
     int n_ext = 2;
@@ -880,7 +881,9 @@ int fs_batch_step(fs_batch* b, int method, float dt)
         const cudaError_t e = ensure_sl_scratch(b);
         if (e != cudaSuccess) return cuda_fail(b, e, "semi-Lagrangian scratch");
     }
-    return step_graph(b, method, dt);
+    rc = step_graph(b, method, dt);
+    if (rc == FS_OK) b->counted = true;
+    return rc;
 }
 
 int fs_batch_synchronize(fs_batch* b)
@@ -918,7 +921,13 @@ int fs_batch_set_tuning(fs_batch* b, int chunks_per_cta)
     if (!b || (chunks_per_cta != 1 && chunks_per_cta != 2 && chunks_per_cta != 4 && chunks_per_cta != 8))
         return b ? fail(b, FS_ERR_INVALID_ARGUMENT, "chunks per CTA must be 1, 2, 4 or 8") : FS_ERR_INVALID_ARGUMENT;
     cudaSetDevice(b->device);
-    if (chunks_per_cta == b->plan_target) return FS_OK;
+    // after a step, plan for the fluid cells that step counted, as the tuner does
+    if (b->counted) {
+        const int rc = refresh_plan_chunks(b);
+        if (rc) return rc;
+    } else if (chunks_per_cta == b->plan_target) {
+        return FS_OK;
+    }
     return make_plan(b, chunks_per_cta);
 }
 

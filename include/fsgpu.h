@@ -385,6 +385,9 @@ FS_API int fs_batch_synchronize(fs_batch* b);
  * pressure solve (ms fields are 0). */
 FS_API int fs_batch_get_stats(fs_batch* b, int sim, fs_step_stats* out);
 FS_API int fs_batch_tune(fs_batch* b, int method, float dt, int steps, float* ms_out);
+/* Plans clusters of chunks_per_cta (1, 2, 4 or 8) chunks per CTA without
+ * timing: after a step, for the fluid cells that step counted (plus the
+ * tuner's 25% margin), before any step for each simulation's interior. */
 FS_API int fs_batch_set_tuning(fs_batch* b, int chunks_per_cta);
 FS_API int fs_batch_get_tuning(const fs_batch* b);
 FS_API int fs_batch_set_graphs(fs_batch* b, int enable);

@@ -174,9 +174,10 @@ def test_batch_validate_quirk_and_empty_members():
 
 @pytest.mark.gpu
 def test_batch_member_outgrowing_its_cluster_plan_stays_exact():
-    """The tuner sizes each member's cluster for its current fluid cells; a
-    member whose fluid then grows past that size solves from global memory,
-    with the same results."""
+    """A plan made after a step (here by fs_batch_set_tuning, as the tuner
+    does) sizes each member's cluster for its current fluid cells; a member
+    whose fluid then grows past that size solves from global memory, with the
+    same results."""
     fsbuild.build()
     sc = scenes.batch_scenes(n=3, seed=51, min_side=120, max_side=200)
     s0 = sc[0]
@@ -188,7 +189,7 @@ def test_batch_member_outgrowing_its_cluster_plan_stays_exact():
     b.step(fsg.STEP_PICFLIP, 0.005)
     for o in os_:
         o.step(po.STEP_PICFLIP, 0.005)
-    b.tune(fsg.STEP_PICFLIP, 0.005, steps=1)
+    b.set_tuning(8)  # after a step: sized for the fluid cells that step counted
     b.set_particles(0, s0.particles)
     os_[0].set_particles(s0.particles)
     for k in range(3):
