@@ -311,6 +311,18 @@ __device__ __forceinline__ void level1(const Elem<R> (&v)[NV], int slot, Smem& s
     }
 }
 
+// Level-1 trees of one float value of two slots at once (packed adds).
+__device__ __forceinline__ void level1_pair(float v0, float v1, int slot0, Smem& sm)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    float t[2] = {v0, v1};
+    warp_trees<float, 2>(t);
+    if (lane == 0) {
+        Ar<float>::put1(sm, slot0, warp, 0, t[0]);
+        Ar<float>::put1(sm, slot0 + 1, warp, 0, t[1]);
+    }
+}
+
 // Level-2 trees for slots [0, nslots) -> chunk partials part[buf][k][chunk0 + slot].
 template <typename R, int NV, bool PACK = true>
 __device__ __forceinline__ void level2(const CgArgs& a, int buf, int chunk0, int nslots, Smem& sm)
@@ -1229,11 +1241,16 @@ __device__ __forceinline__ bool cg_lean(const CgArgs& a, Smem& sm, unsigned char
             pv[OWN + h] = first ? zn : fadd(zn, fmul(beta, __ldcg(&a.p[n])));
         }
         __syncthreads();
+        // with float dots in a grid solve, the p.q trees of slots 2i and 2i + 1
+        // share one tree of packed adds (a slot past the CTA's range adds zeros
+        // into a level-1 entry nothing reads)
+        constexpr bool PAIR_A = std::is_same<R, float>::value && std::is_same<Sync, GridSync>::value && K % 2 == 0;
+        float held = 0.0f;
 #pragma unroll
         for (int s = 0; s < K; ++s) {
-            if (s < kb) {
+            if (PAIR_A || s < kb) {
                 Elem<R> v[1] = {Elem<R>()};
-                if ((c0 + s) * CHUNK + tid < nf) {
+                if (s < kb && (c0 + s) * CHUNK + tid < nf) {
                     const float ps = PREG ? pn[s] : pv[s * CHUNK + tid];
                     float acc = 0.0f;
                     if constexpr (NB4) {
@@ -1261,7 +1278,12 @@ __device__ __forceinline__ bool cg_lean(const CgArgs& a, Smem& sm, unsigned char
                     v[0] = Ar<R>::prod(ps, acc);
                     zq[s] = acc;
                 }
-                level1<R, 1>(v, s, sm);
+                if constexpr (PAIR_A) {
+                    if (s % 2 == 0) held = v[0];
+                    else if (s - 1 < kb) level1_pair(held, v[0], s - 1, sm);
+                } else {
+                    level1<R, 1>(v, s, sm);
+                }
             }
         }
         if (!local) level2<R, 1, std::is_same<Sync, GridSync>::value>(a, 1, c0, kb, sm);
