@@ -1241,10 +1241,10 @@ __device__ __forceinline__ bool cg_lean(const CgArgs& a, Smem& sm, unsigned char
             pv[OWN + h] = first ? zn : fadd(zn, fmul(beta, __ldcg(&a.p[n])));
         }
         __syncthreads();
-        // with float dots in a grid solve, the p.q trees of slots 2i and 2i + 1
-        // share one tree of packed adds (a slot past the CTA's range adds zeros
-        // into a level-1 entry nothing reads)
-        constexpr bool PAIR_A = std::is_same<R, float>::value && std::is_same<Sync, GridSync>::value && K % 2 == 0;
+        // with float dots, the p.q trees of slots 2i and 2i + 1 share one tree
+        // of packed adds (a slot past the CTA's range adds zeros into a level-1
+        // entry nothing reads)
+        constexpr bool PAIR_A = std::is_same<R, float>::value && K % 2 == 0;
         float held = 0.0f;
 #pragma unroll
         for (int s = 0; s < K; ++s) {
