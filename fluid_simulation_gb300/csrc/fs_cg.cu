@@ -290,8 +290,10 @@ __device__ __forceinline__ typename Ar<R>::Lv1 elem_tree(Elem<R> v)
 
 // Level-1 (warp) tree of NV values for chunk slot `slot`; lane 0 keeps it.
 // Two float values go through one tree of packed adds (add.rn.f32x2: each
-// half rounded as its own fadd), the same sums with half the add instructions.
-template <typename R, int NV>
+// half rounded as its own fadd), the same sums with half the add instructions;
+// with PACK_DS two double-single values likewise (the register-resident
+// forms spill with it, so only the pipelined form asks for it).
+template <typename R, int NV, bool PACK_DS = false>
 __device__ __forceinline__ void level1(const Elem<R> (&v)[NV], int slot, Smem& sm)
 {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -301,6 +303,29 @@ __device__ __forceinline__ void level1(const Elem<R> (&v)[NV], int slot, Smem& s
         if (lane == 0) {
             Ar<R>::put1(sm, slot, warp, 0, t[0]);
             Ar<R>::put1(sm, slot, warp, 1, t[1]);
+        }
+        return;
+    }
+    if constexpr (PACK_DS && std::is_same<R, DSD>::value && NV == 2) {
+        // both values' pairs in packed arithmetic: ds_add on each half, its
+        // subtractions as additions of the negation (exact in round-to-nearest)
+        auto sub2 = [](float2 x, float2 y) { return __fadd2_rn(x, make_float2(-y.x, -y.y)); };
+        float2 hi = make_float2(v[0].hi, v[1].hi), lo = make_float2(v[0].lo, v[1].lo);
+#pragma unroll
+        for (int s = 16; s >= 1; s >>= 1) {
+            const float2 ohi = make_float2(__shfl_down_sync(0xffffffffu, hi.x, s), __shfl_down_sync(0xffffffffu, hi.y, s));
+            const float2 olo = make_float2(__shfl_down_sync(0xffffffffu, lo.x, s), __shfl_down_sync(0xffffffffu, lo.y, s));
+            const float2 sum = __fadd2_rn(hi, ohi);
+            const float2 vv = sub2(sum, hi);
+            float2 e = __fadd2_rn(sub2(hi, sub2(sum, vv)), sub2(ohi, vv));
+            e = __fadd2_rn(e, lo);
+            e = __fadd2_rn(e, olo);
+            hi = sum;
+            lo = e;
+        }
+        if (lane == 0) {
+            Ar<R>::put1(sm, slot, warp, 0, ds{hi.x, lo.x});
+            Ar<R>::put1(sm, slot, warp, 1, ds{hi.y, lo.y});
         }
         return;
     }
@@ -1019,7 +1044,7 @@ __device__ __forceinline__ void cg_pipe(const CgArgs& a, Smem& sm, unsigned char
                 v[0] = Ar<R>::prod(r, r);
                 v[1] = Ar<R>::prod(r, z);
             }
-            level1<R, 2>(v, k & 31, sm);
+            level1<R, 2, true>(v, k & 31, sm);
             if ((k & 31) == 31 || k == kb - 1) level2<R, 2>(a, 0, c0 + (k & ~31), (k & 31) + 1, sm);
             ob_prev = ob;
             ob = wrap(ob, PB_ENTRY, B_END);
