@@ -284,6 +284,10 @@ class FluidSim:
     def set_graphs(self, on: bool) -> None:
         self._check(self.lib.fs_set_graphs(self.h, int(on)))
 
+    def set_stream(self, stream: int) -> None:
+        """Queue the handle's work on a caller's CUDA stream (a cudaStream_t as an int)."""
+        self._check(self.lib.fs_set_stream(self.h, C.c_void_p(stream)))
+
     # particles
     def set_particles(self, xyuv: np.ndarray) -> None:
         a = np.ascontiguousarray(xyuv, dtype=np.float32).reshape(-1, 4)

@@ -68,6 +68,27 @@ def test_step_methods_bit_exact(method):
         assert_same(g.state(), o.state(), where="method %d step %d" % (method, k))
 
 
+@pytest.mark.parametrize("graphs", [True, False], ids=["graph", "launches"])
+@pytest.mark.parametrize("method", [fsg.STEP_PICFLIP, fsg.STEP_SEMI_LAGRANGIAN])
+def test_steps_on_a_caller_stream_bit_exact(method, graphs):
+    """A handle whose work is queued on a stream the caller owns
+    (fs_set_stream), replayed through its graph or launched kernel by kernel:
+    each step forks its v splat onto the handle's second stream and joins it
+    back, and every result equals the oracle's."""
+    import torch
+
+    sc = scenes.dam_break_small()
+    g, o = pair(sc, cg_maxit=400)
+    s = torch.cuda.Stream()
+    g.set_stream(s.cuda_stream)
+    g.set_graphs(graphs)
+    for k in range(6):
+        g.step(method, sc.dt)
+        assert o.step(method, sc.dt) == 0
+        assert_same(g.state(), o.state(), where="method %d step %d" % (method, k))
+    g.close()  # before the caller's stream goes away
+
+
 @pytest.mark.parametrize("precision", [fsg.CG_FLOAT, fsg.CG_DOUBLE])
 def test_picflip_200_steps_bit_exact_with_graphs(precision):
     """The 64x64 dam break of the small configuration, 200 steps, replayed
