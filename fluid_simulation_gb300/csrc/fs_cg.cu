@@ -186,17 +186,19 @@ __device__ __forceinline__ R warp_tree(R v)
 }
 
 // The warp trees of NV values in place; with PACK, two floats share one tree
-// of packed adds (add.rn.f32x2: each half rounded as its own fadd).  The
-// grid-synchronised kernels pack; in the cluster kernel the paired values
-// cost spills.
+// of packed adds (add.rn.f32x2: each half rounded as its own fadd).  Level-1
+// trees pack in every kernel; level 2 and the cross-CTA reduction only in the
+// grid-synchronised ones (in the cluster kernel their paired values spill).
 template <typename A, int NV, bool PACK = true>
 __device__ __forceinline__ void warp_trees(A (&v)[NV])
 {
     if constexpr (PACK && std::is_same<A, float>::value && NV == 2) {
         float2 t = make_float2(v[0], v[1]);
 #pragma unroll
-        for (int s = 16; s >= 1; s >>= 1)
-            t = __fadd2_rn(t, make_float2(__shfl_down_sync(0xffffffffu, t.x, s), __shfl_down_sync(0xffffffffu, t.y, s)));
+        for (int s = 16; s >= 1; s >>= 1) {
+            const float2 o = make_float2(__shfl_down_sync(0xffffffffu, t.x, s), __shfl_down_sync(0xffffffffu, t.y, s));
+            t = __fadd2_rn(t, o);
+        }
         v[0] = t.x;
         v[1] = t.y;
     } else {
@@ -313,8 +315,10 @@ __device__ __forceinline__ void level1(const Elem<R> (&v)[NV], int slot, Smem& s
         float2 hi = make_float2(v[0].hi, v[1].hi), lo = make_float2(v[0].lo, v[1].lo);
 #pragma unroll
         for (int s = 16; s >= 1; s >>= 1) {
-            const float2 ohi = make_float2(__shfl_down_sync(0xffffffffu, hi.x, s), __shfl_down_sync(0xffffffffu, hi.y, s));
-            const float2 olo = make_float2(__shfl_down_sync(0xffffffffu, lo.x, s), __shfl_down_sync(0xffffffffu, lo.y, s));
+            const float2 ohi =
+                make_float2(__shfl_down_sync(0xffffffffu, hi.x, s), __shfl_down_sync(0xffffffffu, hi.y, s));
+            const float2 olo =
+                make_float2(__shfl_down_sync(0xffffffffu, lo.x, s), __shfl_down_sync(0xffffffffu, lo.y, s));
             const float2 sum = __fadd2_rn(hi, ohi);
             const float2 vv = sub2(sum, hi);
             float2 e = __fadd2_rn(sub2(hi, sub2(sum, vv)), sub2(ohi, vv));
